@@ -1,0 +1,325 @@
+"""Benchmark: PBF particle-steps/s at 1,048,576 particles (plain 4-iteration Jacobi form) on one GB300.
+
+A step is one PBF solver step (the reference's substep: predict + sort, 4 x (lambda, delta p), velocity +
+XSPH) over the 1M-particle scene (a 960 x 1024 lattice block plus a 65,536-particle splash, 20.48 x 20.48
+domain, h = 0.02, dt = 1/120). Inputs are resident in HBM when the timed region starts; L2 is flushed (a
+256 MiB memset) before every timed step, since the working set (~60 MB) would otherwise stay in the 129 MB
+L2 across steps.
+
+value: particle-steps/s through the graph-launched step (gpe_pbf_step), CUDA events on the launch stream.
+e2e:   the same metric through the C ABI with host buffers: per step set_state from pinned host memory,
+       one step, get_state back to pinned host memory, all inside the timed region.
+roofline: the dominant kernel (largest share of step time) timed per launch in a stage-by-stage pass with
+       CUDA events, against its algorithmic bytes per particle.
+cpu_baseline: the oracle's OpenMP FP64 restatement of the same step on a bounded sample, host cores.
+
+`--impl reference` times the reference's path on the host cores: the reference has no CPU implementation
+of its solver, so the oracle port stands in for it (kind "port").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "gpu-physics-engine_gb300"))
+sys.path.insert(0, str(ROOT))
+
+HBM_FALLBACK = 6800.0
+ALG_BYTES = {  # algorithmic bytes per particle per launch (FP32 SoA, each field read/written once)
+    "predict_sort": 36.0,  # read x, v; write x, x*, perm
+    "lambda": 12.0,        # read x*; write lambda
+    "delta_p": 20.0,       # read x*, lambda; write x*
+    "xsph": 24.0,          # read x, x*; write v
+}
+
+
+def peaks():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[2:6]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("GPE_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload():
+    from gpe import scenes
+
+    p = scenes.dam_params(iters=4)
+    pos, vel, boxes = scenes.million()
+    cfg = {"workload": "pbf_1m_plain_k4", "particles": int(len(pos)), "iters": 4, "h": 0.02,
+           "dt": "1/120", "domain": "20.48 x 20.48 (4 x 4 chunks of 5.12)", "cells": 1024 * 1024,
+           "scene": "960x1024 lattice block + 256x256 splash |v|~U(0,2), seed 2",
+           "l2": "flushed before every timed step (256 MiB memset)"}
+    return p, pos, vel, boxes, cfg
+
+
+def cpu_baseline(p, pos, vel, boxes, budget_s=12.0, max_steps=30):
+    from oracle import pyoracle
+
+    o = pyoracle.PbfOracle(p, boxes)
+    o.step(pos, vel, None, 1)  # warm-up (page-in, thread pool)
+    x, v = pos, vel
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < budget_s:
+        r = o.step(x, v, None, 1)
+        x, v = r["x"], r["v"]
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": len(pos) * steps / dt, "unit": "particle-steps/s", "cores": pyoracle.num_threads(),
+            "kind": "port",
+            "sample": f"{steps} full steps of the {len(pos)}-particle workload (FP64 oracle, OpenMP)"}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    p, pos, vel, boxes, cfg = workload()
+    from oracle import pyoracle
+
+    o = pyoracle.PbfOracle(p, boxes)
+    x, v = pos, vel
+    for _ in range(args.warmup):
+        r = o.step(x, v, None, 1)
+        x, v = r["x"], r["v"]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = o.step(x, v, None, 1)
+        x, v = r["x"], r["v"]
+    dt = time.perf_counter() - t0
+    val = len(pos) * args.steps / dt
+    line = {"metric": "pbf_particle_steps_per_s_1m", "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": pyoracle.num_threads(),
+                             "kind": "port",
+                             "sample": f"{args.steps} full steps of the {len(pos)}-particle workload; the "
+                                       "reference has no CPU solver, so its FP64 restatement stands in"},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpe(args, rank, ws):
+    import torch
+
+    import gpe
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    p, pos, vel, boxes, cfg = workload()
+    n = len(pos)
+    eng = gpe.Pbf(p, boxes, capacity=n)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    # pinned host buffers for the end-to-end leg
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_vel = torch.from_numpy(vel).pin_memory()
+    o_pos = torch.empty((n, 2), dtype=torch.float32).pin_memory()
+    o_vel = torch.empty((n, 2), dtype=torch.float32).pin_memory()
+
+    eng.set_state(pos, vel, stream=sh)
+    for _ in range(args.warmup):
+        eng.step(1, stream=sh)
+    torch.cuda.synchronize()
+
+    # ---- timed region: graph-launched steps ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        for a, b in ev:
+            flush_l2()
+            a.record(stream)
+            eng.step(1, stream=sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = allmax(sum(step_ms) / 1e3, ws)
+    value = ws * n * args.steps / total_s
+    dmax, dmean = eng.density_error(stream=sh)
+    launches = eng.launches_per_step()
+
+    # ---- stage-by-stage pass for the per-kernel roofline ----
+    stage_ms = {k: [] for k in ALG_BYTES}
+    stage_launches = {"predict_sort": 6, "lambda": 1, "delta_p": 1, "xsph": 1}
+    for _ in range(args.steps):
+        flush_l2()
+        seq = [("predict_sort", gpe.PBF_STAGE_PREDICT_SORT)]
+        for _ in range(p.iters):
+            seq += [("lambda", gpe.PBF_STAGE_LAMBDA), ("delta_p", gpe.PBF_STAGE_DELTA_P)]
+        seq += [("xsph", gpe.PBF_STAGE_XSPH)]
+        evs = []
+        for name, st in seq:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.stage(st, stream=sh)
+            b.record(stream)
+            evs.append((name, a, b))
+        eng.stage(gpe.PBF_STAGE_FINISH, stream=sh)
+        torch.cuda.synchronize()
+        for name, a, b in evs:
+            stage_ms[name].append(a.elapsed_time(b))
+    share = {k: sum(v) for k, v in stage_ms.items()}
+    tot = sum(share.values())
+    dom_name = max(share, key=lambda k: share[k])
+    per_launch_ms = statistics.mean(stage_ms[dom_name]) / stage_launches[dom_name]
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES[dom_name] * n / (per_launch_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": {"lambda": "k_lambda", "delta_p": "k_delta_p", "xsph": "k_xsph",
+                                           "predict_sort": "sort group"}[dom_name],
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": ALG_BYTES[dom_name] * n, "launch_ms": per_launch_ms,
+                "share": {k: v / tot for k, v in share.items()},
+                "stage_ms_per_step": {k: statistics.mean(v) for k, v in stage_ms.items()}}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    for a, b in e2e_ev:
+        flush_l2()
+        a.record(stream)
+        eng.set_state(h_pos.numpy(), h_vel.numpy(), stream=sh)
+        eng.step(1, stream=sh)
+        eng.get_state(o_pos.numpy(), o_vel.numpy(), stream=sh)
+        b.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = allmax(sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3, ws)
+    e2e = {"value": ws * n * args.steps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 16 * n,
+           "d2h_bytes_per_step": 16 * n}
+
+    if rank != 0:
+        return
+    base = None
+    if ws == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(p, pos, vel, boxes)
+    ms = 1e3 * total_s / args.steps
+    line = {"metric": "pbf_particle_steps_per_s_1m", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": cfg, "e2e": e2e, "roofline": roofline, "cpu_baseline": base,
+            "gpu_launches": launches * args.steps, "launches_per_step": launches,
+            "hbm_effective_gbs": 212.0 * value / ws / 1e9,
+            "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpe", choices=["gpe", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_gpe(args, rank, ws)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,67 @@
+// gpe_internal.h — shared host/device helpers of the engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/gpe.h"
+
+namespace gpe {
+
+// ----- error plumbing (thread-local, like the reference's last_error in cuda-render.cu:20-27) -----
+void set_error(int32_t status, const char* fmt, ...);
+void set_cuda_error(cudaError_t e, const char* what);
+void clear_error();
+
+#define GPE_TRY_CUDA(expr)                                                                                 \
+    do {                                                                                                   \
+        cudaError_t e_ = (expr);                                                                           \
+        if (e_ != cudaSuccess) {                                                                           \
+            ::gpe::set_cuda_error(e_, #expr);                                                              \
+            return GPE_ERR_CUDA;                                                                           \
+        }                                                                                                  \
+    } while (0)
+
+#define GPE_CHECK_LAUNCH(name)                                                                             \
+    do {                                                                                                   \
+        cudaError_t e_ = cudaGetLastError();                                                               \
+        if (e_ != cudaSuccess) {                                                                           \
+            ::gpe::set_cuda_error(e_, name);                                                               \
+            return GPE_ERR_CUDA;                                                                           \
+        }                                                                                                  \
+    } while (0)
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
+
+// Bump allocator over one device allocation (the reference carves each arena out of one cudaMalloc at
+// 128 B alignment, cuda-engine.cpp:14-29; 256 B here so every array can be a TMA or vector base).
+struct Carver {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count)
+    {
+        const size_t o = off;
+        off            = align_up(off + sizeof(T) * (count ? count : 1), 256);
+        return o;
+    }
+};
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int32_t current_device(int* dev);
+int32_t sm_count();
+
+// ----- counting sort of 32-bit keys (shared by PBF and the MPM spatial sort) -----
+// Workspace sizes for a sort of up to n_max items into n_keys buckets.
+size_t scan_blocks(uint32_t n_keys);
+// count[n_keys] -> start[n_keys+1] exclusive scan; zeroes count. bsum needs scan_blocks(n_keys) entries.
+int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, uint32_t* start,
+                              cudaStream_t st);
+// bucket[start[key] + rank] = i for every (key, rank) pair.
+int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket,
+                       cudaStream_t st);
+
+} // namespace gpe

@@ -1,0 +1,1047 @@
+// mpm.cu — MLS-MPM step on GB300 (sm_103a).
+//
+// The reference runs, per substep, resetGrid -> P2GKernel -> gridKernel -> G2PKernel (MPM.cu:353-371) with
+// 27 scalar global atomics per particle (MPM.cu:124-126) and a separate streaming pass over the grid.
+// Here one step is one launch after the first:
+//   k_p2g            P2G of the first step: each block accumulates its particles' 3x3 stencils in a
+//                    shared-memory node tile with shared atomics and flushes every touched node with one
+//                    vector global atomic (red.v4.f32) — particles are kept spatially sorted so a block's
+//                    stencils cover a small tile.
+//   k_g2p_p2g        G2P of step s fused with P2G of step s+1: the grid update (v = p/m + g dt, walls,
+//                    MPM.cu:150-175) is applied on the fly to each node the gather reads, the particle is
+//                    advanced and immediately scattered into the next grid, and the grid after that is
+//                    zeroed in the same launch (three grids rotate), so v and C never leave registers.
+//   k_g2p            G2P of the last step, writing the full particle state.
+// Stage kernels (k_clear, k_p2g, k_grid, k_g2p on an updated grid) reproduce the reference's four kernels
+// one to one for stage-level parity tests.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "gpe_internal.h"
+
+namespace gpe {
+
+struct MpmK {
+    float dx, inv_dx, goff, dt;
+    int32_t nx, ny;
+    float gdt_x, gdt_y;
+    float mass, vol0;
+    int32_t bc_type, bc_width;
+    float lo_x, lo_y, hi_x, hi_y, mid_x, mid_y;
+    int32_t material;
+    uint32_t flags;
+    float k_bulk, gamma, p_min, p_max, J_min, J_max;
+    float mu0, la0, theta_c, theta_s, hardening;
+    float apic_s; // 4 / dx^2
+    int32_t n;
+};
+
+namespace {
+
+constexpr int T_MPM     = 256;
+constexpr int TILE_CAP  = 2048; // nodes of the shared-memory accumulation tile (24 KB)
+
+enum MatMode { MODE_FLUID = 0, MODE_COROT = 1, MODE_SNOW = 2, MODE_MIXED = 3 };
+
+struct Stencil {
+    int32_t bx, by;
+    float fx, fy;
+    float wx[3], wy[3];
+};
+
+// quadratic B-spline weights, MPM.cu:92-110 (gridCoord MPM.cu:84)
+__device__ __forceinline__ Stencil stencil(const MpmK& k, float2 p, uint32_t* status)
+{
+    Stencil s;
+    const float gx = p.x * k.inv_dx + k.goff;
+    const float gy = p.y * k.inv_dx + k.goff;
+    int32_t bx     = (int32_t)floorf(gx - 0.5f);
+    int32_t by     = (int32_t)floorf(gy - 0.5f);
+    if (bx < 0 || by < 0 || bx > k.nx - 3 || by > k.ny - 3) {
+        // outside the halo: clamp the stencil to the grid and report it (the reference relies on its 2-node
+        // halo instead, MPM.cu:84 / cuda-engine.h:192-194)
+        atomicOr(status, GPE_STATUS_CAPACITY);
+        bx = min(max(bx, 0), k.nx - 3);
+        by = min(max(by, 0), k.ny - 3);
+    }
+    s.bx     = bx;
+    s.by     = by;
+    s.fx     = gx - (float)bx;
+    s.fy     = gy - (float)by;
+    s.wx[0]  = 0.5f * (1.5f - s.fx) * (1.5f - s.fx);
+    s.wx[1]  = 0.75f - (s.fx - 1.0f) * (s.fx - 1.0f);
+    s.wx[2]  = 0.5f * (s.fx - 0.5f) * (s.fx - 0.5f);
+    s.wy[0]  = 0.5f * (1.5f - s.fy) * (1.5f - s.fy);
+    s.wy[1]  = 0.75f - (s.fy - 1.0f) * (s.fy - 1.0f);
+    s.wy[2]  = 0.5f * (s.fy - 0.5f) * (s.fy - 0.5f);
+    return s;
+}
+
+__device__ __forceinline__ int mat_of(const MpmK& k, int mode, const int32_t* __restrict__ mat, int32_t i)
+{
+    return mode == MODE_MIXED ? __ldg(&mat[i]) : mode;
+}
+
+// rotation of the polar decomposition F = R S of a 2x2 matrix (row-major xx, xy, yx, yy)
+__device__ __forceinline__ float4 polar_rotation(float4 F)
+{
+    const float c = F.x + F.w, s = F.z - F.y;
+    const float n2 = c * c + s * s;
+    if (n2 < 1e-30f) { return make_float4(1.f, 0.f, 0.f, 1.f); }
+    const float in = rsqrtf(n2);
+    return make_float4(c * in, -s * in, s * in, c * in);
+}
+
+// Affine momentum Q = m C + coeff * Kirchhoff stress. Fluid: P2GKernel MPM.cu:68-80; elastic: fixed
+// corotated tau = 2 mu (F - R) F^T + la (J - 1) J I (Stomakhin et al. 2012), snow hardening exp(xi(1-Jp)).
+__device__ __forceinline__ float4 affine(const MpmK& k, int m, float4 Cp, float4 F, float J)
+{
+    if (m == MODE_FLUID) {
+        const float p_hat    = k.k_bulk * (powf(1.f / J, k.gamma) - 1.f);
+        const float pressure = fminf(fmaxf(p_hat, k.p_min), k.p_max);
+        const float V_p      = k.vol0 * J;
+        const float coeff    = -k.dt * V_p * 4 * k.inv_dx * k.inv_dx;
+        return make_float4(k.mass * Cp.x + coeff * -pressure, k.mass * Cp.y + coeff * 0.f,
+                           k.mass * Cp.z + coeff * 0.f, k.mass * Cp.w + coeff * -pressure);
+    }
+    float mu = k.mu0, la = k.la0;
+    if (m == MODE_SNOW) {
+        const float hf = __expf(k.hardening * (1.f - J));
+        mu *= hf;
+        la *= hf;
+    }
+    const float4 R  = polar_rotation(F);
+    const float Je  = F.x * F.w - F.y * F.z;
+    const float a0 = F.x - R.x, a1 = F.y - R.y, a2 = F.z - R.z, a3 = F.w - R.w;
+    const float vol = la * (Je - 1.f) * Je;
+    const float t0  = 2.f * mu * (a0 * F.x + a1 * F.y) + vol;
+    const float t1  = 2.f * mu * (a0 * F.z + a1 * F.w);
+    const float t2  = 2.f * mu * (a2 * F.x + a3 * F.y);
+    const float t3  = 2.f * mu * (a2 * F.z + a3 * F.w) + vol;
+    const float coeff = -k.dt * k.vol0 * 4.f * k.inv_dx * k.inv_dx;
+    return make_float4(k.mass * Cp.x + coeff * t0, k.mass * Cp.y + coeff * t1, k.mass * Cp.z + coeff * t2,
+                       k.mass * Cp.w + coeff * t3);
+}
+
+// node velocity as the reference's gridKernel leaves it (MPM.cu:150-175), from the raw accumulated node
+__device__ __forceinline__ float2 node_velocity(const MpmK& k, float4 g, int32_t x, int32_t y)
+{
+    if (!(g.z > 0.f)) { return make_float2(0.f, 0.f); }
+    const float inv_m = 1.f / g.z;
+    float vx          = g.x * inv_m + k.gdt_x;
+    float vy          = g.y * inv_m + k.gdt_y;
+    const bool wl = x <= k.bc_width, wr = x >= k.nx - 1 - k.bc_width;
+    const bool wb = y <= k.bc_width, wt = y >= k.ny - 1 - k.bc_width;
+    if (k.bc_type == GPE_MPM_BC_STICKY) {
+        if (wl || wr || wb || wt) { vx = vy = 0.f; }
+    } else {
+        if (wl && vx < 0.f) {
+            vx = 0.f;
+        } else if (wr && vx > 0.f) {
+            vx = 0.f;
+        }
+        if (wb && vy < 0.f) {
+            vy = 0.f;
+        } else if (wt && vy > 0.f) {
+            vy = 0.f;
+        }
+    }
+    return make_float2(vx, vy);
+}
+
+struct PState {
+    float2 x, v;
+    float4 C, F;
+    float J;
+};
+
+// 2x2 SVD through the polar decomposition: F = U diag(s) V^T with U, V rotations
+__device__ __forceinline__ void svd2(float4 F, float4& U, float2& s, float4& V)
+{
+    const float4 R = polar_rotation(F);
+    const float a  = R.x * F.x + R.z * F.z;
+    const float b  = R.x * F.y + R.z * F.w;
+    const float d  = R.y * F.y + R.w * F.w;
+    float c = 1.f, sn = 0.f;
+    if (fabsf(b) > 1e-30f) { sincosf(0.5f * atan2f(2.f * b, a - d), &sn, &c); }
+    V   = make_float4(c, -sn, sn, c);
+    s.x = c * c * a + 2.f * c * sn * b + sn * sn * d;
+    s.y = sn * sn * a - 2.f * c * sn * b + c * c * d;
+    U   = make_float4(R.x * V.x + R.y * V.z, R.x * V.y + R.y * V.w, R.z * V.x + R.w * V.z, R.z * V.y + R.w * V.w);
+}
+
+// G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301). RAW: the grid holds accumulated
+// momentum/mass and the node update is applied on the fly; otherwise it holds velocities.
+template <bool RAW>
+__device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, const float4* __restrict__ grid,
+                                         PState& ps, uint32_t* status)
+{
+    const Stencil s = stencil(k, ps.x, status);
+    float2 vel      = make_float2(0.f, 0.f);
+    float4 B        = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float w       = s.wx[i] * s.wy[j];
+            const float dpx     = ((float)i - s.fx) * k.dx;
+            const float dpy     = ((float)j - s.fy) * k.dx;
+            const int32_t nxi   = s.bx + i, nyj = s.by + j;
+            const float4 g      = __ldg(&grid[(size_t)nyj * (size_t)k.nx + (size_t)nxi]);
+            float2 vi;
+            if (RAW) {
+                vi = node_velocity(k, g, nxi, nyj);
+            } else {
+                vi = make_float2(g.x, g.y);
+            }
+            vel.x += w * vi.x;
+            vel.y += w * vi.y;
+            const float wvx = w * vi.x, wvy = w * vi.y;
+            B.x += wvx * dpx;
+            B.y += wvx * dpy;
+            B.z += wvy * dpx;
+            B.w += wvy * dpy;
+        }
+    }
+    float2 pos = make_float2(ps.x.x + vel.x * k.dt, ps.x.y + vel.y * k.dt);
+    ps.C       = make_float4(k.apic_s * B.x, k.apic_s * B.y, k.apic_s * B.z, k.apic_s * B.w);
+    // handleOOB
+    if (!isfinite(pos.x) || !isfinite(vel.x)) {
+        pos.x = k.mid_x;
+        vel.x = 0.f;
+        atomicOr(status, GPE_STATUS_NONFINITE);
+    }
+    if (!isfinite(pos.y) || !isfinite(vel.y)) {
+        pos.y = k.mid_y;
+        vel.y = 0.f;
+        atomicOr(status, GPE_STATUS_NONFINITE);
+    }
+    if (pos.x < k.lo_x) {
+        pos.x = k.lo_x;
+        vel.x = fmaxf(vel.x, 0.f);
+    }
+    if (pos.x > k.hi_x) {
+        pos.x = k.hi_x;
+        vel.x = fminf(vel.x, 0.f);
+    }
+    if (pos.y < k.lo_y) {
+        pos.y = k.lo_y;
+        vel.y = fmaxf(vel.y, 0.f);
+    }
+    if (pos.y > k.hi_y) {
+        pos.y = k.hi_y;
+        vel.y = fminf(vel.y, 0.f);
+    }
+    ps.x = pos;
+    ps.v = vel;
+    // F <- (I + dt C) F; J <- J det(I + dt C), clamped (MPM.cu:258-265)
+    const float4 A = make_float4(1 + ps.C.x * k.dt, ps.C.y * k.dt, ps.C.z * k.dt, 1 + ps.C.w * k.dt);
+    if (m != MODE_FLUID || track_f) {
+        const float4 F = ps.F;
+        ps.F           = make_float4(A.x * F.x + A.y * F.z, A.x * F.y + A.y * F.w, A.z * F.x + A.w * F.z,
+                                     A.z * F.y + A.w * F.w);
+    }
+    if (m == MODE_FLUID) {
+        float J = ps.J * (A.x * A.w - A.y * A.z);
+        ps.J    = fminf(fmaxf(J, k.J_min), k.J_max);
+    } else if (m == MODE_SNOW) {
+        float4 U, V;
+        float2 sg;
+        svd2(ps.F, U, sg, V);
+        const float lo = 1.f - k.theta_c, hi = 1.f + k.theta_s;
+        const float c0 = fminf(fmaxf(sg.x, lo), hi), c1 = fminf(fmaxf(sg.y, lo), hi);
+        ps.J *= (sg.x * sg.y) / (c0 * c1);
+        ps.F = make_float4(U.x * c0 * V.x + U.y * c1 * V.y, U.x * c0 * V.z + U.y * c1 * V.w,
+                           U.z * c0 * V.x + U.w * c1 * V.y, U.z * c0 * V.z + U.w * c1 * V.w);
+    }
+}
+
+// per-particle contribution for one stencil node (particleToGrid MPM.cu:116-126)
+__device__ __forceinline__ float4 node_contrib(const MpmK& k, const Stencil& s, float2 v, float4 Q, int i, int j)
+{
+    const float w   = s.wx[i] * s.wy[j];
+    const float dpx = ((float)i - s.fx) * k.dx;
+    const float dpy = ((float)j - s.fy) * k.dx;
+    const float ax  = dpx * Q.x + dpy * Q.y;
+    const float ay  = dpx * Q.z + dpy * Q.w;
+    return make_float4(w * (v.x * k.mass + ax), w * (v.y * k.mass + ay), w * k.mass, 0.f);
+}
+
+// Scatter of one block's particles through a shared-memory tile. All threads of the block must call it;
+// `valid` marks threads that carry a particle.
+__device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stencil& s, float2 v, float4 Q,
+                                          float4* __restrict__ grid)
+{
+    __shared__ float s_x[TILE_CAP], s_y[TILE_CAP], s_m[TILE_CAP];
+    __shared__ int32_t s_box[4];
+    if (threadIdx.x == 0) {
+        s_box[0] = INT32_MAX;
+        s_box[1] = INT32_MAX;
+        s_box[2] = INT32_MIN;
+        s_box[3] = INT32_MIN;
+    }
+    __syncthreads();
+    // bounding box of the block's stencil bases
+    int32_t mnx = valid ? s.bx : INT32_MAX, mny = valid ? s.by : INT32_MAX;
+    int32_t mxx = valid ? s.bx : INT32_MIN, mxy = valid ? s.by : INT32_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    if ((threadIdx.x & 31) == 0 && mnx != INT32_MAX) {
+        atomicMin(&s_box[0], mnx);
+        atomicMin(&s_box[1], mny);
+        atomicMax(&s_box[2], mxx);
+        atomicMax(&s_box[3], mxy);
+    }
+    __syncthreads();
+    const int32_t tx0 = s_box[0], ty0 = s_box[1];
+    if (tx0 == INT32_MAX) { return; } // no particle in this block (uniform)
+    const int32_t tw = s_box[2] - tx0 + 3, th = s_box[3] - ty0 + 3;
+    const bool tiled = tw * th <= TILE_CAP;
+    if (tiled) {
+        for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+            s_x[t] = 0.f;
+            s_y[t] = 0.f;
+            s_m[t] = 0.f;
+        }
+        __syncthreads();
+        if (valid) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const float4 c = node_contrib(k, s, v, Q, i, j);
+                    const int t    = (s.by + j - ty0) * tw + (s.bx + i - tx0);
+                    atomicAdd(&s_x[t], c.x);
+                    atomicAdd(&s_y[t], c.y);
+                    atomicAdd(&s_m[t], c.z);
+                }
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+            const float m = s_m[t];
+            if (m != 0.f) {
+                const int32_t gx = tx0 + t % tw, gy = ty0 + t / tw;
+                atomicAdd(&grid[(size_t)gy * (size_t)k.nx + (size_t)gx], make_float4(s_x[t], s_y[t], m, 0.f));
+            }
+        }
+    } else if (valid) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float4 c = node_contrib(k, s, v, Q, i, j);
+                atomicAdd(&grid[(size_t)(s.by + j) * (size_t)k.nx + (size_t)(s.bx + i)], c);
+            }
+        }
+    }
+}
+
+// ----- kernels -------------------------------------------------------------------------------------------
+
+__global__ void k_clear(float4* __restrict__ grid, int64_t nn)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += stride) {
+        grid[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(T_MPM)
+    k_p2g(const MpmK k, const float2* __restrict__ x, const float2* __restrict__ v, const float4* __restrict__ C,
+          const float4* __restrict__ F, const float* __restrict__ J, const int32_t* __restrict__ mat,
+          float4* __restrict__ grid, uint32_t* status)
+{
+    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < k.n;
+    Stencil s{};
+    float2 vv = make_float2(0.f, 0.f);
+    float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+        const int m     = mat_of(k, MODE, mat, i);
+        const float4 Fp = (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : F[i];
+        const float Jp  = (m == MODE_COROT) ? 1.f : J[i];
+        Q               = affine(k, m, C[i], Fp, Jp);
+        vv              = v[i];
+        s               = stencil(k, x[i], status);
+    }
+    p2g_block(k, valid, s, vv, Q, grid);
+}
+
+// gridKernel, MPM.cu:131-177 (in place)
+__global__ void k_grid(const MpmK k, float4* __restrict__ grid)
+{
+    const int64_t nn     = (int64_t)k.nx * k.ny;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn; idx += stride) {
+        float4 g        = grid[idx];
+        const float2 vv = node_velocity(k, g, (int32_t)(idx % k.nx), (int32_t)(idx / k.nx));
+        g.x             = vv.x;
+        g.y             = vv.y;
+        grid[idx]       = g;
+    }
+}
+
+// G2P on a grid of velocities (RAW=false) or of raw momentum (RAW=true); writes the whole particle state
+template <int MODE, bool RAW>
+__global__ void __launch_bounds__(T_MPM)
+    k_g2p(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ x, float2* __restrict__ v,
+          float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
+          float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (zero_grid) {
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t z = i; z < zero_nodes; z += stride) { zero_grid[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    }
+    if (i >= k.n) { return; }
+    const int m        = mat_of(k, MODE, mat, i);
+    const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
+    PState ps;
+    ps.x = x[i];
+    ps.F = (m != MODE_FLUID || track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+    ps.J = (m != MODE_COROT) ? J[i] : 1.f;
+    g2p_body<RAW>(k, m, track_f, grid, ps, status);
+    x[i] = ps.x;
+    v[i] = ps.v;
+    C[i] = ps.C;
+    if (m != MODE_FLUID || track_f) { F[i] = ps.F; }
+    if (m != MODE_COROT) { J[i] = ps.J; }
+}
+
+// G2P of one step fused with P2G of the next; zeroes the grid used two steps later
+template <int MODE>
+__global__ void __launch_bounds__(T_MPM)
+    k_g2p_p2g(const MpmK k, const float4* __restrict__ grid_in, float4* __restrict__ grid_out,
+              float4* __restrict__ grid_zero, int64_t nn, float2* __restrict__ x, float4* __restrict__ F,
+              float* __restrict__ J, const int32_t* __restrict__ mat, uint32_t* status)
+{
+    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
+    {
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t z = i; z < nn; z += stride) { grid_zero[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    }
+    const bool valid   = i < k.n;
+    const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
+    Stencil s{};
+    float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 vv = make_float2(0.f, 0.f);
+    if (valid) {
+        const int m = mat_of(k, MODE, mat, i);
+        PState ps;
+        ps.x = x[i];
+        ps.F = (m != MODE_FLUID || track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+        ps.J = (m != MODE_COROT) ? J[i] : 1.f;
+        g2p_body<true>(k, m, track_f, grid_in, ps, status);
+        x[i] = ps.x;
+        if (m != MODE_FLUID || track_f) { F[i] = ps.F; }
+        if (m != MODE_COROT) { J[i] = ps.J; }
+        Q  = affine(k, m, ps.C, (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : ps.F, ps.J);
+        vv = ps.v;
+        s  = stencil(k, ps.x, status);
+    }
+    p2g_block(k, valid, s, vv, Q, grid_out);
+}
+
+// ----- spatial sort of the particles (keeps P2G tiles small) ---------------------------------------------
+__global__ void __launch_bounds__(T_MPM)
+    k_mpm_key(const MpmK k, const float2* __restrict__ x, uint2* __restrict__ keyrank, uint32_t* __restrict__ count,
+              uint32_t* status)
+{
+    const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid   = i < k.n;
+    const int32_t lane = threadIdx.x & 31;
+    uint32_t key       = 0xffffffffu;
+    if (valid) {
+        const Stencil s = stencil(k, x[i], status);
+        key             = (uint32_t)s.by * (uint32_t)k.nx + (uint32_t)s.bx;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const int32_t leader = __ffs(peers) - 1;
+    uint32_t base        = 0;
+    if (valid && lane == leader) { base = atomicAdd(&count[key], (uint32_t)__popc(peers)); }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) { keyrank[i] = make_uint2(key, base + (uint32_t)__popc(peers & ((1u << lane) - 1u))); }
+}
+
+__global__ void __launch_bounds__(T_MPM)
+    k_mpm_gather(int32_t n, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
+                 const uint32_t* __restrict__ bucket, const float2* __restrict__ x0, const float2* __restrict__ v0,
+                 const float4* __restrict__ C0, const float4* __restrict__ F0, const float* __restrict__ J0,
+                 const int32_t* __restrict__ m0, const uint32_t* __restrict__ id0, float2* __restrict__ x1,
+                 float2* __restrict__ v1, float4* __restrict__ C1, float4* __restrict__ F1, float* __restrict__ J1,
+                 int32_t* __restrict__ m1, uint32_t* __restrict__ id1)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    const uint2 kr   = keyrank[i];
+    const uint32_t s = __ldg(&start[kr.x]);
+    const uint32_t e = __ldg(&start[kr.x + 1]);
+    uint32_t rank    = 0;
+    for (uint32_t t = s; t < e; ++t) { rank += (__ldg(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
+    const uint32_t d = s + rank;
+    x1[d]            = x0[i];
+    v1[d]            = v0[i];
+    C1[d]            = C0[i];
+    F1[d]            = F0[i];
+    J1[d]            = J0[i];
+    m1[d]            = m0[i];
+    id1[d]           = id0[i];
+}
+
+// get_state helper: put particle i back at its original index id[i]
+__global__ void k_mpm_unsort(int32_t n, const uint32_t* __restrict__ id, const float2* __restrict__ x0,
+                             const float2* __restrict__ v0, const float4* __restrict__ C0,
+                             const float4* __restrict__ F0, const float* __restrict__ J0, float2* __restrict__ x1,
+                             float2* __restrict__ v1, float4* __restrict__ C1, float4* __restrict__ F1,
+                             float* __restrict__ J1)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    const uint32_t d = id[i];
+    x1[d]            = x0[i];
+    v1[d]            = v0[i];
+    C1[d]            = C0[i];
+    F1[d]            = F0[i];
+    J1[d]            = J0[i];
+}
+
+__global__ void k_mpm_init(int32_t n, uint32_t* __restrict__ id, float2* __restrict__ v, float4* __restrict__ C,
+                           float4* __restrict__ F, float* __restrict__ J, int32_t* __restrict__ mat, int set_v,
+                           int set_C, int set_F, int set_J, int set_m, int32_t material)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    id[i] = (uint32_t)i;
+    if (set_v) { v[i] = make_float2(0.f, 0.f); }
+    if (set_C) { C[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    if (set_F) { F[i] = make_float4(1.f, 0.f, 0.f, 1.f); }
+    if (set_J) { J[i] = 1.f; }
+    if (set_m) { mat[i] = material; }
+}
+
+} // namespace
+} // namespace gpe
+
+using namespace gpe;
+
+struct MpmGraph {
+    cudaGraphExec_t exec = nullptr;
+    int ga_end;
+    int cur_end;
+};
+
+struct gpe_mpm {
+    int device = 0;
+    gpe_mpm_params prm{};
+    MpmK k{};
+    int64_t cap = 0, n = 0;
+    int64_t nn  = 0; // nodes
+    void* base  = nullptr;
+    float2* x[2]    = {};
+    float2* v[2]    = {};
+    float4* C[2]    = {};
+    float4* F[2]    = {};
+    float* J[2]     = {};
+    int32_t* mat[2] = {};
+    uint32_t* id[2] = {};
+    float4* grid[3] = {};
+    uint2* keyrank  = nullptr;
+    uint32_t* bucket = nullptr;
+    uint32_t* count  = nullptr;
+    uint32_t* start  = nullptr;
+    uint32_t* bsum   = nullptr;
+    uint32_t* status = nullptr;
+    int cur = 0;        // which particle buffer set is current
+    int ga  = 0;        // grid holding the current step's nodes; ga+1, ga+2 (mod 3) are zero between steps
+    bool grids_dirty = false;
+    bool have_state  = false;
+    int64_t steps_since_sort = 0;
+    int32_t launches = 0;
+    std::map<std::tuple<int, int, int, int>, MpmGraph> graphs;
+
+    void drop_graphs()
+    {
+        for (auto& g : graphs) {
+            if (g.second.exec) { cudaGraphExecDestroy(g.second.exec); }
+        }
+        graphs.clear();
+    }
+};
+
+namespace {
+
+int32_t mpm_validate(const gpe_mpm_params* p)
+{
+    if (!p || !(p->dx > 0.f) || p->nx < 3 || p->ny < 3 || !(p->dt > 0.f) || !(p->mass > 0.f) || p->bc_width < 0 ||
+        p->material < 0 || p->material > 2 || (int64_t)p->nx * p->ny > ((int64_t)1 << 30)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "invalid MPM parameters");
+        return GPE_ERR_BAD_ARG;
+    }
+    return GPE_OK;
+}
+
+MpmK mpm_make_k(const gpe_mpm_params& p)
+{
+    MpmK k{};
+    k.dx        = p.dx;
+    k.inv_dx    = 1.f / p.dx;
+    k.goff      = p.grid_offset;
+    k.dt        = p.dt;
+    k.nx        = p.nx;
+    k.ny        = p.ny;
+    k.gdt_x     = p.gravity[0] * p.dt;
+    k.gdt_y     = p.gravity[1] * p.dt;
+    k.mass      = p.mass;
+    k.vol0      = p.vol0;
+    k.bc_type   = p.bc_type;
+    k.bc_width  = p.bc_width;
+    k.lo_x      = p.clamp_lo[0];
+    k.lo_y      = p.clamp_lo[1];
+    k.hi_x      = p.clamp_hi[0];
+    k.hi_y      = p.clamp_hi[1];
+    k.mid_x     = 0.5f * (p.clamp_lo[0] + p.clamp_hi[0]);
+    k.mid_y     = 0.5f * (p.clamp_lo[1] + p.clamp_hi[1]);
+    k.material  = p.material;
+    k.flags     = p.flags;
+    k.k_bulk    = p.k_bulk;
+    k.gamma     = p.gamma;
+    k.p_min     = p.p_min;
+    k.p_max     = p.p_max;
+    k.J_min     = p.J_min;
+    k.J_max     = p.J_max;
+    k.mu0       = p.E / (2.f * (1.f + p.nu));
+    k.la0       = p.E * p.nu / ((1.f + p.nu) * (1.f - 2.f * p.nu));
+    k.theta_c   = p.theta_c;
+    k.theta_s   = p.theta_s;
+    k.hardening = p.hardening;
+    k.apic_s    = 4.f * k.inv_dx * k.inv_dx;
+    return k;
+}
+
+int mode_of(const gpe_mpm* s)
+{
+    return (s->prm.flags & GPE_MPM_FLAG_PER_PARTICLE_MATERIAL) ? MODE_MIXED : s->prm.material;
+}
+
+unsigned mblocks(int64_t n) { return (unsigned)((n + T_MPM - 1) / T_MPM); }
+
+unsigned grid_blocks(int64_t nn)
+{
+    const int64_t want = (nn + T_MPM - 1) / T_MPM;
+    const int64_t cap  = (int64_t)gpe::sm_count() * 8;
+    return (unsigned)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+template <int MODE>
+int32_t launch_p2g_t(gpe_mpm* s, float4* grid, cudaStream_t st)
+{
+    const int c = s->cur;
+    k_p2g<MODE><<<mblocks(s->n), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
+                                                  grid, s->status);
+    GPE_CHECK_LAUNCH("k_p2g");
+    return GPE_OK;
+}
+
+int32_t launch_p2g(gpe_mpm* s, float4* grid, cudaStream_t st)
+{
+    if (s->n == 0) { return GPE_OK; }
+    s->launches += 1;
+    switch (mode_of(s)) {
+        case MODE_FLUID: return launch_p2g_t<MODE_FLUID>(s, grid, st);
+        case MODE_COROT: return launch_p2g_t<MODE_COROT>(s, grid, st);
+        case MODE_SNOW: return launch_p2g_t<MODE_SNOW>(s, grid, st);
+        default: return launch_p2g_t<MODE_MIXED>(s, grid, st);
+    }
+}
+
+template <int MODE, bool RAW>
+int32_t launch_g2p_t(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
+{
+    const int c      = s->cur;
+    const unsigned g = std::max(mblocks(s->n), zero ? grid_blocks(s->nn) : 1u);
+    k_g2p<MODE, RAW><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
+                                          zero, zero ? s->nn : 0, s->status);
+    GPE_CHECK_LAUNCH("k_g2p");
+    return GPE_OK;
+}
+
+template <bool RAW>
+int32_t launch_g2p(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
+{
+    if (s->n == 0 && !zero) { return GPE_OK; }
+    s->launches += 1;
+    switch (mode_of(s)) {
+        case MODE_FLUID: return launch_g2p_t<MODE_FLUID, RAW>(s, grid, zero, st);
+        case MODE_COROT: return launch_g2p_t<MODE_COROT, RAW>(s, grid, zero, st);
+        case MODE_SNOW: return launch_g2p_t<MODE_SNOW, RAW>(s, grid, zero, st);
+        default: return launch_g2p_t<MODE_MIXED, RAW>(s, grid, zero, st);
+    }
+}
+
+template <int MODE>
+int32_t launch_fused_t(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero, cudaStream_t st)
+{
+    const int c      = s->cur;
+    const unsigned g = std::max(mblocks(s->n), grid_blocks(s->nn));
+    k_g2p_p2g<MODE><<<g, T_MPM, 0, st>>>(s->k, gin, gout, gzero, s->nn, s->x[c], s->F[c], s->J[c], s->mat[c],
+                                         s->status);
+    GPE_CHECK_LAUNCH("k_g2p_p2g");
+    return GPE_OK;
+}
+
+int32_t launch_fused(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero, cudaStream_t st)
+{
+    s->launches += 1;
+    switch (mode_of(s)) {
+        case MODE_FLUID: return launch_fused_t<MODE_FLUID>(s, gin, gout, gzero, st);
+        case MODE_COROT: return launch_fused_t<MODE_COROT>(s, gin, gout, gzero, st);
+        case MODE_SNOW: return launch_fused_t<MODE_SNOW>(s, gin, gout, gzero, st);
+        default: return launch_fused_t<MODE_MIXED>(s, gin, gout, gzero, st);
+    }
+}
+
+int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
+{
+    if (s->n <= 1) { return GPE_OK; }
+    const int c = s->cur, o = c ^ 1;
+    k_mpm_key<<<mblocks(s->n), T_MPM, 0, st>>>(s->k, s->x[c], s->keyrank, s->count, s->status);
+    GPE_CHECK_LAUNCH("k_mpm_key");
+    int32_t rc = launch_exclusive_scan(s->count, (uint32_t)s->nn, s->bsum, s->start, st);
+    if (rc) { return rc; }
+    rc = launch_scatter(s->keyrank, s->n, s->start, s->bucket, st);
+    if (rc) { return rc; }
+    k_mpm_gather<<<mblocks(s->n), T_MPM, 0, st>>>((int32_t)s->n, s->keyrank, s->start, s->bucket, s->x[c], s->v[c],
+                                                   s->C[c], s->F[c], s->J[c], s->mat[c], s->id[c], s->x[o],
+                                                   s->v[o], s->C[o], s->F[o], s->J[o], s->mat[o], s->id[o]);
+    GPE_CHECK_LAUNCH("k_mpm_gather");
+    s->cur ^= 1;
+    s->launches += 6;
+    return GPE_OK;
+}
+
+// n_steps steps: [sort], P2G, (n-1) x fused G2P+P2G, G2P. Grids ga+1 and ga+2 are zero on entry and exit.
+int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
+{
+    int32_t rc = GPE_OK;
+    if (do_sort) { rc = mpm_sort(s, st); }
+    if (rc) { return rc; }
+    int a = (s->ga + 1) % 3;
+    rc    = launch_p2g(s, s->grid[a], st);
+    for (int32_t t = 1; t < n_steps && rc == GPE_OK; ++t) {
+        const int b = (a + 1) % 3, z = (a + 2) % 3;
+        if (s->n > 0) {
+            rc = launch_fused(s, s->grid[a], s->grid[b], s->grid[z], st);
+        } else {
+            k_clear<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->grid[z], s->nn);
+            GPE_CHECK_LAUNCH("k_clear");
+        }
+        a = b;
+    }
+    if (rc) { return rc; }
+    // last G2P; zero the grid that was used before this one so two zero grids follow `a`
+    rc    = launch_g2p<true>(s, s->grid[a], s->grid[(a + 2) % 3], st);
+    s->ga = a;
+    return rc;
+}
+
+int32_t mpm_alloc(gpe_mpm* s)
+{
+    const size_t N = (size_t)s->cap;
+    const size_t M = (size_t)s->nn;
+    Carver c;
+    size_t ox[2], ov[2], oC[2], oF[2], oJ[2], om[2], oid[2], og[3];
+    for (int b = 0; b < 2; ++b) {
+        ox[b]  = c.take<float2>(N);
+        ov[b]  = c.take<float2>(N);
+        oC[b]  = c.take<float4>(N);
+        oF[b]  = c.take<float4>(N);
+        oJ[b]  = c.take<float>(N);
+        om[b]  = c.take<int32_t>(N);
+        oid[b] = c.take<uint32_t>(N);
+    }
+    for (int b = 0; b < 3; ++b) { og[b] = c.take<float4>(M); }
+    const size_t okr = c.take<uint2>(N);
+    const size_t obk = c.take<uint32_t>(N);
+    const size_t ocn = c.take<uint32_t>(M);
+    const size_t ost = c.take<uint32_t>(M + 1);
+    const size_t obs = c.take<uint32_t>(scan_blocks((uint32_t)M) + 1);
+    const size_t oss = c.take<uint32_t>(4);
+    GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
+    GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
+    uint8_t* b = static_cast<uint8_t*>(s->base);
+    for (int q = 0; q < 2; ++q) {
+        s->x[q]   = reinterpret_cast<float2*>(b + ox[q]);
+        s->v[q]   = reinterpret_cast<float2*>(b + ov[q]);
+        s->C[q]   = reinterpret_cast<float4*>(b + oC[q]);
+        s->F[q]   = reinterpret_cast<float4*>(b + oF[q]);
+        s->J[q]   = reinterpret_cast<float*>(b + oJ[q]);
+        s->mat[q] = reinterpret_cast<int32_t*>(b + om[q]);
+        s->id[q]  = reinterpret_cast<uint32_t*>(b + oid[q]);
+    }
+    for (int q = 0; q < 3; ++q) { s->grid[q] = reinterpret_cast<float4*>(b + og[q]); }
+    s->keyrank = reinterpret_cast<uint2*>(b + okr);
+    s->bucket  = reinterpret_cast<uint32_t*>(b + obk);
+    s->count   = reinterpret_cast<uint32_t*>(b + ocn);
+    s->start   = reinterpret_cast<uint32_t*>(b + ost);
+    s->bsum    = reinterpret_cast<uint32_t*>(b + obs);
+    s->status  = reinterpret_cast<uint32_t*>(b + oss);
+    return GPE_OK;
+}
+
+cudaMemcpyKind mk_in(int32_t mem) { return mem == GPE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+cudaMemcpyKind mk_out(int32_t mem) { return mem == GPE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost; }
+
+} // namespace
+
+extern "C" {
+
+int32_t gpe_mpm_create(const gpe_mpm_params* params, int64_t capacity, gpe_mpm** out)
+{
+    gpe::clear_error();
+    if (!out || capacity < 0 || capacity > (int64_t)INT32_MAX / 2) { return GPE_ERR_BAD_ARG; }
+    *out       = nullptr;
+    int32_t rc = mpm_validate(params);
+    if (rc) { return rc; }
+    int dev = 0;
+    rc      = gpe::current_device(&dev);
+    if (rc) { return rc; }
+    gpe_mpm* s = new gpe_mpm();
+    s->device  = dev;
+    s->prm     = *params;
+    s->k       = mpm_make_k(*params);
+    s->cap     = capacity;
+    s->nn      = (int64_t)params->nx * params->ny;
+    rc         = mpm_alloc(s);
+    if (rc) {
+        if (s->base) { cudaFree(s->base); }
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_destroy(gpe_mpm* s)
+{
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    s->drop_graphs();
+    if (s->base) { cudaFree(s->base); }
+    delete s;
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_set_params(gpe_mpm* s, const gpe_mpm_params* params)
+{
+    gpe::clear_error();
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    int32_t rc = mpm_validate(params);
+    if (rc) { return rc; }
+    if (params->nx != s->prm.nx || params->ny != s->prm.ny) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_params: the node grid is fixed at creation");
+        return GPE_ERR_BAD_ARG;
+    }
+    s->prm        = *params;
+    const int32_t n = s->k.n;
+    s->k          = mpm_make_k(*params);
+    s->k.n        = n;
+    s->drop_graphs();
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_set_state(gpe_mpm* s, const float* pos, const float* vel, const float* C, const float* F,
+                          const float* J, const int32_t* material, int64_t n, int32_t mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n < 0 || (n > 0 && !pos) || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_state: bad arguments");
+        return GPE_ERR_BAD_ARG;
+    }
+    if (n > s->cap) {
+        gpe::set_error(GPE_ERR_CAPACITY, "gpe_mpm_set_state: %lld particles exceed capacity %lld", (long long)n,
+                       (long long)s->cap);
+        return GPE_ERR_CAPACITY;
+    }
+    if (mem == GPE_MEM_HOST && material) {
+        for (int64_t i = 0; i < n; ++i) {
+            if (material[i] < 0 || material[i] > 2) {
+                gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_state: material ids must be in [0, 2]");
+                return GPE_ERR_BAD_ARG;
+            }
+        }
+    }
+    cudaStream_t st = as_stream(stream);
+    s->cur          = 0;
+    if (n > 0) {
+        GPE_TRY_CUDA(cudaMemcpyAsync(s->x[0], pos, sizeof(float2) * (size_t)n, mk_in(mem), st));
+        if (vel) { GPE_TRY_CUDA(cudaMemcpyAsync(s->v[0], vel, sizeof(float2) * (size_t)n, mk_in(mem), st)); }
+        if (C) { GPE_TRY_CUDA(cudaMemcpyAsync(s->C[0], C, sizeof(float4) * (size_t)n, mk_in(mem), st)); }
+        if (F) { GPE_TRY_CUDA(cudaMemcpyAsync(s->F[0], F, sizeof(float4) * (size_t)n, mk_in(mem), st)); }
+        if (J) { GPE_TRY_CUDA(cudaMemcpyAsync(s->J[0], J, sizeof(float) * (size_t)n, mk_in(mem), st)); }
+        if (material) {
+            GPE_TRY_CUDA(cudaMemcpyAsync(s->mat[0], material, sizeof(int32_t) * (size_t)n, mk_in(mem), st));
+        }
+        k_mpm_init<<<mblocks(n), T_MPM, 0, st>>>((int32_t)n, s->id[0], s->v[0], s->C[0], s->F[0], s->J[0], s->mat[0],
+                                                  !vel, !C, !F, !J, !material, s->prm.material);
+        GPE_CHECK_LAUNCH("k_mpm_init");
+    }
+    if (s->n != n) { s->drop_graphs(); }
+    s->n                = n;
+    s->k.n              = (int32_t)n;
+    s->have_state       = true;
+    s->grids_dirty      = true;
+    s->steps_since_sort = 0;
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_get_state(gpe_mpm* s, float* pos, float* vel, float* C, float* F, float* J, int64_t n, int32_t mem,
+                          void* stream)
+{
+    gpe::clear_error();
+    if (!s || n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_get_state: n must equal the particle count");
+        return GPE_ERR_BAD_ARG;
+    }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    if (n > 0) {
+        // particles are returned at their original indices
+        const int c = s->cur, o = c ^ 1;
+        k_mpm_unsort<<<mblocks(n), T_MPM, 0, st>>>((int32_t)n, s->id[c], s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+                                                   s->x[o], s->v[o], s->C[o], s->F[o], s->J[o]);
+        GPE_CHECK_LAUNCH("k_mpm_unsort");
+        if (pos) { GPE_TRY_CUDA(cudaMemcpyAsync(pos, s->x[o], sizeof(float2) * (size_t)n, mk_out(mem), st)); }
+        if (vel) { GPE_TRY_CUDA(cudaMemcpyAsync(vel, s->v[o], sizeof(float2) * (size_t)n, mk_out(mem), st)); }
+        if (C) { GPE_TRY_CUDA(cudaMemcpyAsync(C, s->C[o], sizeof(float4) * (size_t)n, mk_out(mem), st)); }
+        if (F) { GPE_TRY_CUDA(cudaMemcpyAsync(F, s->F[o], sizeof(float4) * (size_t)n, mk_out(mem), st)); }
+        if (J) { GPE_TRY_CUDA(cudaMemcpyAsync(J, s->J[o], sizeof(float) * (size_t)n, mk_out(mem), st)); }
+    }
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_count(const gpe_mpm* s, int64_t* n)
+{
+    if (!s || !n) { return GPE_ERR_BAD_ARG; }
+    *n = s->n;
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_step(gpe_mpm* s, int32_t n_steps, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    if (n_steps == 0) { return GPE_OK; }
+    cudaStream_t st = as_stream(stream);
+    if (s->grids_dirty) {
+        for (int q = 0; q < 3; ++q) { GPE_TRY_CUDA(cudaMemsetAsync(s->grid[q], 0, sizeof(float4) * (size_t)s->nn, st)); }
+        s->grids_dirty = false;
+    }
+    const bool do_sort = s->prm.sort_interval > 0 && s->steps_since_sort >= s->prm.sort_interval;
+    const auto key     = std::make_tuple(n_steps, s->ga, s->cur, (int)do_sort);
+    auto it            = s->graphs.find(key);
+    if (it == s->graphs.end()) {
+        cudaStream_t cap_st = st;
+        bool own            = false;
+        if (cap_st == nullptr) {
+            GPE_TRY_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
+            own = true;
+        }
+        const int ga0 = s->ga, cur0 = s->cur;
+        GPE_TRY_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+        s->launches = 0;
+        int32_t rc  = mpm_run(s, n_steps, do_sort, cap_st);
+        cudaGraph_t graph    = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(cap_st, &graph);
+        MpmGraph g;
+        g.ga_end  = s->ga;
+        g.cur_end = s->cur;
+        s->ga     = ga0;
+        s->cur    = cur0;
+        if (rc == GPE_OK && ce != cudaSuccess) {
+            gpe::set_cuda_error(ce, "cudaStreamEndCapture");
+            rc = GPE_ERR_CUDA;
+        }
+        if (rc == GPE_OK) {
+            const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+            if (ie != cudaSuccess) {
+                gpe::set_cuda_error(ie, "cudaGraphInstantiate");
+                rc = GPE_ERR_CUDA;
+            }
+        }
+        if (graph) { cudaGraphDestroy(graph); }
+        if (own) { cudaStreamDestroy(cap_st); }
+        if (rc) { return rc; }
+        it = s->graphs.emplace(key, g).first;
+    }
+    GPE_TRY_CUDA(cudaGraphLaunch(it->second.exec, st));
+    s->ga  = it->second.ga_end;
+    s->cur = it->second.cur_end;
+    s->steps_since_sort = do_sort ? n_steps : s->steps_since_sort + n_steps;
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_stage(gpe_mpm* s, int32_t stage, void* stream)
+{
+    gpe::clear_error();
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    float4* g       = s->grid[s->ga];
+    s->grids_dirty  = true;
+    switch (stage) {
+        case GPE_MPM_STAGE_CLEAR:
+            k_clear<<<grid_blocks(s->nn), T_MPM, 0, st>>>(g, s->nn);
+            GPE_CHECK_LAUNCH("k_clear");
+            return GPE_OK;
+        case GPE_MPM_STAGE_P2G: return launch_p2g(s, g, st);
+        case GPE_MPM_STAGE_GRID:
+            k_grid<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->k, g);
+            GPE_CHECK_LAUNCH("k_grid");
+            return GPE_OK;
+        case GPE_MPM_STAGE_G2P: return launch_g2p<false>(s, g, nullptr, st);
+        case GPE_MPM_STAGE_SORT: return mpm_sort(s, st);
+        default: return GPE_ERR_BAD_ARG;
+    }
+}
+
+int32_t gpe_mpm_get_grid(gpe_mpm* s, float* dst, int64_t n_nodes, int32_t mem, void* stream)
+{
+    if (!s || !dst || n_nodes != s->nn) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    GPE_TRY_CUDA(cudaMemcpyAsync(dst, s->grid[s->ga], sizeof(float4) * (size_t)s->nn, mk_out(mem), st));
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_status(gpe_mpm* s, uint32_t* status, void* stream)
+{
+    if (!s || !status) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    GPE_TRY_CUDA(cudaMemcpyAsync(status, s->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaMemsetAsync(s->status, 0, sizeof(uint32_t), st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_launches_per_step(const gpe_mpm* s, int32_t* launches)
+{
+    if (!s || !launches) { return GPE_ERR_BAD_ARG; }
+    *launches = 1;
+    return GPE_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,1189 @@
+// pbf.cu — Position-Based Fluids step on GB300 (sm_103a).
+//
+// One step (the reference's substep, PBF.cu:921-956) is:
+//   predict + key + histogram   k_predict_hist   (prepNextSubstepKernel PBF.cu:786-797, made device-wide)
+//   scan / scatter              sort.cu          (incPrefSum256 PBF.cu:835-860)
+//   stable placement + gather   k_place          (PBF.cu:801-833; stable here, the reference's intra-cell
+//                                                  order follows shared-memory atomic order)
+//   iters x (lambda, delta p)   k_lambda, k_delta_p (PBF.cu:215-308, 365-499)
+//   velocity + XSPH (+omega)    k_xsph           (PBF.cu:500-638 fused: v_j = (x*_j - x_j)/dt on the fly)
+//   vorticity confinement       k_vorticity      (Macklin & Mueller 2013; absent in the reference)
+//
+// Layout: structure-of-arrays in HBM, particles of all scenes in one array sorted by global cell key
+// (scene-major, then row-major cells), so a row of neighbour cells is one contiguous index range. The
+// reference's per-chunk shared-memory pools, 1-cell halo copies and migration queues exist because a block
+// of its design must hold a whole chunk; with a device-wide sort every scene is one domain, neighbours
+// across what were chunk borders are read in place from L2, and a particle that crosses a border simply
+// lands in another cell range at the next sort.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "gpe_internal.h"
+
+namespace gpe {
+
+struct DomDev {
+    float ox, oy;             // sort-grid origin (the scene's lower corner)
+    float lox, loy, hix, hiy; // wall clamp box (handleOOB, PBF.cu:487-490)
+    int32_t ncx, ncy;         // cells
+    uint32_t coff;            // first global cell of the scene
+    uint32_t pad[3];
+};
+
+struct PbfK {
+    float h, h2, c6, cs, inv_w_dq, inv_cell;
+    float rho0, inv_rho0, mass, inv_mass;
+    float dt, inv_dt, g2x, g2y;
+    float eps, scorr_k, dp_scale, c_min, xsph_c, vort_eps, v_max, v_min2, vort_dt;
+    int32_t R;
+    uint32_t flags;
+    int32_t n;
+    DomDev d0; // the scene when there is only one
+};
+
+namespace {
+
+constexpr int T_PART = 256; // threads per block for the per-particle kernels
+
+__device__ __forceinline__ int32_t cell_coord(float pos, float org, float inv, int32_t nc)
+{
+    // (pos - org) and the product are each rounded exactly once, as in the oracle; no contraction
+    const float t = __fsub_rn(pos, org);
+    const float u = __fmul_rn(t, inv);
+    if (!(u >= 0.f)) { return 0; }
+    if (u >= (float)nc) { return nc - 1; }
+    return (int32_t)u;
+}
+
+template <bool MULTI>
+__device__ __forceinline__ DomDev load_dom(const PbfK& k, const DomDev* __restrict__ doms,
+                                           const int32_t* __restrict__ dom, int32_t i)
+{
+    if constexpr (MULTI) {
+        return doms[__ldg(&dom[i])];
+    } else {
+        return k.d0;
+    }
+}
+
+// Visits every particle index in the cells within R of the base cell of (px, py) (the reference scans the
+// 3x3 cells around clamp(floorf(x)/kCellDim), PBF.cu:252-263). Each row of cells is one contiguous range.
+template <class F>
+__device__ __forceinline__ void for_neighbours(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
+                                               float px, float py, F&& f)
+{
+    const int32_t bx = cell_coord(px, d.ox, k.inv_cell, d.ncx);
+    const int32_t by = cell_coord(py, d.oy, k.inv_cell, d.ncy);
+    const int32_t x0 = max(bx - k.R, 0);
+    const int32_t x1 = min(bx + k.R, d.ncx - 1);
+    const int32_t y0 = max(by - k.R, 0);
+    const int32_t y1 = min(by + k.R, d.ncy - 1);
+    for (int32_t y = y0; y <= y1; ++y) {
+        const uint32_t row = d.coff + (uint32_t)y * (uint32_t)d.ncx;
+        const uint32_t b   = __ldg(&start[row + x0]);
+        const uint32_t e   = __ldg(&start[row + x1 + 1]);
+        for (uint32_t j = b; j < e; ++j) { f(j); }
+    }
+}
+
+// integer mixer of the reference (hash, cuda-internal.cuh:19-27)
+__device__ __forceinline__ uint32_t mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// pairDirection, PBF.cu:309-321
+__device__ __forceinline__ void pair_direction(uint32_t a, uint32_t b, float& nx, float& ny)
+{
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    const float ang   = (float)(mix32(lo * 0x9E3779B9u ^ hi) & 0xFFFFu) * (6.2831853f / 65536.f);
+    float s, c;
+    __sincosf(ang, &s, &c);
+    const float sign = (a < b) ? 1.f : -1.f;
+    nx               = sign * c;
+    ny               = sign * s;
+}
+
+// ----- predict + cell key + histogram rank (PBF.cu:786-797) ---------------------------------------------
+// Lanes of a warp that share a cell take consecutive ranks in lane order from one atomicAdd.
+template <bool MULTI>
+__global__ void __launch_bounds__(T_PART)
+    k_predict_hist(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                   const float2* __restrict__ x, const float2* __restrict__ v, float2* __restrict__ xs_tmp,
+                   uint2* __restrict__ keyrank, uint32_t* __restrict__ count)
+{
+    const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid   = i < k.n;
+    const int32_t lane = threadIdx.x & 31;
+    uint32_t key       = 0xffffffffu;
+    float2 ps          = make_float2(0.f, 0.f);
+    if (valid) {
+        const DomDev d = load_dom<MULTI>(k, doms, dom, i);
+        const float2 p = x[i];
+        const float2 w = v[i];
+        ps.x           = __fadd_rn(__fmaf_rn(k.dt, w.x, p.x), k.g2x);
+        ps.y           = __fadd_rn(__fmaf_rn(k.dt, w.y, p.y), k.g2y);
+        const int32_t cx = cell_coord(ps.x, d.ox, k.inv_cell, d.ncx);
+        const int32_t cy = cell_coord(ps.y, d.oy, k.inv_cell, d.ncy);
+        key              = d.coff + (uint32_t)cy * (uint32_t)d.ncx + (uint32_t)cx;
+    }
+    const uint32_t peers  = __match_any_sync(0xffffffffu, key);
+    const int32_t leader  = __ffs(peers) - 1;
+    uint32_t base         = 0;
+    if (valid && lane == leader) { base = atomicAdd(&count[key], (uint32_t)__popc(peers)); }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) {
+        const uint32_t rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        xs_tmp[i]           = ps;
+        keyrank[i]          = make_uint2(key, rank);
+    }
+}
+
+// ----- stable placement + gather (PBF.cu:801-833) -------------------------------------------------------
+// The atomic ranks are unique but depend on warp scheduling; the stable slot of particle i is the number of
+// entries of its cell's bucket with a smaller pre-sort index.
+__global__ void __launch_bounds__(T_PART)
+    k_place(int32_t n, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
+            const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
+            const float2* __restrict__ xs_tmp, float2* __restrict__ x_out, float2* __restrict__ xs_out,
+            uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
+            uint32_t* __restrict__ id_out)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    const uint2 kr   = keyrank[i];
+    const uint32_t s = __ldg(&start[kr.x]);
+    const uint32_t e = __ldg(&start[kr.x + 1]);
+    uint32_t rank    = 0;
+    for (uint32_t t = s; t < e; ++t) { rank += (__ldg(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
+    const uint32_t dst = s + rank;
+    x_out[dst]         = x_in[i];
+    xs_out[dst]        = xs_tmp[i];
+    perm[dst]          = (uint32_t)i;
+    key_out[dst]       = kr.x;
+    if (id_in) { id_out[dst] = id_in[i]; }
+}
+
+// ----- lambda (PBF.cu:243-294) --------------------------------------------------------------------------
+template <bool MULTI, bool SELFG>
+__global__ void __launch_bounds__(T_PART)
+    k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) { return; }
+    const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
+    const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
+    const float2 p       = xs[i];
+    float gx = 0.f, gy = 0.f, gsq = 0.f, rho = 0.f;
+    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+        const float2 q = __ldg(&xs[j]);
+        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float r2 = rx * rx + ry * ry;
+        if (r2 > k.h2) { return; }
+        const float inv  = (r2 > 1e-12f) ? rsqrtf(r2) : 0.f;
+        const float dist = (inv > 0.f) ? inv * r2 : 0.f;
+        float nx, ny;
+        if (p.x != q.x || p.y != q.y) {
+            nx = rx * inv;
+            ny = ry * inv;
+        } else if (SELFG) {
+            pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
+        } else {
+            nx = 0.f;
+            ny = 0.f;
+        }
+        const float diff = k.h - dist;
+        const float sc   = -k.cs * diff * diff;
+        const float svx  = sc * nx * k.mass;
+        const float svy  = sc * ny * k.mass;
+        gx += svx;
+        gy += svy;
+        gsq += k.inv_mass * (svx * svx + svy * svy);
+        const float qq = k.h2 - r2;
+        rho += k.mass * (k.c6 * qq * qq * qq);
+    });
+    const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
+    const float self = k.inv_mass * (gx * gx + gy * gy);
+    const float grad = k.inv_rho0 * k.inv_rho0 * (self + gsq);
+    lam[i]           = -C / (grad + k.eps);
+}
+
+// ----- delta p with artificial pressure and over-relaxation, then walls (PBF.cu:398-447, 471-499) -------
+template <bool MULTI, bool SCORR>
+__global__ void __launch_bounds__(T_PART)
+    k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+              const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
+              float2* __restrict__ xs_out)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) { return; }
+    const DomDev d = load_dom<MULTI>(k, doms, dom, i);
+    const float2 p = xs[i];
+    const float li = lam[i];
+    float dx = 0.f, dy = 0.f;
+    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+        const float2 q = __ldg(&xs[j]);
+        const float lj = __ldg(&lam[j]);
+        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float r2 = rx * rx + ry * ry;
+        if (r2 > k.h2) { return; }
+        const float inv = (r2 > 1e-12f) ? rsqrtf(r2) : 0.f;
+        const float nx = rx * inv, ny = ry * inv;
+        float scorr = 0.f;
+        if (SCORR) {
+            const float qq     = k.h2 - r2;
+            const float ratio  = k.c6 * qq * qq * qq * k.inv_w_dq;
+            const float ratio2 = ratio * ratio;
+            scorr              = k.scorr_k * ratio2 * ratio2;
+        }
+        const float l    = li * k.mass + lj * k.mass - scorr;
+        const float dist = inv * r2;
+        const float diff = k.h - dist;
+        const float sc   = -k.cs * diff * diff;
+        dx += sc * nx * l;
+        dy += sc * ny * l;
+    });
+    dx *= k.dp_scale;
+    dy *= k.dp_scale;
+    float ox = p.x + dx, oy = p.y + dy;
+    // clamp<float>(v, lb, ub), PBF.cu:496-497
+    oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
+    ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
+    xs_out[i] = make_float2(ox, oy);
+}
+
+// velocityClamp, PBF.cu:629-638
+__device__ __forceinline__ void velocity_clamp(const PbfK& k, float& vx, float& vy)
+{
+    const float v2  = vx * vx + vy * vy;
+    // v2 == 0 can only pass the first test when v_min == 0 (never in the reference); avoid 0 * inf there
+    const float inv = (v2 < k.v_min2 || v2 == 0.f) ? 0.f : rsqrtf(v2);
+    const float nx = vx * inv, ny = vy * inv;
+    const float a   = v2 * inv;
+    const float sp  = fminf(a, k.v_max);
+    vx              = nx * sp;
+    vy              = ny * sp;
+}
+
+// ----- velocity + XSPH (+ vorticity omega) (PBF.cu:538, 585-627) ---------------------------------------
+template <bool MULTI, bool VORT>
+__global__ void __launch_bounds__(T_PART)
+    k_xsph(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+           const uint32_t* __restrict__ start, const float2* __restrict__ x, const float2* __restrict__ xs,
+           float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) { return; }
+    const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
+    const float2 p  = xs[i];
+    const float2 po = x[i];
+    const float vax = (p.x - po.x) * k.inv_dt, vay = (p.y - po.y) * k.inv_dt;
+    float dvx = 0.f, dvy = 0.f, w = 0.f;
+    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+        const float2 q  = __ldg(&xs[j]);
+        const float2 qo = __ldg(&x[j]);
+        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float r2 = rx * rx + ry * ry;
+        if (r2 > k.h2) { return; }
+        const float vbx = (q.x - qo.x) * k.inv_dt, vby = (q.y - qo.y) * k.inv_dt;
+        const float qq  = k.h2 - r2;
+        const float p6  = k.c6 * qq * qq * qq;
+        dvx += (vbx - vax) * p6;
+        dvy += (vby - vay) * p6;
+        if (VORT) {
+            if (r2 > 1e-12f) {
+                const float inv  = rsqrtf(r2);
+                const float diff = k.h - r2 * inv;
+                const float gm   = k.cs * diff * diff * inv; // grad_j W_ij = +cs (h-r)^2 r_ij/|r_ij|
+                w += (vbx - vax) * (gm * ry) - (vby - vay) * (gm * rx);
+            }
+        }
+    });
+    float vx = vax + dvx * k.xsph_c;
+    float vy = vay + dvy * k.xsph_c;
+    if (!VORT && (k.flags & GPE_PBF_VEL_CLAMP)) { velocity_clamp(k, vx, vy); }
+    if (!(isfinite(vx) && isfinite(vy) && isfinite(p.x) && isfinite(p.y))) {
+        atomicOr(status, GPE_STATUS_NONFINITE);
+    }
+    v_out[i] = make_float2(vx, vy);
+    if (VORT) { omega[i] = w; }
+}
+
+// ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
+template <bool MULTI>
+__global__ void __launch_bounds__(T_PART)
+    k_vorticity(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                const uint32_t* __restrict__ start, const float2* __restrict__ xs,
+                const float* __restrict__ omega, float2* __restrict__ v)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) { return; }
+    const DomDev d = load_dom<MULTI>(k, doms, dom, i);
+    const float2 p = xs[i];
+    const float wi = omega[i];
+    const float aw = fabsf(wi);
+    float ex = 0.f, ey = 0.f;
+    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+        const float2 q = __ldg(&xs[j]);
+        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float r2 = rx * rx + ry * ry;
+        if (r2 > k.h2 || r2 <= 1e-12f) { return; }
+        const float inv  = rsqrtf(r2);
+        const float diff = k.h - r2 * inv;
+        const float gm   = -k.cs * diff * diff * inv; // grad_i W_ij
+        const float dw   = fabsf(__ldg(&omega[j])) - aw;
+        ex += dw * gm * rx;
+        ey += dw * gm * ry;
+    });
+    float2 vv      = v[i];
+    const float e2 = ex * ex + ey * ey;
+    if (e2 > 1e-40f) {
+        const float il = rsqrtf(e2);
+        vv.x += k.vort_dt * (ey * il * wi);
+        vv.y += k.vort_dt * (-ex * il * wi);
+    }
+    if (k.flags & GPE_PBF_VEL_CLAMP) { velocity_clamp(k, vv.x, vv.y); }
+    v[i] = vv;
+}
+
+// ----- density for the density-error metric --------------------------------------------------------------
+template <bool MULTI>
+__global__ void __launch_bounds__(T_PART)
+    k_density(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+              const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ rho_out,
+              float* __restrict__ red)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float e         = 0.f;
+    if (i < k.n) {
+        const DomDev d = load_dom<MULTI>(k, doms, dom, i);
+        const float2 p = xs[i];
+        float rho      = 0.f;
+        for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+            const float2 q = __ldg(&xs[j]);
+            const float rx = p.x - q.x, ry = p.y - q.y;
+            const float r2 = rx * rx + ry * ry;
+            if (r2 > k.h2) { return; }
+            const float qq = k.h2 - r2;
+            rho += k.mass * (k.c6 * qq * qq * qq);
+        });
+        rho_out[i] = rho;
+        e          = fmaxf(rho * k.inv_rho0 - 1.f, 0.f);
+    }
+    // block max and sum, then one atomic each (e >= 0 so its bits order like unsigned ints)
+    float mx = e, sm = e;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    }
+    __shared__ float s_mx[T_PART / 32], s_sm[T_PART / 32];
+    if ((threadIdx.x & 31) == 0) {
+        s_mx[threadIdx.x >> 5] = mx;
+        s_sm[threadIdx.x >> 5] = sm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bm = 0.f, bs = 0.f;
+        for (int w = 0; w < T_PART / 32; ++w) {
+            bm = fmaxf(bm, s_mx[w]);
+            bs += s_sm[w];
+        }
+        atomicMax(reinterpret_cast<unsigned int*>(&red[0]), __float_as_uint(bm));
+        atomicAdd(reinterpret_cast<double*>(&red[2]), (double)bs);
+    }
+}
+
+__global__ void k_check_domains(const int32_t* __restrict__ dom, int32_t n, int32_t nd, uint32_t* status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    const int32_t d = dom[i];
+    if (d < 0 || d >= nd || (i + 1 < n && dom[i + 1] < d)) { atomicOr(status, GPE_STATUS_CAPACITY); }
+}
+
+__global__ void k_iota(uint32_t* __restrict__ a, int32_t n)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { a[i] = (uint32_t)i; }
+}
+
+} // namespace
+
+} // namespace gpe
+
+// =====================================================================================================
+// Engine object
+// =====================================================================================================
+
+using namespace gpe;
+
+struct PbfGraph {
+    cudaGraphExec_t exec = nullptr;
+    int X_end, id_end;
+};
+
+struct gpe_pbf {
+    int device = 0;
+    gpe_pbf_params prm{};
+    PbfK k{};
+    int32_t nd = 0;
+    std::vector<gpe_domain> doms;
+    std::vector<DomDev> domdev;
+    int64_t cap = 0, n = 0;
+    uint32_t ncells = 0;
+
+    void* base        = nullptr;
+    DomDev* d_doms    = nullptr;
+    float2* pos[4]    = {};
+    float2* vel       = nullptr;
+    float2* xs_tmp    = nullptr;
+    float* lam        = nullptr;
+    float* omega      = nullptr;
+    float* rho        = nullptr;
+    uint2* keyrank    = nullptr;
+    uint32_t* bucket  = nullptr;
+    uint32_t* count   = nullptr;
+    uint32_t* start   = nullptr;
+    uint32_t* bsum    = nullptr;
+    uint32_t* perm    = nullptr;
+    uint32_t* keys    = nullptr;
+    int32_t* dom      = nullptr;
+    uint32_t* ids[2]  = {};
+    uint32_t* status  = nullptr;
+    float* red        = nullptr;
+
+    // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
+    int X = 0, SX = -1, XS = -1, XO = -1;
+    int id_cur        = 0;
+    bool have_state   = false;
+    bool have_sort    = false;
+    int32_t launches  = 0;
+    std::map<std::tuple<int, int, int>, PbfGraph> graphs;
+
+    void drop_graphs()
+    {
+        for (auto& g : graphs) {
+            if (g.second.exec) { cudaGraphExecDestroy(g.second.exec); }
+        }
+        graphs.clear();
+    }
+};
+
+namespace {
+
+bool multi(const gpe_pbf* s) { return s->nd > 1; }
+
+int32_t validate_params(const gpe_pbf_params* p)
+{
+    if (!p) { return GPE_ERR_BAD_ARG; }
+    if (!(p->h > 0.f) || !(p->rho0 > 0.f) || !(p->mass > 0.f) || !(p->dt > 0.f) || p->iters < 0 ||
+        p->iters > 1000 || !(p->eps >= 0.f) || p->cell < 0.f) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "invalid PBF parameters (h, rho0, mass, dt must be > 0, iters in [0,1000])");
+        return GPE_ERR_BAD_ARG;
+    }
+    const float cell = p->cell > 0.f ? p->cell : p->h;
+    if (cell < 0.2f * p->h) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "cell size below h/5 is not supported");
+        return GPE_ERR_BAD_ARG;
+    }
+    return GPE_OK;
+}
+
+// kernel constants; the float products follow the reference's constexpr evaluation order
+PbfK make_k(const gpe_pbf_params& p)
+{
+    PbfK k{};
+    const float cell = p.cell > 0.f ? p.cell : p.h;
+    k.h              = p.h;
+    k.h2             = p.h * p.h;
+    const double hd  = p.h;
+    k.c6             = p.poly6_coeff > 0.f ? p.poly6_coeff : (float)(4.0 / (M_PI * std::pow(hd, 8)));
+    k.cs             = p.spiky_coeff > 0.f ? p.spiky_coeff : (float)(30.0 / (M_PI * std::pow(hd, 5)));
+    const float d    = k.h2 - p.scorr_dq * p.scorr_dq;
+    k.inv_w_dq       = 1.f / (k.c6 * d * d * d);
+    k.inv_cell       = 1.0f / cell;
+    k.rho0           = p.rho0;
+    k.inv_rho0       = 1.f / p.rho0;
+    k.mass           = p.mass;
+    k.inv_mass       = 1.f / p.mass;
+    k.dt             = p.dt;
+    k.inv_dt         = 1.f / p.dt;
+    const float dt2  = p.dt * p.dt;
+    k.g2x            = dt2 * p.gravity[0];
+    k.g2y            = dt2 * p.gravity[1];
+    k.eps            = p.eps;
+    k.scorr_k        = p.scorr_k;
+    k.dp_scale       = p.omega * k.inv_mass * k.inv_rho0;
+    k.c_min          = p.c_min;
+    k.xsph_c         = p.xsph_c;
+    k.vort_eps       = p.vort_eps;
+    k.vort_dt        = p.dt * p.vort_eps;
+    k.v_max          = p.v_max;
+    k.v_min2         = p.v_min * p.v_min;
+    int32_t R        = (int32_t)std::ceil(p.h / cell - 1e-4f);
+    k.R              = R < 1 ? 1 : R;
+    k.flags          = p.flags;
+    return k;
+}
+
+int32_t cells_along(float extent, float cell)
+{
+    const int32_t c = (int32_t)std::ceil(extent / cell);
+    return c < 1 ? 1 : c;
+}
+
+void build_domains(gpe_pbf* s)
+{
+    const float cell = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
+    s->domdev.resize((size_t)s->nd);
+    uint64_t off = 0;
+    for (int32_t d = 0; d < s->nd; ++d) {
+        DomDev& o = s->domdev[(size_t)d];
+        o         = DomDev{};
+        o.ox      = s->doms[(size_t)d].origin[0];
+        o.oy      = s->doms[(size_t)d].origin[1];
+        o.lox     = s->doms[(size_t)d].origin[0];
+        o.loy     = s->doms[(size_t)d].origin[1];
+        o.hix     = (s->doms[(size_t)d].origin[0] + s->doms[(size_t)d].extent[0]) - s->prm.wall_margin;
+        o.hiy     = (s->doms[(size_t)d].origin[1] + s->doms[(size_t)d].extent[1]) - s->prm.wall_margin;
+        o.ncx     = cells_along(s->doms[(size_t)d].extent[0], cell);
+        o.ncy     = cells_along(s->doms[(size_t)d].extent[1], cell);
+        o.coff    = (uint32_t)off;
+        off += (uint64_t)o.ncx * (uint64_t)o.ncy;
+    }
+    s->ncells = (uint32_t)off;
+    s->k      = make_k(s->prm);
+    s->k.d0   = s->domdev[0];
+}
+
+uint64_t count_cells(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd)
+{
+    const float cell = p->cell > 0.f ? p->cell : p->h;
+    uint64_t off     = 0;
+    for (int32_t d = 0; d < nd; ++d) {
+        off += (uint64_t)cells_along(doms[d].extent[0], cell) * (uint64_t)cells_along(doms[d].extent[1], cell);
+    }
+    return off;
+}
+
+unsigned blocks_for(int64_t n) { return (unsigned)((n + T_PART - 1) / T_PART); }
+
+// ----- stage launchers ----------------------------------------------------------------------------------
+
+int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
+{
+    const int32_t n = (int32_t)s->n;
+    // roles for this step: the three buffers other than X, in order
+    int fr[3], c = 0;
+    for (int b = 0; b < 4; ++b) {
+        if (b != s->X) { fr[c++] = b; }
+    }
+    s->SX = fr[0];
+    s->XS = fr[1];
+    s->XO = fr[2];
+    s->k.n = n;
+    if (n > 0) {
+        if (multi(s)) {
+            k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X], s->vel,
+                                                                   s->xs_tmp, s->keyrank, s->count);
+        } else {
+            k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X],
+                                                                    s->vel, s->xs_tmp, s->keyrank, s->count);
+        }
+        GPE_CHECK_LAUNCH("k_predict_hist");
+    }
+    int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st);
+    if (rc) { return rc; }
+    rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st);
+    if (rc) { return rc; }
+    if (n > 0) {
+        const bool ids = (s->prm.flags & GPE_PBF_TRACK_IDS) != 0;
+        k_place<<<blocks_for(n), T_PART, 0, st>>>(n, s->keyrank, s->start, s->bucket, s->pos[s->X], s->xs_tmp,
+                                                  s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
+                                                  ids ? s->ids[s->id_cur] : nullptr,
+                                                  ids ? s->ids[s->id_cur ^ 1] : nullptr);
+        GPE_CHECK_LAUNCH("k_place");
+        if (ids) { s->id_cur ^= 1; }
+    }
+    s->have_sort = true;
+    s->launches += 6;
+    return GPE_OK;
+}
+
+int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
+{
+    if (s->n == 0) { return GPE_OK; }
+    const bool sg = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0;
+    const unsigned g = blocks_for(s->n);
+    if (multi(s)) {
+        if (sg) {
+            k_lambda<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+        } else {
+            k_lambda<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+        }
+    } else {
+        if (sg) {
+            k_lambda<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+        } else {
+            k_lambda<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
+                                                         s->lam);
+        }
+    }
+    GPE_CHECK_LAUNCH("k_lambda");
+    s->launches += 1;
+    return GPE_OK;
+}
+
+int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
+{
+    if (s->n > 0) {
+        const bool sc    = s->prm.scorr_k != 0.f;
+        const unsigned g = blocks_for(s->n);
+        float2* in       = s->pos[s->XS];
+        float2* out      = s->pos[s->XO];
+        if (multi(s)) {
+            if (sc) {
+                k_delta_p<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
+            } else {
+                k_delta_p<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
+            }
+        } else {
+            if (sc) {
+                k_delta_p<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
+            } else {
+                k_delta_p<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam,
+                                                               out);
+            }
+        }
+        GPE_CHECK_LAUNCH("k_delta_p");
+        s->launches += 1;
+    }
+    std::swap(s->XS, s->XO);
+    return GPE_OK;
+}
+
+int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
+{
+    if (s->n == 0) { return GPE_OK; }
+    const bool vort  = s->prm.vort_eps != 0.f;
+    const unsigned g = blocks_for(s->n);
+    if (multi(s)) {
+        if (vort) {
+            k_xsph<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+                                                     s->pos[s->XS], s->vel, s->omega, s->status);
+        } else {
+            k_xsph<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+                                                      s->pos[s->XS], s->vel, s->omega, s->status);
+        }
+    } else {
+        if (vort) {
+            k_xsph<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+                                                      s->pos[s->XS], s->vel, s->omega, s->status);
+        } else {
+            k_xsph<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+                                                       s->pos[s->XS], s->vel, s->omega, s->status);
+        }
+    }
+    GPE_CHECK_LAUNCH("k_xsph");
+    s->launches += 1;
+    return GPE_OK;
+}
+
+int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
+{
+    if (s->n == 0 || s->prm.vort_eps == 0.f) { return GPE_OK; }
+    const unsigned g = blocks_for(s->n);
+    if (multi(s)) {
+        k_vorticity<true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega, s->vel);
+    } else {
+        k_vorticity<false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega,
+                                                 s->vel);
+    }
+    GPE_CHECK_LAUNCH("k_vorticity");
+    s->launches += 1;
+    return GPE_OK;
+}
+
+int32_t stage_finish(gpe_pbf* s)
+{
+    s->X  = s->XS;
+    s->SX = s->XS = s->XO = -1;
+    return GPE_OK;
+}
+
+int32_t run_step(gpe_pbf* s, cudaStream_t st)
+{
+    int32_t rc = stage_predict_sort(s, st);
+    for (int32_t it = 0; it < s->prm.iters && rc == GPE_OK; ++it) {
+        rc = stage_lambda(s, st);
+        if (rc == GPE_OK) { rc = stage_delta_p(s, st); }
+    }
+    if (rc == GPE_OK) { rc = stage_xsph(s, st); }
+    if (rc == GPE_OK) { rc = stage_vorticity(s, st); }
+    if (rc == GPE_OK) { rc = stage_finish(s); }
+    return rc;
+}
+
+int32_t alloc_buffers(gpe_pbf* s)
+{
+    const size_t N = (size_t)s->cap;
+    const size_t M = (size_t)s->ncells;
+    Carver c;
+    const size_t o_doms = c.take<DomDev>((size_t)s->nd);
+    size_t o_pos[4];
+    for (int b = 0; b < 4; ++b) { o_pos[b] = c.take<float2>(N); }
+    const size_t o_vel   = c.take<float2>(N);
+    const size_t o_xst   = c.take<float2>(N);
+    const size_t o_lam   = c.take<float>(N);
+    const size_t o_om    = c.take<float>(N);
+    const size_t o_rho   = c.take<float>(N);
+    const size_t o_kr    = c.take<uint2>(N);
+    const size_t o_bk    = c.take<uint32_t>(N);
+    const size_t o_cnt   = c.take<uint32_t>(M);
+    const size_t o_st    = c.take<uint32_t>(M + 1);
+    const size_t o_bs    = c.take<uint32_t>(scan_blocks((uint32_t)M) + 1);
+    const size_t o_perm  = c.take<uint32_t>(N);
+    const size_t o_keys  = c.take<uint32_t>(N);
+    const size_t o_dom   = c.take<int32_t>(N);
+    const size_t o_id0   = c.take<uint32_t>(N);
+    const size_t o_id1   = c.take<uint32_t>(N);
+    const size_t o_stat  = c.take<uint32_t>(4);
+    const size_t o_red   = c.take<float>(8);
+    GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
+    GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
+    uint8_t* b = static_cast<uint8_t*>(s->base);
+    s->d_doms  = reinterpret_cast<DomDev*>(b + o_doms);
+    for (int q = 0; q < 4; ++q) { s->pos[q] = reinterpret_cast<float2*>(b + o_pos[q]); }
+    s->vel     = reinterpret_cast<float2*>(b + o_vel);
+    s->xs_tmp  = reinterpret_cast<float2*>(b + o_xst);
+    s->lam     = reinterpret_cast<float*>(b + o_lam);
+    s->omega   = reinterpret_cast<float*>(b + o_om);
+    s->rho     = reinterpret_cast<float*>(b + o_rho);
+    s->keyrank = reinterpret_cast<uint2*>(b + o_kr);
+    s->bucket  = reinterpret_cast<uint32_t*>(b + o_bk);
+    s->count   = reinterpret_cast<uint32_t*>(b + o_cnt);
+    s->start   = reinterpret_cast<uint32_t*>(b + o_st);
+    s->bsum    = reinterpret_cast<uint32_t*>(b + o_bs);
+    s->perm    = reinterpret_cast<uint32_t*>(b + o_perm);
+    s->keys    = reinterpret_cast<uint32_t*>(b + o_keys);
+    s->dom     = reinterpret_cast<int32_t*>(b + o_dom);
+    s->ids[0]  = reinterpret_cast<uint32_t*>(b + o_id0);
+    s->ids[1]  = reinterpret_cast<uint32_t*>(b + o_id1);
+    s->status  = reinterpret_cast<uint32_t*>(b + o_stat);
+    s->red     = reinterpret_cast<float*>(b + o_red);
+    GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
+    return GPE_OK;
+}
+
+cudaMemcpyKind kind_in(int32_t mem) { return mem == GPE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+cudaMemcpyKind kind_out(int32_t mem) { return mem == GPE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost; }
+
+} // namespace
+
+// =====================================================================================================
+// C ABI
+// =====================================================================================================
+
+extern "C" {
+
+int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, int32_t n_domains, int64_t capacity,
+                       gpe_pbf** out)
+{
+    gpe::clear_error();
+    if (!out || !domains || n_domains <= 0 || capacity < 0 || capacity > (int64_t)INT32_MAX / 2) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_create: bad arguments");
+        return GPE_ERR_BAD_ARG;
+    }
+    *out       = nullptr;
+    int32_t rc = validate_params(params);
+    if (rc) { return rc; }
+    for (int32_t d = 0; d < n_domains; ++d) {
+        if (!(domains[d].extent[0] > 0.f) || !(domains[d].extent[1] > 0.f)) {
+            gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_create: scene %d has a non-positive extent", d);
+            return GPE_ERR_BAD_ARG;
+        }
+    }
+    const uint64_t cells = count_cells(params, domains, n_domains);
+    if (cells == 0 || cells > (uint64_t)1 << 30) {
+        gpe::set_error(GPE_ERR_CAPACITY, "gpe_pbf_create: %llu cells exceed the 2^30 limit",
+                       (unsigned long long)cells);
+        return GPE_ERR_CAPACITY;
+    }
+    int dev = 0;
+    rc      = gpe::current_device(&dev);
+    if (rc) { return rc; }
+    gpe_pbf* s = new gpe_pbf();
+    s->device  = dev;
+    s->prm     = *params;
+    s->nd      = n_domains;
+    s->doms.assign(domains, domains + n_domains);
+    s->cap = capacity;
+    build_domains(s);
+    rc = alloc_buffers(s);
+    if (rc) {
+        if (s->base) { cudaFree(s->base); }
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_destroy(gpe_pbf* s)
+{
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    s->drop_graphs();
+    if (s->base) { cudaFree(s->base); }
+    delete s;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_set_params(gpe_pbf* s, const gpe_pbf_params* params)
+{
+    gpe::clear_error();
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    int32_t rc = validate_params(params);
+    if (rc) { return rc; }
+    const float c_old = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
+    const float c_new = params->cell > 0.f ? params->cell : params->h;
+    if (c_old != c_new) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_params: the sort-cell size is fixed at creation");
+        return GPE_ERR_BAD_ARG;
+    }
+    s->prm = *params;
+    build_domains(s);
+    GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
+    s->drop_graphs();
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_get_params(const gpe_pbf* s, gpe_pbf_params* params)
+{
+    if (!s || !params) { return GPE_ERR_BAD_ARG; }
+    *params = s->prm;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const int32_t* domain_id, int64_t n,
+                          int32_t mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n < 0 || (n > 0 && !pos) || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_state: bad arguments");
+        return GPE_ERR_BAD_ARG;
+    }
+    if (n > s->cap) {
+        gpe::set_error(GPE_ERR_CAPACITY, "gpe_pbf_set_state: %lld particles exceed capacity %lld", (long long)n,
+                       (long long)s->cap);
+        return GPE_ERR_CAPACITY;
+    }
+    if (s->nd > 1 && n > 0 && !domain_id) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_state: domain_id is required with several scenes");
+        return GPE_ERR_BAD_ARG;
+    }
+    if (s->nd > 1 && mem == GPE_MEM_HOST) {
+        for (int64_t i = 0; i < n; ++i) {
+            if (domain_id[i] < 0 || domain_id[i] >= s->nd || (i > 0 && domain_id[i] < domain_id[i - 1])) {
+                gpe::set_error(GPE_ERR_BAD_ARG,
+                               "gpe_pbf_set_state: domain_id must be in [0, n_domains) and non-decreasing");
+                return GPE_ERR_BAD_ARG;
+            }
+        }
+    }
+    cudaStream_t st = as_stream(stream);
+    s->X            = 0;
+    s->SX = s->XS = s->XO = -1;
+    s->id_cur     = 0;
+    if (n > 0) {
+        GPE_TRY_CUDA(cudaMemcpyAsync(s->pos[0], pos, sizeof(float2) * (size_t)n, kind_in(mem), st));
+        if (vel) {
+            GPE_TRY_CUDA(cudaMemcpyAsync(s->vel, vel, sizeof(float2) * (size_t)n, kind_in(mem), st));
+        } else {
+            GPE_TRY_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float2) * (size_t)n, st));
+        }
+        if (s->nd > 1) {
+            GPE_TRY_CUDA(cudaMemcpyAsync(s->dom, domain_id, sizeof(int32_t) * (size_t)n, kind_in(mem), st));
+            if (mem == GPE_MEM_DEVICE) {
+                k_check_domains<<<blocks_for(n), T_PART, 0, st>>>(s->dom, (int32_t)n, s->nd, s->status);
+                GPE_CHECK_LAUNCH("k_check_domains");
+                uint32_t stt = 0;
+                GPE_TRY_CUDA(cudaMemcpyAsync(&stt, s->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+                GPE_TRY_CUDA(cudaStreamSynchronize(st));
+                if (stt & GPE_STATUS_CAPACITY) {
+                    GPE_TRY_CUDA(cudaMemsetAsync(s->status, 0, sizeof(uint32_t), st));
+                    gpe::set_error(GPE_ERR_BAD_ARG,
+                                   "gpe_pbf_set_state: domain_id must be in [0, n_domains) and non-decreasing");
+                    return GPE_ERR_BAD_ARG;
+                }
+            }
+        }
+        k_iota<<<blocks_for(n), T_PART, 0, st>>>(s->ids[0], (int32_t)n);
+        GPE_CHECK_LAUNCH("k_iota");
+    }
+    if (s->n != n) { s->drop_graphs(); }
+    s->n          = n;
+    s->have_state = true;
+    s->have_sort  = false;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id, int64_t n, int32_t mem,
+                          void* stream)
+{
+    gpe::clear_error();
+    if (!s || n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_state: n must equal the particle count");
+        return GPE_ERR_BAD_ARG;
+    }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    if (n > 0) {
+        if (pos) { GPE_TRY_CUDA(cudaMemcpyAsync(pos, s->pos[s->X], sizeof(float2) * (size_t)n, kind_out(mem), st)); }
+        if (vel) { GPE_TRY_CUDA(cudaMemcpyAsync(vel, s->vel, sizeof(float2) * (size_t)n, kind_out(mem), st)); }
+        if (domain_id) {
+            if (s->nd > 1) {
+                GPE_TRY_CUDA(cudaMemcpyAsync(domain_id, s->dom, sizeof(int32_t) * (size_t)n, kind_out(mem), st));
+            } else if (mem == GPE_MEM_HOST) {
+                GPE_TRY_CUDA(cudaStreamSynchronize(st));
+                std::memset(domain_id, 0, sizeof(int32_t) * (size_t)n);
+            } else {
+                GPE_TRY_CUDA(cudaMemsetAsync(domain_id, 0, sizeof(int32_t) * (size_t)n, st));
+            }
+        }
+    }
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_count(const gpe_pbf* s, int64_t* n)
+{
+    if (!s || !n) { return GPE_ERR_BAD_ARG; }
+    *n = s->n;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_num_cells(const gpe_pbf* s, int64_t* n_cells)
+{
+    if (!s || !n_cells) { return GPE_ERR_BAD_ARG; }
+    *n_cells = (int64_t)s->ncells;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_step: no state set");
+        return GPE_ERR_NOT_READY;
+    }
+    if (n_steps == 0) { return GPE_OK; }
+    cudaStream_t st = as_stream(stream);
+    // the step sequence is captured once per (steps, starting buffer roles) and replayed as one graph
+    const auto key = std::make_tuple(n_steps, s->X, s->id_cur);
+    auto it        = s->graphs.find(key);
+    if (it == s->graphs.end()) {
+        cudaStream_t cap_st = st;
+        bool own            = false;
+        if (cap_st == nullptr) {
+            GPE_TRY_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
+            own = true;
+        }
+        const int X0 = s->X, id0 = s->id_cur;
+        GPE_TRY_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+        s->launches = 0;
+        int32_t rc  = GPE_OK;
+        for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, cap_st); }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(cap_st, &graph);
+        PbfGraph pg;
+        pg.X_end  = s->X;
+        pg.id_end = s->id_cur;
+        s->X      = X0;
+        s->id_cur = id0;
+        if (rc == GPE_OK && ce != cudaSuccess) {
+            gpe::set_cuda_error(ce, "cudaStreamEndCapture");
+            rc = GPE_ERR_CUDA;
+        }
+        if (rc == GPE_OK) {
+            const cudaError_t ie = cudaGraphInstantiate(&pg.exec, graph, 0);
+            if (ie != cudaSuccess) {
+                gpe::set_cuda_error(ie, "cudaGraphInstantiate");
+                rc = GPE_ERR_CUDA;
+            }
+        }
+        if (graph) { cudaGraphDestroy(graph); }
+        if (own) { cudaStreamDestroy(cap_st); }
+        if (rc) { return rc; }
+        s->launches /= n_steps;
+        it = s->graphs.emplace(key, pg).first;
+    }
+    GPE_TRY_CUDA(cudaGraphLaunch(it->second.exec, st));
+    s->X         = it->second.X_end;
+    s->id_cur    = it->second.id_end;
+    s->have_sort = true;
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
+{
+    gpe::clear_error();
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    const bool in_step = s->SX >= 0;
+    switch (stage) {
+        case GPE_PBF_STAGE_PREDICT_SORT:
+            if (in_step) { break; }
+            return stage_predict_sort(s, st);
+        case GPE_PBF_STAGE_LAMBDA:
+            if (!in_step) { break; }
+            return stage_lambda(s, st);
+        case GPE_PBF_STAGE_DELTA_P:
+            if (!in_step) { break; }
+            return stage_delta_p(s, st);
+        case GPE_PBF_STAGE_XSPH:
+            if (!in_step) { break; }
+            return stage_xsph(s, st);
+        case GPE_PBF_STAGE_VORTICITY:
+            if (!in_step) { break; }
+            return stage_vorticity(s, st);
+        case GPE_PBF_STAGE_FINISH:
+            if (!in_step) { break; }
+            return stage_finish(s);
+        case GPE_PBF_STAGE_DENSITY: {
+            if (!s->have_sort || in_step) { break; }
+            GPE_TRY_CUDA(cudaMemsetAsync(s->red, 0, sizeof(float) * 8, st));
+            if (s->n > 0) {
+                s->k.n = (int32_t)s->n;
+                if (multi(s)) {
+                    k_density<true><<<blocks_for(s->n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                         s->pos[s->X], s->rho, s->red);
+                } else {
+                    k_density<false><<<blocks_for(s->n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                          s->pos[s->X], s->rho, s->red);
+                }
+                GPE_CHECK_LAUNCH("k_density");
+            }
+            return GPE_OK;
+        }
+        default:
+            gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_stage: unknown stage %d", stage);
+            return GPE_ERR_BAD_ARG;
+    }
+    gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_stage: stage %d is out of order", stage);
+    return GPE_ERR_NOT_READY;
+}
+
+int32_t gpe_pbf_density_error(gpe_pbf* s, float* max_err, float* mean_err, void* stream)
+{
+    if (!s || !max_err || !mean_err) { return GPE_ERR_BAD_ARG; }
+    int32_t rc = gpe_pbf_stage(s, GPE_PBF_STAGE_DENSITY, stream);
+    if (rc) { return rc; }
+    float red[8];
+    cudaStream_t st = as_stream(stream);
+    GPE_TRY_CUDA(cudaMemcpyAsync(red, s->red, sizeof(red), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    double sum;
+    std::memcpy(&sum, &red[2], sizeof(double));
+    *max_err  = red[0];
+    *mean_err = s->n > 0 ? (float)(sum / (double)s->n) : 0.f;
+    return GPE_OK;
+}
+
+static int32_t field_ptr(gpe_pbf* s, int32_t field, void** p, size_t* esize, int64_t* count)
+{
+    const bool in_step = s->SX >= 0;
+    *count             = s->n;
+    switch (field) {
+        case GPE_PBF_FIELD_POS: *p = s->pos[in_step ? s->SX : s->X]; *esize = 8; break;
+        case GPE_PBF_FIELD_VEL: *p = s->vel; *esize = 8; break;
+        case GPE_PBF_FIELD_PRED:
+            if (!in_step) { return GPE_ERR_NOT_READY; }
+            *p = s->pos[s->XS]; *esize = 8; break;
+        case GPE_PBF_FIELD_LAMBDA: *p = s->lam; *esize = 4; break;
+        case GPE_PBF_FIELD_KEY: *p = s->keys; *esize = 4; break;
+        case GPE_PBF_FIELD_PERM: *p = s->perm; *esize = 4; break;
+        case GPE_PBF_FIELD_CELL_START: *p = s->start; *esize = 4; *count = (int64_t)s->ncells + 1; break;
+        case GPE_PBF_FIELD_DOMAIN: *p = s->dom; *esize = 4; break;
+        case GPE_PBF_FIELD_DENSITY: *p = s->rho; *esize = 4; break;
+        case GPE_PBF_FIELD_ID: *p = s->ids[s->id_cur]; *esize = 4; break;
+        case GPE_PBF_FIELD_OMEGA: *p = s->omega; *esize = 4; break;
+        default: return GPE_ERR_BAD_ARG;
+    }
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_get_field(gpe_pbf* s, int32_t field, void* dst, int64_t n_elems, int32_t mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !dst || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    void* p;
+    size_t es;
+    int64_t cnt;
+    int32_t rc = field_ptr(s, field, &p, &es, &cnt);
+    if (rc) {
+        gpe::set_error(rc, "gpe_pbf_get_field: field %d unavailable", field);
+        return rc;
+    }
+    if (n_elems != cnt) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_field: field %d has %lld elements", field, (long long)cnt);
+        return GPE_ERR_BAD_ARG;
+    }
+    cudaStream_t st = as_stream(stream);
+    if (cnt > 0) { GPE_TRY_CUDA(cudaMemcpyAsync(dst, p, es * (size_t)cnt, kind_out(mem), st)); }
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_set_field(gpe_pbf* s, int32_t field, const void* src, int64_t n_elems, int32_t mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !src || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    if (field == GPE_PBF_FIELD_KEY || field == GPE_PBF_FIELD_PERM || field == GPE_PBF_FIELD_CELL_START ||
+        field == GPE_PBF_FIELD_DOMAIN) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_field: field %d is derived and read-only", field);
+        return GPE_ERR_BAD_ARG;
+    }
+    void* p;
+    size_t es;
+    int64_t cnt;
+    int32_t rc = field_ptr(s, field, &p, &es, &cnt);
+    if (rc) { return rc; }
+    if (n_elems != cnt) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    if (cnt > 0) { GPE_TRY_CUDA(cudaMemcpyAsync(p, src, es * (size_t)cnt, kind_in(mem), st)); }
+    if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_status(gpe_pbf* s, uint32_t* status, void* stream)
+{
+    if (!s || !status) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    GPE_TRY_CUDA(cudaMemcpyAsync(status, s->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaMemsetAsync(s->status, 0, sizeof(uint32_t), st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    return GPE_OK;
+}
+
+int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
+{
+    if (!s || !launches) { return GPE_ERR_BAD_ARG; }
+    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0);
+    return GPE_OK;
+}
+
+} // extern "C"

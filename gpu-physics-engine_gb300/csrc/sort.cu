@@ -1,0 +1,158 @@
+// sort.cu — the device-wide pieces of the cell counting sort: exclusive scan of the cell histogram and the
+// scatter of (cell, rank) pairs into cell buckets.
+//
+// The reference sorts each 16x16-cell chunk inside one block: a shared-memory histogram by atomicAdd
+// (PBF.cu:786-797), a 256-wide scan incPrefSum256 (PBF.cu:835-860) and a shared-memory scatter
+// (PBF.cu:806-833). Chunks here are not bounded by shared memory (a scene holds up to millions of
+// particles and cells), so the histogram and the scan run device-wide: the histogram is fused into the
+// predict kernel (pbf.cu), the scan below is the usual reduce / scan-of-block-sums / down-sweep over tiles of
+// 2048 cells, and the stable placement is finished by pbf.cu's gather kernel.
+#include "gpe_internal.h"
+
+namespace gpe {
+
+namespace {
+
+constexpr int SCAN_T    = 256;
+constexpr int SCAN_I    = 8;
+constexpr int SCAN_TILE = SCAN_T * SCAN_I;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) { v += t; }
+    }
+    return v;
+}
+
+// exclusive scan of one value per thread across a 256-thread block; returns the block total in *total
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total)
+{
+    __shared__ uint32_t s_warp[SCAN_T / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) { s_warp[warp] = inc; }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < SCAN_T / 32 ? s_warp[lane] : 0u;
+        w          = warp_incl_scan(w);
+        if (lane < SCAN_T / 32) { s_warp[lane] = w; }
+    }
+    __syncthreads();
+    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    *total                = s_warp[SCAN_T / 32 - 1];
+    __syncthreads();
+    return before + inc - v;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t* __restrict__ count, uint32_t M,
+                                                        uint32_t* __restrict__ bsum)
+{
+    const uint32_t base = blockIdx.x * SCAN_TILE;
+    uint32_t s          = 0;
+#pragma unroll
+    for (int t = 0; t < SCAN_I; ++t) {
+        const uint32_t idx = base + t * SCAN_T + threadIdx.x;
+        if (idx < M) { s += count[idx]; }
+    }
+    uint32_t total;
+    block_excl_scan(s, &total);
+    if (threadIdx.x == 0) { bsum[blockIdx.x] = total; }
+}
+
+// one block: in-place exclusive scan of the block sums
+__global__ void __launch_bounds__(SCAN_T) k_scan_bsum(uint32_t* __restrict__ bsum, uint32_t nb)
+{
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nb; base += SCAN_T) {
+        const uint32_t idx = base + threadIdx.x;
+        const uint32_t v   = idx < nb ? bsum[idx] : 0u;
+        uint32_t total;
+        const uint32_t ex = block_excl_scan(v, &total);
+        if (idx < nb) { bsum[idx] = carry + ex; }
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ count, uint32_t M,
+                                                      const uint32_t* __restrict__ bsum,
+                                                      uint32_t* __restrict__ start)
+{
+    __shared__ uint32_t s_tile[SCAN_TILE];
+    const uint32_t base = blockIdx.x * SCAN_TILE;
+    // coalesced load, and zero the histogram for the next sort
+#pragma unroll
+    for (int t = 0; t < SCAN_I; ++t) {
+        const uint32_t li  = t * SCAN_T + threadIdx.x;
+        const uint32_t idx = base + li;
+        uint32_t c         = 0;
+        if (idx < M) {
+            c          = count[idx];
+            count[idx] = 0u;
+        }
+        s_tile[li] = c;
+    }
+    __syncthreads();
+    // each thread owns SCAN_I consecutive cells
+    uint32_t loc[SCAN_I];
+    uint32_t s = 0;
+#pragma unroll
+    for (int t = 0; t < SCAN_I; ++t) {
+        loc[t] = s;
+        s += s_tile[threadIdx.x * SCAN_I + t];
+    }
+    uint32_t total;
+    const uint32_t ex  = block_excl_scan(s, &total);
+    const uint32_t off = bsum[blockIdx.x] + ex;
+#pragma unroll
+    for (int t = 0; t < SCAN_I; ++t) { s_tile[threadIdx.x * SCAN_I + t] = off + loc[t]; }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < SCAN_I; ++t) {
+        const uint32_t li  = t * SCAN_T + threadIdx.x;
+        const uint32_t idx = base + li;
+        if (idx < M) { start[idx] = s_tile[li]; }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = bsum[blockIdx.x] + total; }
+}
+
+__global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n, const uint32_t* __restrict__ start,
+                          uint32_t* __restrict__ bucket)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) { return; }
+    const uint2 kr                  = keyrank[i];
+    bucket[__ldg(&start[kr.x]) + kr.y] = (uint32_t)i;
+}
+
+} // namespace
+
+size_t scan_blocks(uint32_t n_keys) { return (n_keys + SCAN_TILE - 1) / SCAN_TILE; }
+
+int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, uint32_t* start,
+                              cudaStream_t st)
+{
+    const uint32_t nb = (uint32_t)scan_blocks(n_keys);
+    if (nb == 0) { return GPE_ERR_BAD_ARG; }
+    k_scan_reduce<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
+    GPE_CHECK_LAUNCH("k_scan_reduce");
+    k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
+    GPE_CHECK_LAUNCH("k_scan_bsum");
+    k_scan_down<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
+    GPE_CHECK_LAUNCH("k_scan_down");
+    return GPE_OK;
+}
+
+int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, cudaStream_t st)
+{
+    if (n <= 0) { return GPE_OK; }
+    const int T = 256;
+    k_scatter<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(keyrank, n, start, bucket);
+    GPE_CHECK_LAUNCH("k_scatter");
+    return GPE_OK;
+}
+
+} // namespace gpe

@@ -1,0 +1,357 @@
+"""ctypes binding of libgpe.so (include/gpe.h): the host-side handle API of the PBF and MLS-MPM engines.
+
+The library is loaded from the package directory; importing this module fails loudly if it has not been
+built (run gpu-physics-engine_gb300/build.py, or __graft_entry__.build()). There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_DIR / "libgpe.so"
+
+# ----- constants (include/gpe.h) -------------------------------------------------------------------------
+OK, ERR_CUDA, ERR_DEVICE, ERR_NOT_READY, ERR_BAD_ARG, ERR_ALREADY, ERR_CAPACITY, ERR_NONFINITE, ERR_TIMEOUT = (
+    0, -1, -2, -3, -4, -5, -6, -7, -8)
+MEM_HOST, MEM_DEVICE = 0, 1
+STATUS_NONFINITE, STATUS_CAPACITY, STATUS_CELL_OVERFLOW, STATUS_TIMEOUT = 1, 2, 4, 8
+
+PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS = 0x1, 0x2, 0x4
+(PBF_STAGE_PREDICT_SORT, PBF_STAGE_LAMBDA, PBF_STAGE_DELTA_P, PBF_STAGE_XSPH, PBF_STAGE_VORTICITY,
+ PBF_STAGE_FINISH, PBF_STAGE_DENSITY) = range(7)
+(PBF_FIELD_POS, PBF_FIELD_VEL, PBF_FIELD_PRED, PBF_FIELD_LAMBDA, PBF_FIELD_KEY, PBF_FIELD_PERM,
+ PBF_FIELD_CELL_START, PBF_FIELD_DOMAIN, PBF_FIELD_DENSITY, PBF_FIELD_ID, PBF_FIELD_OMEGA) = range(11)
+
+MPM_MAT_FLUID, MPM_MAT_COROTATED, MPM_MAT_SNOW = 0, 1, 2
+MPM_BC_SLIP, MPM_BC_STICKY = 0, 1
+MPM_FLAG_PER_PARTICLE_MATERIAL, MPM_FLAG_FLUID_F = 0x1, 0x2
+MPM_STAGE_CLEAR, MPM_STAGE_P2G, MPM_STAGE_GRID, MPM_STAGE_G2P, MPM_STAGE_SORT = range(5)
+
+
+class PbfParams(C.Structure):
+    _fields_ = [("h", C.c_float), ("cell", C.c_float), ("rho0", C.c_float), ("mass", C.c_float),
+                ("dt", C.c_float), ("gravity", C.c_float * 2), ("iters", C.c_int32), ("eps", C.c_float),
+                ("scorr_k", C.c_float), ("scorr_dq", C.c_float), ("omega", C.c_float), ("c_min", C.c_float),
+                ("xsph_c", C.c_float), ("vort_eps", C.c_float), ("v_max", C.c_float), ("v_min", C.c_float),
+                ("wall_margin", C.c_float), ("poly6_coeff", C.c_float), ("spiky_coeff", C.c_float),
+                ("flags", C.c_uint32)]
+
+    def copy(self) -> "PbfParams":
+        o = PbfParams()
+        C.pointer(o)[0] = self
+        return o
+
+
+class Domain(C.Structure):
+    _fields_ = [("origin", C.c_float * 2), ("extent", C.c_float * 2)]
+
+
+class MpmParams(C.Structure):
+    _fields_ = [("dx", C.c_float), ("grid_offset", C.c_float), ("nx", C.c_int32), ("ny", C.c_int32),
+                ("dt", C.c_float), ("gravity", C.c_float * 2), ("mass", C.c_float), ("vol0", C.c_float),
+                ("bc_type", C.c_int32), ("bc_width", C.c_int32), ("clamp_lo", C.c_float * 2),
+                ("clamp_hi", C.c_float * 2), ("material", C.c_int32), ("k_bulk", C.c_float),
+                ("gamma", C.c_float), ("p_min", C.c_float), ("p_max", C.c_float), ("J_min", C.c_float),
+                ("J_max", C.c_float), ("E", C.c_float), ("nu", C.c_float), ("theta_c", C.c_float),
+                ("theta_s", C.c_float), ("hardening", C.c_float), ("sort_interval", C.c_int32),
+                ("flags", C.c_uint32)]
+
+    def copy(self) -> "MpmParams":
+        o = MpmParams()
+        C.pointer(o)[0] = self
+        return o
+
+
+def make_domains(boxes) -> "C.Array":
+    arr = (Domain * len(boxes))()
+    for i, (ox, oy, ex, ey) in enumerate(boxes):
+        arr[i].origin[0], arr[i].origin[1] = ox, oy
+        arr[i].extent[0], arr[i].extent[1] = ex, ey
+    return arr
+
+
+# ----- library loading -----------------------------------------------------------------------------------
+_lib = None
+
+PBF_EXPORTS = ["gpe_pbf_create", "gpe_pbf_destroy", "gpe_pbf_set_params", "gpe_pbf_get_params",
+               "gpe_pbf_set_state", "gpe_pbf_get_state", "gpe_pbf_count", "gpe_pbf_num_cells", "gpe_pbf_step",
+               "gpe_pbf_stage", "gpe_pbf_get_field", "gpe_pbf_set_field", "gpe_pbf_density_error",
+               "gpe_pbf_status", "gpe_pbf_launches_per_step"]
+MPM_EXPORTS = ["gpe_mpm_create", "gpe_mpm_destroy", "gpe_mpm_set_params", "gpe_mpm_set_state",
+               "gpe_mpm_get_state", "gpe_mpm_count", "gpe_mpm_step", "gpe_mpm_stage", "gpe_mpm_get_grid",
+               "gpe_mpm_status", "gpe_mpm_launches_per_step"]
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"libgpe.so is not built ({LIB_PATH}); run gpu-physics-engine_gb300/build.py")
+        L = C.CDLL(str(LIB_PATH))
+        vp, i32, i64, f32p = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_float)
+        L.gpe_error_name.restype = C.c_char_p
+        L.gpe_error_name.argtypes = [i32]
+        L.gpe_last_error_message.restype = C.c_char_p
+        L.gpe_last_cuda_error.restype = i32
+        L.gpe_version.restype = i32
+        sig = {
+            "gpe_pbf_create": [C.POINTER(PbfParams), C.POINTER(Domain), i32, i64, C.POINTER(vp)],
+            "gpe_pbf_destroy": [vp],
+            "gpe_pbf_set_params": [vp, C.POINTER(PbfParams)],
+            "gpe_pbf_get_params": [vp, C.POINTER(PbfParams)],
+            "gpe_pbf_set_state": [vp, vp, vp, vp, i64, i32, vp],
+            "gpe_pbf_get_state": [vp, vp, vp, vp, i64, i32, vp],
+            "gpe_pbf_count": [vp, C.POINTER(i64)],
+            "gpe_pbf_num_cells": [vp, C.POINTER(i64)],
+            "gpe_pbf_step": [vp, i32, vp],
+            "gpe_pbf_stage": [vp, i32, vp],
+            "gpe_pbf_get_field": [vp, i32, vp, i64, i32, vp],
+            "gpe_pbf_set_field": [vp, i32, vp, i64, i32, vp],
+            "gpe_pbf_density_error": [vp, f32p, f32p, vp],
+            "gpe_pbf_status": [vp, C.POINTER(C.c_uint32), vp],
+            "gpe_pbf_launches_per_step": [vp, C.POINTER(i32)],
+            "gpe_mpm_create": [C.POINTER(MpmParams), i64, C.POINTER(vp)],
+            "gpe_mpm_destroy": [vp],
+            "gpe_mpm_set_params": [vp, C.POINTER(MpmParams)],
+            "gpe_mpm_set_state": [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp],
+            "gpe_mpm_get_state": [vp, vp, vp, vp, vp, vp, i64, i32, vp],
+            "gpe_mpm_count": [vp, C.POINTER(i64)],
+            "gpe_mpm_step": [vp, i32, vp],
+            "gpe_mpm_stage": [vp, i32, vp],
+            "gpe_mpm_get_grid": [vp, vp, i64, i32, vp],
+            "gpe_mpm_status": [vp, C.POINTER(C.c_uint32), vp],
+            "gpe_mpm_launches_per_step": [vp, C.POINTER(i32)],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = i32
+        _lib = L
+    return _lib
+
+
+class GpeError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        L = lib()
+        msg = L.gpe_last_error_message().decode(errors="replace")
+        super().__init__(f"{where}: {L.gpe_error_name(status).decode()} ({status}) {msg}")
+        self.status = status
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise GpeError(status, where)
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array (host) or a torch tensor / int device pointer."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def _mem(a) -> int:
+    if isinstance(a, np.ndarray):
+        return MEM_HOST
+    return MEM_DEVICE
+
+
+def _f32(a, shape_last: int) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a.reshape(-1, shape_last)
+
+
+# ----- PBF ----------------------------------------------------------------------------------------------
+_FIELD_DT = {PBF_FIELD_POS: (np.float32, 2), PBF_FIELD_VEL: (np.float32, 2), PBF_FIELD_PRED: (np.float32, 2),
+             PBF_FIELD_LAMBDA: (np.float32, 1), PBF_FIELD_KEY: (np.uint32, 1), PBF_FIELD_PERM: (np.uint32, 1),
+             PBF_FIELD_CELL_START: (np.uint32, 1), PBF_FIELD_DOMAIN: (np.int32, 1),
+             PBF_FIELD_DENSITY: (np.float32, 1), PBF_FIELD_ID: (np.uint32, 1), PBF_FIELD_OMEGA: (np.float32, 1)}
+
+
+class Pbf:
+    """One PBF engine handle (gpe_pbf): a set of scenes with their particles resident on the GPU."""
+
+    def __init__(self, params: PbfParams, boxes, capacity: int):
+        self.params = params.copy()
+        self.boxes = [tuple(map(float, b)) for b in boxes]
+        self._doms = make_domains(self.boxes)
+        h = C.c_void_p()
+        check(lib().gpe_pbf_create(C.byref(self.params), self._doms, len(self.boxes), int(capacity), C.byref(h)),
+              "gpe_pbf_create")
+        self.h = h
+        self.capacity = int(capacity)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().gpe_pbf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: PbfParams) -> None:
+        check(lib().gpe_pbf_set_params(self.h, C.byref(params)), "gpe_pbf_set_params")
+        self.params = params.copy()
+
+    def set_state(self, pos, vel=None, domain=None, stream=None) -> None:
+        if isinstance(pos, np.ndarray):
+            pos = _f32(pos, 2)
+            vel = None if vel is None else _f32(vel, 2)
+            domain = None if domain is None else np.ascontiguousarray(domain, dtype=np.int32)
+            n = pos.shape[0]
+        else:
+            n = pos.shape[0]
+        check(lib().gpe_pbf_set_state(self.h, _ptr(pos), _ptr(vel), _ptr(domain), n, _mem(pos), stream),
+              "gpe_pbf_set_state")
+        self._keep = (pos, vel, domain)
+
+    @property
+    def n(self) -> int:
+        v = C.c_int64()
+        check(lib().gpe_pbf_count(self.h, C.byref(v)), "gpe_pbf_count")
+        return v.value
+
+    @property
+    def num_cells(self) -> int:
+        v = C.c_int64()
+        check(lib().gpe_pbf_num_cells(self.h, C.byref(v)), "gpe_pbf_num_cells")
+        return v.value
+
+    def get_state(self, pos=None, vel=None, stream=None):
+        """Returns (pos, vel, scene id) in the current sorted order. With caller buffers (host arrays or
+        device pointers) only pos/vel are written and the scene id is not read back."""
+        n = self.n
+        dom = None
+        if pos is None:
+            pos = np.empty((n, 2), np.float32)
+            vel = np.empty((n, 2), np.float32)
+            dom = np.empty(n, np.int32)
+        check(lib().gpe_pbf_get_state(self.h, _ptr(pos), _ptr(vel), _ptr(dom), n, _mem(pos), stream),
+              "gpe_pbf_get_state")
+        return pos, vel, dom
+
+    def step(self, n_steps: int = 1, stream=None) -> None:
+        check(lib().gpe_pbf_step(self.h, int(n_steps), stream), "gpe_pbf_step")
+
+    def stage(self, stage: int, stream=None) -> None:
+        check(lib().gpe_pbf_stage(self.h, int(stage), stream), f"gpe_pbf_stage({stage})")
+
+    def field(self, field: int, stream=None) -> np.ndarray:
+        dt, w = _FIELD_DT[field]
+        n = self.num_cells + 1 if field == PBF_FIELD_CELL_START else self.n
+        out = np.empty((n, w) if w > 1 else (n,), dt)
+        check(lib().gpe_pbf_get_field(self.h, field, out.ctypes.data, n, MEM_HOST, stream),
+              f"gpe_pbf_get_field({field})")
+        return out
+
+    def set_field(self, field: int, values: np.ndarray, stream=None) -> None:
+        dt, w = _FIELD_DT[field]
+        v = np.ascontiguousarray(values, dtype=dt)
+        n = v.shape[0]
+        check(lib().gpe_pbf_set_field(self.h, field, v.ctypes.data, n, MEM_HOST, stream),
+              f"gpe_pbf_set_field({field})")
+
+    def density_error(self, stream=None) -> tuple[float, float]:
+        mx, mn = C.c_float(), C.c_float()
+        check(lib().gpe_pbf_density_error(self.h, C.byref(mx), C.byref(mn), stream), "gpe_pbf_density_error")
+        return mx.value, mn.value
+
+    def status(self, stream=None) -> int:
+        v = C.c_uint32()
+        check(lib().gpe_pbf_status(self.h, C.byref(v), stream), "gpe_pbf_status")
+        return v.value
+
+    def launches_per_step(self) -> int:
+        v = C.c_int32()
+        check(lib().gpe_pbf_launches_per_step(self.h, C.byref(v)), "gpe_pbf_launches_per_step")
+        return v.value
+
+
+# ----- MPM ----------------------------------------------------------------------------------------------
+class Mpm:
+    """One MLS-MPM engine handle (gpe_mpm)."""
+
+    def __init__(self, params: MpmParams, capacity: int):
+        self.params = params.copy()
+        h = C.c_void_p()
+        check(lib().gpe_mpm_create(C.byref(self.params), int(capacity), C.byref(h)), "gpe_mpm_create")
+        self.h = h
+        self.capacity = int(capacity)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().gpe_mpm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: MpmParams) -> None:
+        check(lib().gpe_mpm_set_params(self.h, C.byref(params)), "gpe_mpm_set_params")
+        self.params = params.copy()
+
+    def set_state(self, pos, vel=None, Cm=None, F=None, J=None, material=None, stream=None) -> None:
+        if isinstance(pos, np.ndarray):
+            pos = _f32(pos, 2)
+            vel = None if vel is None else _f32(vel, 2)
+            Cm = None if Cm is None else _f32(Cm, 4)
+            F = None if F is None else _f32(F, 4)
+            J = None if J is None else np.ascontiguousarray(J, dtype=np.float32).reshape(-1)
+            material = None if material is None else np.ascontiguousarray(material, dtype=np.int32)
+        n = pos.shape[0]
+        check(lib().gpe_mpm_set_state(self.h, _ptr(pos), _ptr(vel), _ptr(Cm), _ptr(F), _ptr(J), _ptr(material), n,
+                                      _mem(pos), stream), "gpe_mpm_set_state")
+        self._keep = (pos, vel, Cm, F, J, material)
+
+    @property
+    def n(self) -> int:
+        v = C.c_int64()
+        check(lib().gpe_mpm_count(self.h, C.byref(v)), "gpe_mpm_count")
+        return v.value
+
+    def get_state(self, stream=None):
+        n = self.n
+        pos = np.empty((n, 2), np.float32)
+        vel = np.empty((n, 2), np.float32)
+        Cm = np.empty((n, 4), np.float32)
+        F = np.empty((n, 4), np.float32)
+        J = np.empty(n, np.float32)
+        check(lib().gpe_mpm_get_state(self.h, _ptr(pos), _ptr(vel), _ptr(Cm), _ptr(F), _ptr(J), n, MEM_HOST, stream),
+              "gpe_mpm_get_state")
+        return pos, vel, Cm, F, J
+
+    def get_state_device(self, pos, vel=None, Cm=None, F=None, J=None, stream=None) -> None:
+        check(lib().gpe_mpm_get_state(self.h, _ptr(pos), _ptr(vel), _ptr(Cm), _ptr(F), _ptr(J), self.n, _mem(pos),
+                                      stream), "gpe_mpm_get_state")
+
+    def step(self, n_steps: int = 1, stream=None) -> None:
+        check(lib().gpe_mpm_step(self.h, int(n_steps), stream), "gpe_mpm_step")
+
+    def stage(self, stage: int, stream=None) -> None:
+        check(lib().gpe_mpm_stage(self.h, int(stage), stream), f"gpe_mpm_stage({stage})")
+
+    def grid(self, stream=None) -> np.ndarray:
+        nn = self.params.nx * self.params.ny
+        out = np.empty((nn, 4), np.float32)
+        check(lib().gpe_mpm_get_grid(self.h, out.ctypes.data, nn, MEM_HOST, stream), "gpe_mpm_get_grid")
+        return out
+
+    def status(self, stream=None) -> int:
+        v = C.c_uint32()
+        check(lib().gpe_mpm_status(self.h, C.byref(v), stream), "gpe_mpm_status")
+        return v.value

@@ -1,0 +1,313 @@
+"""Parameter sets and seeded synthetic scenes.
+
+Two parameter regimes:
+  * reference mode — the reference's lattice units and constants (libs/common/include/common/constants.h,
+    PBF.cu:12-23, MPM.cu), used for parity with the reference's own kernels;
+  * the workload configurations the engine is measured on (PBF dam break, MPM elastic squares, 1M-particle
+    PBF, batched PBF scenes, mixed-material MPM), built from seeded Philox streams (numpy's Philox4x32-10
+    generator, Salmon et al. 2011), one stream per configuration.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import (MPM_BC_SLIP, MPM_BC_STICKY, MPM_FLAG_FLUID_F, MPM_FLAG_PER_PARTICLE_MATERIAL, MPM_MAT_COROTATED,
+               MPM_MAT_FLUID, MPM_MAT_SNOW, PBF_SELF_GRAD, PBF_VEL_CLAMP, MpmParams, PbfParams)
+
+F32 = np.float32
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(key=seed))
+
+
+# ===================================================================================================== PBF
+def reference_pbf_params(iters: int = 2) -> PbfParams:
+    """The reference's PBF constants, evaluated in FP32 in the reference's constexpr order
+    (constants.h:24-42, PBF.cu:12-23). Velocities are per-substep displacements (dt = 1)."""
+    kPi = F32(3.14159)
+    kH = F32(2.0)
+    kDt = F32(0.032)
+    kPBF_dt = F32(kDt / F32(20.0))
+    p = PbfParams()
+    p.h = kH
+    p.cell = F32(2.0)
+    p.rho0 = F32(1.015)
+    p.mass = F32(1.0)
+    p.dt = F32(1.0)
+    p.gravity[0] = 0.0
+    p.gravity[1] = F32(F32(F32(1000.0) * kPBF_dt) * kPBF_dt)  # kGravityStep, PBF.cu:19
+    p.iters = iters
+    p.eps = F32(0.005)
+    p.scorr_k = F32(0.005)
+    p.scorr_dq = F32(F32(0.2) * kH)
+    p.omega = F32(1.25)
+    p.c_min = F32(-0.002)
+    p.xsph_c = F32(0.035)
+    p.vort_eps = 0.0
+    p.v_max = F32(1.0)
+    p.v_min = F32(0.00005)
+    p.wall_margin = F32(1e-3)
+    p.poly6_coeff = F32(F32(1.0) / F32(F32(64.0) * kPi))
+    p.spiky_coeff = F32(F32(30.0) / F32(F32(32.0) * kPi))
+    p.flags = PBF_SELF_GRAD | PBF_VEL_CLAMP
+    return p
+
+
+REFERENCE_BOX = (0.0, 0.0, 12 * 32.0, 6 * 32.0)  # kSceneDimX x kSceneDimY chunks of kChunkDim
+
+
+def reference_pbf_block(nx: int = 48, ny: int = 40, spacing: float = 1.05, seed: int = 11,
+                        origin=(100.0, 60.0), disp=0.05, box=REFERENCE_BOX):
+    """A jittered block of atoms with small random displacements (reference units)."""
+    g = rng(seed)
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    pos = np.stack([origin[0] + ix.ravel() * spacing, origin[1] + iy.ravel() * spacing], 1)
+    pos += g.uniform(-0.05, 0.05, pos.shape)
+    vel = g.uniform(-disp, disp, pos.shape)
+    return pos.astype(F32), vel.astype(F32), [box]
+
+
+def lattice_mass(h: float, spacing: float, rho0: float = 1.0) -> float:
+    """Particle mass that makes the 2D poly6 density of a square lattice equal rho0."""
+    c6 = 4.0 / (math.pi * h ** 8)
+    r = int(math.ceil(h / spacing))
+    s = 0.0
+    for i in range(-r, r + 1):
+        for j in range(-r, r + 1):
+            q = h * h - (i * spacing) ** 2 - (j * spacing) ** 2
+            if q >= 0:
+                s += c6 * q ** 3
+    return rho0 / s
+
+
+def dam_params(iters: int = 4, h: float = 0.02, spacing: float = 0.01) -> PbfParams:
+    """Plain PBF dam break: h=0.02, rest density 1, gravity -9.8, dt=1/120, epsilon 100, XSPH c=0.01.
+    The XSPH coefficient is the mass/density-normalised one: the engine applies
+    v += c_abs sum_j (v_j - v_i) W_ij, so c_abs = c m / rho0."""
+    m = lattice_mass(h, spacing)
+    p = PbfParams()
+    p.h = h
+    p.cell = 0.0
+    p.rho0 = 1.0
+    p.mass = m
+    p.dt = 1.0 / 120.0
+    p.gravity[0] = 0.0
+    p.gravity[1] = -9.8
+    p.iters = iters
+    p.eps = 100.0
+    p.scorr_k = 0.0
+    p.scorr_dq = 0.2 * h
+    p.omega = 1.0
+    p.c_min = 0.0
+    p.xsph_c = 0.01 * m / 1.0
+    p.vort_eps = 0.0
+    p.v_max = 0.0
+    p.v_min = 0.0
+    p.wall_margin = 1e-6
+    p.poly6_coeff = 0.0
+    p.spiky_coeff = 0.0
+    p.flags = 0
+    return p
+
+
+def dam_break(n_side: int = 128, spacing: float = 0.01, box: float = 2.56, seed: int = 0, h: float = 0.02):
+    """16,384 particles on a 128x128 lattice (spacing 0.5h) in the lower-left quarter of a square box,
+    jittered by U(+-0.01h), at rest. The box side is 2.56 so that the 1.28-wide block is exactly its
+    lower-left quarter."""
+    g = rng(seed)
+    ix, iy = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="xy")
+    pos = np.stack([(ix.ravel() + 0.5) * spacing, (iy.ravel() + 0.5) * spacing], 1)
+    pos += g.uniform(-0.01 * h, 0.01 * h, pos.shape)
+    vel = np.zeros_like(pos)
+    return pos.astype(F32), vel.astype(F32), [(0.0, 0.0, box, box)]
+
+
+def million(seed: int = 2, spacing: float = 0.01, h: float = 0.02):
+    """1,048,576 particles in a 20.48 x 20.48 domain (4 x 4 chunks of 5.12): a 960 x 1024 lattice block
+    (983,040 particles, spacing 0.5h) in the lower-left corner plus a 256 x 256 splash block
+    (65,536 particles) higher up with random directions and |v| ~ U(0, 2)."""
+    g = rng(seed)
+    side = 20.48
+    ix, iy = np.meshgrid(np.arange(960), np.arange(1024), indexing="xy")
+    block = np.stack([(ix.ravel() + 0.5) * spacing, (iy.ravel() + 0.5) * spacing], 1)
+    sx, sy = np.meshgrid(np.arange(256), np.arange(256), indexing="xy")
+    splash = np.stack([12.0 + (sx.ravel() + 0.5) * spacing, 12.0 + (sy.ravel() + 0.5) * spacing], 1)
+    pos = np.concatenate([block, splash])
+    pos += g.uniform(-0.01 * h, 0.01 * h, pos.shape)
+    vel = np.zeros_like(pos)
+    ang = g.uniform(0.0, 2.0 * math.pi, splash.shape[0])
+    sp = g.uniform(0.0, 2.0, splash.shape[0])
+    vel[block.shape[0]:, 0] = sp * np.cos(ang)
+    vel[block.shape[0]:, 1] = sp * np.sin(ang)
+    return pos.astype(F32), vel.astype(F32), [(0.0, 0.0, side, side)]
+
+
+def batched_scenes(n_scenes: int = 256, seed: int = 3, lo: int = 2048, hi: int = 65536, spacing: float = 0.01):
+    """Independent dam-break scenes: particle counts log-uniform in [lo, hi], box aspect U(0.5, 2). Each
+    scene's block fills the lower-left quarter of its box at spacing 0.5h. Returns (pos, vel, dom, boxes);
+    scenes are laid side by side (disjoint boxes) but never interact."""
+    g = rng(seed)
+    counts = np.exp(g.uniform(math.log(lo), math.log(hi), n_scenes)).astype(np.int64)
+    aspects = g.uniform(0.5, 2.0, n_scenes)
+    pos_l, vel_l, dom_l, boxes = [], [], [], []
+    x0 = 0.0
+    for s in range(n_scenes):
+        n = int(counts[s])
+        a = float(aspects[s])  # width / height of the block (and of the box)
+        bw = max(1, int(round(math.sqrt(n * a))))
+        bh = max(1, int(math.ceil(n / bw)))
+        ix, iy = np.meshgrid(np.arange(bw), np.arange(bh), indexing="xy")
+        p = np.stack([(ix.ravel() + 0.5) * spacing, (iy.ravel() + 0.5) * spacing], 1)[:n]
+        p += g.uniform(-0.0002, 0.0002, p.shape)
+        W, H = 2.0 * bw * spacing, 2.0 * bh * spacing
+        p[:, 0] += x0
+        boxes.append((x0, 0.0, W, H))
+        pos_l.append(p)
+        vel_l.append(np.zeros_like(p))
+        dom_l.append(np.full(n, s, np.int32))
+        x0 += W + 1.0
+    return (np.concatenate(pos_l).astype(F32), np.concatenate(vel_l).astype(F32), np.concatenate(dom_l),
+            boxes)
+
+
+# ===================================================================================================== MPM
+def reference_mpm_params() -> MpmParams:
+    """The reference's MLS-MPM constants (constants.h:72-88, MPM.cu), FP32."""
+    p = MpmParams()
+    kDt = F32(0.032)
+    p.dx = 2.0
+    p.grid_offset = 2.0
+    p.nx = 12 * 32 // 2 + 4
+    p.ny = 6 * 32 // 2 + 4
+    p.dt = F32(kDt / F32(20))
+    p.gravity[0] = 0.0
+    p.gravity[1] = 700.0
+    p.mass = 1.0
+    p.vol0 = 1.2
+    p.bc_type = MPM_BC_SLIP
+    p.bc_width = 2
+    p.clamp_lo[0], p.clamp_lo[1] = 0.0, 0.0
+    p.clamp_hi[0], p.clamp_hi[1] = 384.0, 192.0
+    p.material = MPM_MAT_FLUID
+    p.k_bulk = 8.2e4
+    p.gamma = 3.2
+    p.p_min = F32(-0.0) * F32(8.2e4)
+    p.p_max = F32(10.0) * F32(8.2e4)
+    p.J_min = 0.1
+    p.J_max = 10.0
+    p.E = 0.0
+    p.nu = 0.0
+    p.theta_c = 0.0
+    p.theta_s = 0.0
+    p.hardening = 0.0
+    p.sort_interval = 0
+    p.flags = MPM_FLAG_FLUID_F
+    return p
+
+
+def reference_mpm_block(nx: int = 60, ny: int = 40, spacing: float = 1.26, seed: int = 21,
+                        origin=(60.0, 40.0)):
+    g = rng(seed)
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    pos = np.stack([origin[0] + ix.ravel() * spacing, origin[1] + iy.ravel() * spacing], 1)
+    pos += g.uniform(-0.1, 0.1, pos.shape)
+    vel = g.uniform(-20.0, 20.0, pos.shape)
+    n = pos.shape[0]
+    Cm = g.uniform(-0.5, 0.5, (n, 4))
+    F = np.tile(np.array([1, 0, 0, 1], F32), (n, 1)) + g.uniform(-0.01, 0.01, (n, 4))
+    J = g.uniform(0.95, 1.05, n)
+    return pos.astype(F32), vel.astype(F32), Cm.astype(F32), F.astype(F32), J.astype(F32)
+
+
+def elastic_params(n: int = 65536, grid: int = 128) -> MpmParams:
+    """Plain MLS-MPM: 128^2 grid over the unit box, fixed-corotated E=1e3, nu=0.2, particle mass 1/65536,
+    dt=1e-4, gravity -9.8, sticky walls 3 nodes wide."""
+    dx = 1.0 / grid
+    p = MpmParams()
+    p.dx = dx
+    p.grid_offset = 0.0
+    p.nx = grid
+    p.ny = grid
+    p.dt = 1e-4
+    p.gravity[0] = 0.0
+    p.gravity[1] = -9.8
+    p.mass = 1.0 / 65536.0
+    p.vol0 = 2 * 0.25 * 0.25 / n
+    p.bc_type = MPM_BC_STICKY
+    p.bc_width = 2
+    p.clamp_lo[0] = p.clamp_lo[1] = 2 * dx
+    p.clamp_hi[0] = p.clamp_hi[1] = 1.0 - 3 * dx
+    p.material = MPM_MAT_COROTATED
+    p.k_bulk = 0.0
+    p.gamma = 1.0
+    p.p_min = -1e30
+    p.p_max = 1e30
+    p.J_min = 0.1
+    p.J_max = 10.0
+    p.E = 1e3
+    p.nu = 0.2
+    p.theta_c = 2.5e-2
+    p.theta_s = 4.5e-3
+    p.hardening = 10.0
+    p.sort_interval = 0
+    p.flags = 0
+    return p
+
+
+def two_squares(n: int = 65536, seed: int = 1):
+    """65,536 particles uniform in two 0.25 x 0.25 squares (4 per cell on a 128^2 grid would need 0.0625
+    area per 4096 particles; here each square holds 32,768, i.e. 32 per cell)."""
+    g = rng(seed)
+    h = n // 2
+    a = g.uniform(0.0, 0.25, (h, 2)) + np.array([0.2, 0.2])
+    b = g.uniform(0.0, 0.25, (n - h, 2)) + np.array([0.55, 0.45])
+    pos = np.concatenate([a, b]).astype(F32)
+    vel = np.zeros_like(pos)
+    vel[:h, 0] = 0.5
+    vel[h:, 0] = -0.5
+    return pos, vel
+
+
+def mixed_params(n: int, grid: int = 1024) -> MpmParams:
+    """Mixed materials on a 1024^2 grid: water (J-based EOS, bulk modulus 10), snow (theta_c=2.5e-2,
+    theta_s=4.5e-3, hardening 10) and jelly (E=5e3, nu=0.2); dt=5e-5."""
+    p = elastic_params(n, grid)
+    p.dt = 5e-5
+    p.E = 5e3
+    p.nu = 0.2
+    p.k_bulk = 10.0
+    p.gamma = 1.0
+    p.p_min = -1e30
+    p.p_max = 1e30
+    p.flags = MPM_FLAG_PER_PARTICLE_MATERIAL
+    p.mass = 1.0 / n
+    p.vol0 = 0.3 / n
+    p.sort_interval = 16
+    return p
+
+
+def mixed_discs(n: int = 4194304, seed: int = 4, discs_per_material: int = 3, area: float = 0.3):
+    """n particles, a third each of water, snow and jelly, in seeded random discs of equal radius."""
+    g = rng(seed)
+    nd = 3 * discs_per_material
+    r = math.sqrt(area / (nd * math.pi))
+    per_mat = [n // 3, n // 3, n - 2 * (n // 3)]
+    pos_l, mat_l = [], []
+    for m, cnt in zip((MPM_MAT_FLUID, MPM_MAT_SNOW, MPM_MAT_COROTATED), per_mat):
+        cs = g.uniform(0.15 + r, 0.85 - r, (discs_per_material, 2))
+        split = [cnt // discs_per_material] * discs_per_material
+        split[-1] += cnt - sum(split)
+        for c, k in zip(cs, split):
+            rad = r * np.sqrt(g.uniform(0, 1, k))
+            th = g.uniform(0, 2 * math.pi, k)
+            pos_l.append(np.stack([c[0] + rad * np.cos(th), c[1] + rad * np.sin(th)], 1))
+            mat_l.append(np.full(k, m, np.int32))
+    pos = np.concatenate(pos_l).astype(F32)
+    mat = np.concatenate(mat_l)
+    # spatially coherent initial order (row-major by grid cell), which keeps P2G tiles small
+    cell = (np.floor(pos[:, 1] * 1024).astype(np.int64) * 1024 + np.floor(pos[:, 0] * 1024).astype(np.int64))
+    order = np.argsort(cell, kind="stable")
+    return pos[order], mat[order]

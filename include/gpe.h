@@ -1,0 +1,218 @@
+/*
+ * gpe.h — C ABI of the GB300 particle engine (PBF and MLS-MPM solver steps).
+ *
+ * Every entry point takes plain pointers and sizes and returns an int32 status (GPE_OK == 0, negative on
+ * failure), following the error convention of the reference's only C ABI,
+ * libs/render/include/render/cuda-interface.h:30-42 (0 ok, -1 CUDA error kept in last_error, -2 device
+ * mismatch, -3 not initialised, -4 bad argument, -5 already initialised), extended with -6 capacity
+ * overflow, -7 non-finite state and -8 device wait timeout.
+ *
+ * The handle-based entry points replace the reference's C++ engine interface
+ * (libs/cuda-engine/include/cuda-engine/cuda-engine.h): gpe_pbf_create/destroy stand in for the PBFArena
+ * constructor/destructor (cuda-engine.cpp:102-143), gpe_pbf_step for one launch of the tick graph built by
+ * instantiatePBFGraph (cuda-engine.h:164-167, PBF.cu:901-961), gpe_mpm_* likewise for MPMArena
+ * (cuda-engine.h:190-216) and instantiateMPMGraph (cuda-engine.h:227-230, MPM.cu:326-374).
+ *
+ * Streams are passed as void* holding a cudaStream_t (NULL = legacy default stream). All work of one handle
+ * must be issued from one host thread on one stream, as in the reference (cuda-engine.h:171).
+ */
+#ifndef GPE_H
+#define GPE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----- status codes ------------------------------------------------------------------------------------ */
+#define GPE_OK 0
+#define GPE_ERR_CUDA (-1)      /* a CUDA runtime call failed; gpe_last_cuda_error() has the cudaError_t   */
+#define GPE_ERR_DEVICE (-2)    /* no usable device, or the handle belongs to another device               */
+#define GPE_ERR_NOT_READY (-3) /* handle not initialised / state not set / extension missing            */
+#define GPE_ERR_BAD_ARG (-4)   /* null pointer, negative size, inconsistent parameters                   */
+#define GPE_ERR_ALREADY (-5)   /* already initialised                                                    */
+#define GPE_ERR_CAPACITY (-6)  /* particle, cell or scratch capacity exceeded                            */
+#define GPE_ERR_NONFINITE (-7) /* the device status word recorded a non-finite value                     */
+#define GPE_ERR_TIMEOUT (-8)   /* a bounded device wait gave up                                          */
+
+/* memory kinds for state transfer */
+#define GPE_MEM_HOST 0
+#define GPE_MEM_DEVICE 1
+
+/* device status word bits (gpe_*_status) */
+#define GPE_STATUS_NONFINITE 0x1u
+#define GPE_STATUS_CAPACITY 0x2u
+#define GPE_STATUS_CELL_OVERFLOW 0x4u
+#define GPE_STATUS_TIMEOUT 0x8u
+
+const char* gpe_error_name(int32_t status);
+int32_t gpe_last_cuda_error(void);        /* cudaError_t of the last failing CUDA call on this thread */
+const char* gpe_last_error_message(void); /* human readable detail of the last failure on this thread */
+int32_t gpe_version(void);                /* major*10000 + minor*100 + patch                           */
+
+/* ======================================================================================================
+ * Position-Based Fluids
+ * ====================================================================================================== */
+
+/* PBF flags */
+#define GPE_PBF_SELF_GRAD 0x1u    /* include the self pair's pseudo-random spiky gradient in the lambda
+                                     denominator exactly as the reference does (PBF.cu:264-285 loops over
+                                     the atom itself; coincident pairs take pairDirection, PBF.cu:309-321) */
+#define GPE_PBF_VEL_CLAMP 0x2u    /* clamp |v| to [v_min, v_max] after XSPH (velocityClamp, PBF.cu:629-638) */
+#define GPE_PBF_TRACK_IDS 0x4u    /* carry a particle id through every sort (for external bookkeeping)      */
+#define GPE_PBF_SELF_XSPH 0x8u    /* reserved                                                                */
+
+typedef struct gpe_pbf_params {
+    float h;            /* smoothing radius (reference kH, constants.h:35)                          */
+    float cell;         /* sort-cell edge; 0 selects h (reference kCellDim == kH, constants.h:46)  */
+    float rho0;         /* rest density (kRho0, constants.h:36)                                     */
+    float mass;         /* particle mass (kMass, constants.h:27)                                    */
+    float dt;           /* step length; 1 makes velocities per-step displacements as in the
+                           reference (cuda-engine.h:131)                                              */
+    float gravity[2];   /* acceleration; x* = x + dt v + dt^2 g (PBF.cu:790-791 adds kGravityStep) */
+    int32_t iters;      /* Jacobi iterations per step (kIters, PBF.cu:12)                            */
+    float eps;          /* constraint relaxation (kEpsilon, PBF.cu:14)                               */
+    float scorr_k;      /* artificial pressure scale (kSCorrK, PBF.cu:15); 0 disables                */
+    float scorr_dq;     /* artificial pressure reference distance (kDq, constants.h:40)              */
+    float omega;        /* over-relaxation of the Jacobi update (kOmega, PBF.cu:20)                  */
+    float c_min;        /* lower clamp of the density constraint (kMinC, PBF.cu:21)                   */
+    float xsph_c;       /* XSPH coefficient applied to sum (v_j - v_i) W_ij (kC, PBF.cu:16)          */
+    float vort_eps;     /* vorticity-confinement strength; 0 disables (absent in the reference)     */
+    float v_max;        /* velocity clamp (kMaxSpeed, PBF.cu:23), used with GPE_PBF_VEL_CLAMP        */
+    float v_min;        /* below this speed v is zeroed (kMinSpeed, PBF.cu:22)                       */
+    float wall_margin;  /* positions are clamped to [lo, hi - wall_margin] (PBF.cu:487-490 uses 1e-3) */
+    float poly6_coeff;  /* 0 selects 4/(pi h^8); the reference uses 1/(64*3.14159f), constants.h:38  */
+    float spiky_coeff;  /* 0 selects 30/(pi h^5); the reference uses 30/(32*3.14159f), constants.h:39 */
+    uint32_t flags;     /* GPE_PBF_* */
+} gpe_pbf_params;
+
+/* One independent scene (domain). A scene is an axis-aligned box with walls on all four sides and its own
+ * uniform sort grid; scenes never exchange particles. One scene reproduces the reference's whole world
+ * (kSceneDimX x kSceneDimY chunks, constants.h:11-12); many scenes form the batched launch. */
+typedef struct gpe_domain {
+    float origin[2]; /* lower corner */
+    float extent[2]; /* box size     */
+} gpe_domain;
+
+typedef struct gpe_pbf gpe_pbf;
+
+/* Stages of one PBF step, in order. gpe_pbf_step runs PREDICT_SORT, iters x (LAMBDA, DELTA_P), XSPH,
+ * [VORTICITY if vort_eps != 0], FINISH. */
+#define GPE_PBF_STAGE_PREDICT_SORT 0 /* prepNextSubstepKernel PBF.cu:738-834 (predict, cell key, sort)       */
+#define GPE_PBF_STAGE_LAMBDA 1       /* lambdaKernel PBF.cu:215-308                                           */
+#define GPE_PBF_STAGE_DELTA_P 2      /* posCorrectionKernel PBF.cu:365-470 + handleOOB PBF.cu:471-499         */
+#define GPE_PBF_STAGE_XSPH 3         /* velocityKernel PBF.cu:500-553 + XSPHKernel PBF.cu:554-638 (fused)     */
+#define GPE_PBF_STAGE_VORTICITY 4    /* vorticity confinement (Macklin & Mueller 2013 eq. 15-16)              */
+#define GPE_PBF_STAGE_FINISH 5       /* x <- x*, publish the step                                             */
+#define GPE_PBF_STAGE_DENSITY 6      /* recompute rho for the density-error metric (not part of a step)       */
+
+/* Fields that can be read or written for inspection (element types in brackets). All are in the current
+ * sorted order; n_elems counts elements of the field's type. */
+#define GPE_PBF_FIELD_POS 0        /* x  [float2]                                          */
+#define GPE_PBF_FIELD_VEL 1        /* v  [float2]                                          */
+#define GPE_PBF_FIELD_PRED 2       /* x* [float2]                                          */
+#define GPE_PBF_FIELD_LAMBDA 3     /* lambda [float]                                       */
+#define GPE_PBF_FIELD_KEY 4        /* global cell key of each sorted particle [uint32]     */
+#define GPE_PBF_FIELD_PERM 5       /* pre-sort index of each sorted particle [uint32]      */
+#define GPE_PBF_FIELD_CELL_START 6 /* exclusive scan of cell counts, n_cells+1 [uint32]    */
+#define GPE_PBF_FIELD_DOMAIN 7     /* scene of each particle [int32]                       */
+#define GPE_PBF_FIELD_DENSITY 8    /* rho from the last DENSITY stage [float]              */
+#define GPE_PBF_FIELD_ID 9         /* particle id (GPE_PBF_TRACK_IDS) [uint32]             */
+#define GPE_PBF_FIELD_OMEGA 10     /* vorticity from the last XSPH stage [float]           */
+
+int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, int32_t n_domains,
+                       int64_t capacity, gpe_pbf** out);
+int32_t gpe_pbf_destroy(gpe_pbf* pbf);
+int32_t gpe_pbf_set_params(gpe_pbf* pbf, const gpe_pbf_params* params);
+int32_t gpe_pbf_get_params(const gpe_pbf* pbf, gpe_pbf_params* params);
+/* Replace the particle state. pos/vel hold n float2 (interleaved x,y); domain_id holds n scene indices and
+ * may be NULL when there is one scene. mem selects host or device pointers. */
+int32_t gpe_pbf_set_state(gpe_pbf* pbf, const float* pos, const float* vel, const int32_t* domain_id,
+                          int64_t n, int32_t mem, void* stream);
+int32_t gpe_pbf_get_state(gpe_pbf* pbf, float* pos, float* vel, int32_t* domain_id, int64_t n, int32_t mem,
+                          void* stream);
+int32_t gpe_pbf_count(const gpe_pbf* pbf, int64_t* n);
+int32_t gpe_pbf_num_cells(const gpe_pbf* pbf, int64_t* n_cells);
+int32_t gpe_pbf_step(gpe_pbf* pbf, int32_t n_steps, void* stream);
+int32_t gpe_pbf_stage(gpe_pbf* pbf, int32_t stage, void* stream);
+int32_t gpe_pbf_get_field(gpe_pbf* pbf, int32_t field, void* dst, int64_t n_elems, int32_t mem, void* stream);
+int32_t gpe_pbf_set_field(gpe_pbf* pbf, int32_t field, const void* src, int64_t n_elems, int32_t mem,
+                          void* stream);
+/* max_i max(rho_i/rho0 - 1, 0) and its mean over particles, with rho recomputed by a separate pass. */
+int32_t gpe_pbf_density_error(gpe_pbf* pbf, float* max_err, float* mean_err, void* stream);
+/* Reads and clears the device status word (GPE_STATUS_*); synchronises the stream. */
+int32_t gpe_pbf_status(gpe_pbf* pbf, uint32_t* status, void* stream);
+/* Number of kernel launches the last gpe_pbf_step issued per step. */
+int32_t gpe_pbf_launches_per_step(const gpe_pbf* pbf, int32_t* launches);
+
+/* ======================================================================================================
+ * MLS-MPM
+ * ====================================================================================================== */
+
+#define GPE_MPM_MAT_FLUID 0      /* J-based equation of state (reference P2GKernel, MPM.cu:68-80)          */
+#define GPE_MPM_MAT_COROTATED 1  /* fixed-corotated elasticity (Stomakhin et al. 2012)                     */
+#define GPE_MPM_MAT_SNOW 2       /* fixed-corotated with plasticity clamp and hardening (Stomakhin 2013)  */
+
+#define GPE_MPM_BC_SLIP 0        /* zero the velocity component into the wall (MPM.cu:159-168)             */
+#define GPE_MPM_BC_STICKY 1      /* zero the whole node velocity inside the wall band                      */
+
+#define GPE_MPM_FLAG_PER_PARTICLE_MATERIAL 0x1u /* read a material id per particle instead of params.material */
+#define GPE_MPM_FLAG_FLUID_F 0x2u /* keep updating F for fluid particles, as the reference does although nothing
+                                     reads it (MPM.cu:258-263, cuda-engine.h:203); off saves 32 B/particle */
+
+typedef struct gpe_mpm_params {
+    float dx;          /* node spacing (kDx, constants.h:80)                                    */
+    float grid_offset; /* node coordinate of world x = 0, in nodes (kGridHalo, MPM.cu:84)        */
+    int32_t nx, ny;    /* node grid (kGridDimX/Y, constants.h:76-77)                              */
+    float dt;          /* step (dt, constants.h:88)                                              */
+    float gravity[2];  /* added as g dt to node velocity (MPM.cu:154 adds kGravity*dt on y)       */
+    float mass;        /* particle mass (kMass)                                                  */
+    float vol0;        /* rest volume (kRestVol, constants.h:81)                                 */
+    int32_t bc_type;   /* GPE_MPM_BC_*                                                           */
+    int32_t bc_width;  /* wall band in nodes (kGridHalo == 2 in the reference)                   */
+    float clamp_lo[2]; /* particle position clamp in G2P (handleOOB, MPM.cu:267-301)             */
+    float clamp_hi[2];
+    int32_t material;  /* GPE_MPM_MAT_* when no per-particle material is given                   */
+    float k_bulk;      /* EOS stiffness (kStiffness, constants.h:84)                              */
+    float gamma;       /* EOS exponent (kGamma, constants.h:85)                                   */
+    float p_min, p_max;/* pressure clamp (kMinPress/kMaxPress, constants.h:86-87)                */
+    float J_min, J_max;/* J clamp after the update (MPM.cu:265 uses 0.1, 10)                     */
+    float E, nu;       /* Young's modulus and Poisson ratio (corotated / snow)                   */
+    float theta_c, theta_s, hardening; /* snow plasticity (Stomakhin 2013)                       */
+    int32_t sort_interval; /* re-sort particles by cell every this many steps; 0 = never          */
+    uint32_t flags;    /* GPE_MPM_FLAG_*                                                         */
+} gpe_mpm_params;
+
+typedef struct gpe_mpm gpe_mpm;
+
+#define GPE_MPM_STAGE_CLEAR 0 /* resetGridKernel MPM.cu:46-51            */
+#define GPE_MPM_STAGE_P2G 1   /* P2GKernel MPM.cu:53-129                  */
+#define GPE_MPM_STAGE_GRID 2  /* gridKernel MPM.cu:131-177                */
+#define GPE_MPM_STAGE_G2P 3   /* G2PKernel MPM.cu:178-301                 */
+#define GPE_MPM_STAGE_SORT 4  /* spatial re-sort of the particles         */
+
+int32_t gpe_mpm_create(const gpe_mpm_params* params, int64_t capacity, gpe_mpm** out);
+int32_t gpe_mpm_destroy(gpe_mpm* mpm);
+int32_t gpe_mpm_set_params(gpe_mpm* mpm, const gpe_mpm_params* params);
+/* pos, vel: n float2; C, F: n float4 row-major (xx, xy, yx, yy); J: n float (for snow it is the plastic
+ * J_p); material: n int32 or NULL. Any of vel/C/F/J may be NULL (zero velocity and C, identity F, J = 1). */
+int32_t gpe_mpm_set_state(gpe_mpm* mpm, const float* pos, const float* vel, const float* C, const float* F,
+                          const float* J, const int32_t* material, int64_t n, int32_t mem, void* stream);
+int32_t gpe_mpm_get_state(gpe_mpm* mpm, float* pos, float* vel, float* C, float* F, float* J, int64_t n,
+                          int32_t mem, void* stream);
+int32_t gpe_mpm_count(const gpe_mpm* mpm, int64_t* n);
+/* One step = clear + P2G + grid update + G2P; consecutive steps run fused (G2P of one step with P2G of the
+ * next in one launch). */
+int32_t gpe_mpm_step(gpe_mpm* mpm, int32_t n_steps, void* stream);
+int32_t gpe_mpm_stage(gpe_mpm* mpm, int32_t stage, void* stream);
+/* Node grid of the current step: nx*ny float4 (momentum or velocity x, y; mass; unused). */
+int32_t gpe_mpm_get_grid(gpe_mpm* mpm, float* dst, int64_t n_nodes, int32_t mem, void* stream);
+int32_t gpe_mpm_status(gpe_mpm* mpm, uint32_t* status, void* stream);
+int32_t gpe_mpm_launches_per_step(const gpe_mpm* mpm, int32_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPE_H */

@@ -1,0 +1,68 @@
+/*
+ * oracle.h — CPU restatement of the reference solver steps. TEST INFRASTRUCTURE ONLY: this library is
+ * the checker for the CUDA engine and the timed CPU baseline; the engine never links or calls it.
+ *
+ * Arithmetic is FP64 except where the reference's FP32 rounding decides an integer result (the predicted
+ * position that feeds the cell key, the cell key itself and the base cell of a neighbour scan), which is
+ * restated in FP32 with the same operation order as the device so that keys and sorted order are
+ * bit-exact. Parity of this restatement with the reference build is checked by the GPU tests that run the
+ * reference's own kernels (tests/test_reference_parity.py) and by the committed fixtures in tests/golden.
+ */
+#ifndef GPE_ORACLE_H
+#define GPE_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/gpe.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------- PBF ---------- */
+int64_t orc_pbf_num_cells(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd);
+/* Predict x* = fma(dt, v, x) + dt^2 g in FP32, compute the cell key and stable-sort by key.
+ * Outputs are in sorted order: key, perm (pre-sort index), x, x*, dom; cell_start has n_cells+1 entries. */
+void orc_pbf_predict_sort(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n,
+                          const float* x, const float* v, const int32_t* dom, uint32_t* key, uint32_t* perm,
+                          uint32_t* cell_start, float* x_sorted, float* xs_sorted, int32_t* dom_sorted);
+/* Stage restatements on sorted inputs (FP64 arithmetic, FP32 in/out). */
+void orc_pbf_lambda(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
+                    const int32_t* dom, const uint32_t* cell_start, float* lambda, float* rho);
+void orc_pbf_delta_p(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
+                     const int32_t* dom, const uint32_t* cell_start, const float* lambda, float* xs_out);
+void orc_pbf_xsph(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* x,
+                  const float* xs, const int32_t* dom, const uint32_t* cell_start, float* v_out, float* omega);
+void orc_pbf_vorticity(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n,
+                       const float* xs, const int32_t* dom, const uint32_t* cell_start, const float* omega,
+                       float* v_inout);
+void orc_pbf_density(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
+                     const int32_t* dom, const uint32_t* cell_start, float* rho);
+/* Whole steps. x, v, dom are the state in the current order and are replaced by the state in the new sorted
+ * order after each step (x <- final x*). Between iterations x* is kept in FP64. lambda (may be NULL)
+ * receives the last iteration's lambda. */
+void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
+                  int32_t* dom, int32_t n_steps, float* lambda, uint32_t* cell_start_out);
+/* max_i max(rho_i/rho0-1,0) and mean of the same over particles, from orc_pbf_density on x. */
+void orc_pbf_density_error(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n,
+                           const float* x, const int32_t* dom, const uint32_t* cell_start, double* max_err,
+                           double* mean_err);
+
+/* ---------- MLS-MPM ---------- */
+/* grid: nx*ny*3 doubles (momentum x, momentum y, mass) */
+void orc_mpm_p2g(const gpe_mpm_params* p, int64_t n, const float* x, const float* v, const float* C,
+                 const float* F, const float* J, const int32_t* mat, double* grid);
+/* in place: momentum -> velocity, gravity, walls */
+void orc_mpm_grid_update(const gpe_mpm_params* p, double* grid);
+/* grid: velocities (after orc_mpm_grid_update). Updates the particle state in place. */
+void orc_mpm_g2p(const gpe_mpm_params* p, int64_t n, const double* grid, float* x, float* v, float* C,
+                 float* F, float* J, const int32_t* mat);
+void orc_mpm_step(const gpe_mpm_params* p, int64_t n, float* x, float* v, float* C, float* F, float* J,
+                  const int32_t* mat, int32_t n_steps);
+
+int32_t orc_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,157 @@
+"""MLS-MPM parity of the CUDA engine (through the C ABI) against the oracle.
+
+Stage tests feed both sides identical FP32 inputs. The grid after P2G is a sum of float atomics whose order
+is not fixed, so grid fields are compared to 1e-5 of the field's scale; particle fields after G2P to 1e-5 of
+their scale plus the FP32 rounding of the coordinates.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EPS32 = np.finfo(np.float32).eps
+
+
+def _scene(kind):
+    import gpe
+    from gpe import scenes
+
+    g = np.random.default_rng(12)
+    if kind == "reference":
+        p = scenes.reference_mpm_params()
+        x, v, Cm, F, J = scenes.reference_mpm_block()
+        return p, x, v, Cm, F, J, None
+    p = scenes.elastic_params(4096, 64)
+    n = 4096
+    x = g.uniform(0.25, 0.75, (n, 2)).astype(np.float32)
+    v = g.normal(0, 0.5, (n, 2)).astype(np.float32)
+    Cm = g.normal(0, 2.0, (n, 4)).astype(np.float32)
+    F = (np.tile(np.eye(2).ravel(), (n, 1)) + g.normal(0, 0.02, (n, 4))).astype(np.float32)
+    J = g.uniform(0.97, 1.03, n).astype(np.float32)
+    mat = None
+    if kind == "corotated":
+        p.material = gpe.MPM_MAT_COROTATED
+    elif kind == "snow":
+        p.material = gpe.MPM_MAT_SNOW
+    elif kind == "fluid":
+        p.material = gpe.MPM_MAT_FLUID
+        p.k_bulk, p.gamma = 10.0, 1.0
+    elif kind == "mixed":
+        p.flags = gpe.MPM_FLAG_PER_PARTICLE_MATERIAL
+        p.k_bulk, p.gamma = 10.0, 1.0
+        mat = (np.arange(n) * 3 // n).astype(np.int32)
+    return p, x, v, Cm, F, J, mat
+
+
+KINDS = ["reference", "corotated", "snow", "fluid", "mixed"]
+
+
+def _engine(gpe_mod, p, x, v, Cm, F, J, mat, sort_interval=0):
+    p = p.copy()
+    p.sort_interval = sort_interval
+    e = gpe_mod.Mpm(p, capacity=len(x))
+    e.set_state(x, v, Cm, F, J, mat)
+    return e
+
+
+def _close(a, b, scale, what, rel=1e-5, floor=0.0):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    err = np.abs(a - b)
+    tol = rel * scale + floor
+    bad = err > tol
+    assert not bad.any(), f"{what}: {bad.sum()} of {bad.size} beyond tolerance; max err {err.max():.3e}"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_p2g_stage(gpe_mod, oracle, cuda_ok, kind):
+    p, x, v, Cm, F, J, mat = _scene(kind)
+    e = _engine(gpe_mod, p, x, v, Cm, F, J, mat)
+    e.stage(gpe_mod.MPM_STAGE_CLEAR)
+    e.stage(gpe_mod.MPM_STAGE_P2G)
+    g = e.grid()
+    want = oracle.MpmOracle(p).p2g(x, v, Cm, F, J, mat)
+    _close(g[:, 2], want[:, 2], np.abs(want[:, 2]).max(), "grid mass")
+    _close(g[:, :2], want[:, :2], np.abs(want[:, :2]).max(), "grid momentum", rel=2e-5)
+    assert e.status() == 0
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_grid_and_g2p_stages(gpe_mod, oracle, cuda_ok, kind):
+    p, x, v, Cm, F, J, mat = _scene(kind)
+    e = _engine(gpe_mod, p, x, v, Cm, F, J, mat)
+    o = oracle.MpmOracle(p)
+    e.stage(gpe_mod.MPM_STAGE_CLEAR)
+    e.stage(gpe_mod.MPM_STAGE_P2G)
+    raw = e.grid()[:, :3].astype(np.float64)
+    e.stage(gpe_mod.MPM_STAGE_GRID)
+    upd = e.grid()
+    want = o.grid_update(raw)
+    vs = np.abs(want[:, :2]).max()
+    _close(upd[:, :2], want[:, :2], vs, "grid velocity", rel=1e-6, floor=0.0)
+    e.stage(gpe_mod.MPM_STAGE_G2P)
+    x1, v1, C1, F1, J1 = e.get_state()
+    wx, wv, wC, wF, wJ = o.g2p(upd[:, :3].astype(np.float64), x, v, Cm, F, J, mat)
+    _close(x1, wx, np.abs(wx), "x", rel=1e-6, floor=4 * EPS32 * np.abs(wx).max())
+    _close(v1, wv, np.abs(wv).max(), "v")
+    _close(C1, wC, np.abs(wC).max(), "C", rel=2e-5)
+    if kind != "fluid" and kind != "mixed":
+        _close(F1, wF, np.abs(wF).max(), "F", rel=2e-5)
+    if kind != "corotated":
+        sel = slice(None) if mat is None else (mat != gpe_mod.MPM_MAT_COROTATED)
+        _close(J1[sel], wJ[sel], np.abs(wJ[sel]).max(), "J", rel=2e-5)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("steps", [1, 4])
+def test_fused_steps(gpe_mod, oracle, cuda_ok, kind, steps):
+    p, x, v, Cm, F, J, mat = _scene(kind)
+    e = _engine(gpe_mod, p, x, v, Cm, F, J, mat)
+    e.step(steps)
+    x1, v1, C1, F1, J1 = e.get_state()
+    wx, wv, wC, wF, wJ = oracle.MpmOracle(p).step(x, v, Cm, F, J, mat, n_steps=steps)
+    rel = 1e-5 * steps
+    _close(x1, wx, np.abs(wx), "x", rel=rel, floor=8 * EPS32 * np.abs(wx).max())
+    _close(v1, wv, np.abs(wv).max(), "v", rel=10 * rel)
+    _close(C1, wC, np.abs(wC).max(), "C", rel=10 * rel)
+    if kind in ("corotated", "snow") or kind == "reference":
+        _close(F1, wF, np.abs(wF).max(), "F", rel=10 * rel)
+    assert e.status() == 0
+
+
+def test_spatial_sort_keeps_results_and_order(gpe_mod, cuda_ok):
+    p, x, v, Cm, F, J, mat = _scene("mixed")
+    perm = np.random.default_rng(3).permutation(len(x))
+    a = _engine(gpe_mod, p, x, v, Cm, F, J, mat, sort_interval=0)
+    b = _engine(gpe_mod, p, x, v, Cm, F, J, mat, sort_interval=1)
+    for _ in range(3):
+        a.step(2)
+        b.step(2)
+    sa, sb = a.get_state(), b.get_state()
+    # get_state returns particles at their original indices even after re-sorting
+    for fa, fb, nm in zip(sa, sb, "xvCFJ"):
+        _close(fb, fa, np.abs(fa).max() + 1e-30, nm, rel=1e-4)
+    del perm
+
+
+def test_mpm_edge_cases(gpe_mod, cuda_ok):
+    from gpe import scenes
+
+    p = scenes.elastic_params(16, 32)
+    e = gpe_mod.Mpm(p, capacity=8)
+    e.set_state(np.zeros((0, 2), np.float32))
+    e.step(3)
+    e.set_state(np.array([[0.5, 0.5]], np.float32))
+    e.step(2)
+    x, v, _, _, _ = e.get_state()
+    assert x[0, 1] < 0.5 and v[0, 1] < 0
+    with pytest.raises(gpe_mod.GpeError) as ei:
+        e.set_state(np.zeros((9, 2), np.float32))
+    assert ei.value.status == gpe_mod.ERR_CAPACITY
+    bad = np.array([[0.5, np.nan]], np.float32)
+    e.set_state(bad)
+    e.step(1)
+    x, _, _, _, _ = e.get_state()
+    assert np.all(np.isfinite(x))  # handleOOB resets non-finite particles to the box centre
+    assert e.status() & gpe_mod.STATUS_NONFINITE
+    e.close()

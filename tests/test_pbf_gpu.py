@@ -1,0 +1,236 @@
+"""PBF parity of the CUDA engine (through the C ABI) against the oracle.
+
+Tolerances: cell keys, sorted order, cell starts and the sorted copies of x and x* are compared bit for bit.
+Floating-point stages run on identical FP32 inputs on both sides; the oracle computes in FP64, so the bound
+is the FP32 rounding of the engine: |gpu - oracle| <= 1e-5 * scale + 4 ulp(|x|) where scale is the field's
+largest magnitude (positions: 1e-5 of the particle's own coordinate plus 1e-6 of the domain scale).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EPS32 = np.finfo(np.float32).eps
+
+
+def _scene(kind):
+    import gpe
+    from gpe import scenes
+
+    if kind == "reference":
+        p = scenes.reference_pbf_params(iters=2)
+        pos, vel, boxes = scenes.reference_pbf_block()
+        return p, pos, vel, None, boxes
+    if kind == "dam":
+        p = scenes.dam_params(iters=4)
+        pos, vel, boxes = scenes.dam_break()
+        vel = np.random.default_rng(7).normal(0, 0.3, pos.shape).astype(np.float32)
+        return p, pos, vel, None, boxes
+    if kind == "dam_half_cell":
+        p = scenes.dam_params(iters=3)
+        p.cell = 0.5 * p.h
+        pos, vel, boxes = scenes.dam_break(n_side=64)
+        return p, pos, vel, None, boxes
+    if kind == "batched":
+        p = scenes.dam_params(iters=2)
+        pos, vel, dom, boxes = scenes.batched_scenes(n_scenes=5, seed=9, lo=500, hi=3000)
+        vel = np.random.default_rng(8).normal(0, 0.2, pos.shape).astype(np.float32)
+        return p, pos, vel, dom, boxes
+    if kind == "vortex":
+        p = scenes.dam_params(iters=2)
+        p.vort_eps = 5e-4
+        pos, vel, boxes = scenes.dam_break(n_side=64)
+        c = pos - pos.mean(0)
+        vel = np.stack([-c[:, 1], c[:, 0]], 1).astype(np.float32) * 3.0
+        return p, pos, vel, None, boxes
+    raise ValueError(kind)
+
+
+KINDS = ["reference", "dam", "dam_half_cell", "batched", "vortex"]
+
+
+def _engine(gpe_mod, p, pos, vel, dom, boxes):
+    e = gpe_mod.Pbf(p, boxes, capacity=len(pos) + 7)
+    e.set_state(pos, vel, dom)
+    return e
+
+
+def _close(a, b, scale, what, rel=1e-5, ulp_of=None):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    tol = rel * scale
+    if ulp_of is not None:
+        tol = tol + 4 * EPS32 * np.abs(np.asarray(ulp_of, np.float64))
+    err = np.abs(a - b)
+    bad = err > tol
+    assert not bad.any(), f"{what}: {bad.sum()} of {bad.size} beyond tolerance; max err {err.max():.3e}"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_predict_sort_bit_exact(gpe_mod, oracle, cuda_ok, kind):
+    p, pos, vel, dom, boxes = _scene(kind)
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    s = oracle.PbfOracle(p, boxes).predict_sort(pos, vel, dom)
+    assert np.array_equal(e.field(gpe_mod.PBF_FIELD_KEY), s["key"])
+    assert np.array_equal(e.field(gpe_mod.PBF_FIELD_PERM), s["perm"])
+    assert np.array_equal(e.field(gpe_mod.PBF_FIELD_CELL_START), s["cell_start"])
+    assert np.array_equal(e.field(gpe_mod.PBF_FIELD_POS).view(np.uint32), s["x"].view(np.uint32))
+    assert np.array_equal(e.field(gpe_mod.PBF_FIELD_PRED).view(np.uint32), s["xs"].view(np.uint32))
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_lambda_stage(gpe_mod, oracle, cuda_ok, kind):
+    p, pos, vel, dom, boxes = _scene(kind)
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    e.stage(gpe_mod.PBF_STAGE_LAMBDA)
+    lam = e.field(gpe_mod.PBF_FIELD_LAMBDA)
+    o = oracle.PbfOracle(p, boxes)
+    s = o.predict_sort(pos, vel, dom)
+    lo, _ = o.lambda_(s["xs"], s["dom"], s["cell_start"])
+    assert np.abs(lo).max() > 0
+    _close(lam, lo, np.abs(lo).max(), "lambda", rel=2e-5)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_delta_p_stage(gpe_mod, oracle, cuda_ok, kind):
+    p, pos, vel, dom, boxes = _scene(kind)
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    o = oracle.PbfOracle(p, boxes)
+    s = o.predict_sort(pos, vel, dom)
+    lo, _ = o.lambda_(s["xs"], s["dom"], s["cell_start"])
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    e.set_field(gpe_mod.PBF_FIELD_LAMBDA, lo)
+    e.stage(gpe_mod.PBF_STAGE_DELTA_P)
+    got = e.field(gpe_mod.PBF_FIELD_PRED)
+    want = o.delta_p(s["xs"], s["dom"], s["cell_start"], lo)
+    dp = np.abs(want.astype(np.float64) - s["xs"]).max()
+    assert dp > 0
+    _close(got, want, dp, "delta p", rel=1e-5, ulp_of=want)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_xsph_stage(gpe_mod, oracle, cuda_ok, kind):
+    p, pos, vel, dom, boxes = _scene(kind)
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    o = oracle.PbfOracle(p, boxes)
+    s = o.predict_sort(pos, vel, dom)
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    g = np.random.default_rng(1)
+    span = float(np.abs(s["xs"] - s["x"]).max()) + 1e-3 * p.h
+    xs2 = (s["xs"] + g.normal(0, 0.05 * span, s["xs"].shape)).astype(np.float32)
+    e.set_field(gpe_mod.PBF_FIELD_PRED, xs2)
+    e.stage(gpe_mod.PBF_STAGE_XSPH)
+    got = e.field(gpe_mod.PBF_FIELD_VEL)
+    want, w = o.xsph(s["x"], xs2, s["dom"], s["cell_start"])
+    vscale = np.abs(want).max()
+    # v = (x* - x)/dt carries the rounding of both positions
+    ulp_v = 4 * EPS32 * np.abs(xs2).max() / p.dt
+    _close(got, want, vscale, "xsph velocity", rel=1e-5 + ulp_v / vscale)
+    if p.vort_eps != 0:
+        got_w = e.field(gpe_mod.PBF_FIELD_OMEGA)
+        _close(got_w, w, np.abs(w).max(), "vorticity omega", rel=1e-4)
+        e.stage(gpe_mod.PBF_STAGE_VORTICITY)
+        got_v2 = e.field(gpe_mod.PBF_FIELD_VEL)
+        want_v2 = o.vorticity(xs2, s["dom"], s["cell_start"], got_w, got)
+        _close(got_v2, want_v2, np.abs(want_v2).max(), "vorticity velocity", rel=1e-5 + ulp_v / vscale)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_one_step(gpe_mod, oracle, cuda_ok, kind):
+    p, pos, vel, dom, boxes = _scene(kind)
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.step(1)
+    x, v, d = e.get_state()
+    r = oracle.PbfOracle(p, boxes).step(pos, vel, dom, n_steps=1)
+    if dom is not None:
+        assert np.array_equal(d, r["dom"])
+    # positions: 1e-5 relative to the coordinate, with a floor of 1e-6 of the domain scale
+    _close(x, r["x"], np.abs(r["x"]) + 0.1 * np.abs(r["x"]).max(), "x after one step", rel=1e-5)
+    vscale = np.abs(r["v"]).max()
+    ulp_v = 16 * EPS32 * np.abs(r["x"]).max() / p.dt
+    _close(v, r["v"], vscale, "v after one step", rel=1e-5 + ulp_v / vscale)
+    assert e.status() == 0
+
+
+def test_graph_replay_is_deterministic(gpe_mod, cuda_ok):
+    p, pos, vel, dom, boxes = _scene("dam")
+    a = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    b = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    a.step(3)
+    for _ in range(3):
+        b.step(1)
+    xa, va, _ = a.get_state()
+    xb, vb, _ = b.get_state()
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+def test_batched_equals_solo_bit_exact(gpe_mod, cuda_ok):
+    p, pos, vel, dom, boxes = _scene("batched")
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.step(3)
+    xb, vb, db = e.get_state()
+    for s, box in enumerate(boxes):
+        m = dom == s
+        solo = _engine(gpe_mod, p, pos[m], vel[m], None, [box])
+        solo.step(3)
+        xs, vs, _ = solo.get_state()
+        mb = db == s
+        assert np.array_equal(xb[mb].view(np.uint32), xs.view(np.uint32)), f"scene {s} positions differ"
+        assert np.array_equal(vb[mb].view(np.uint32), vs.view(np.uint32)), f"scene {s} velocities differ"
+
+
+def test_several_steps_track_oracle(gpe_mod, oracle, cuda_ok):
+    p, pos, vel, dom, boxes = _scene("dam")
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.step(5)
+    x, v, _ = e.get_state()
+    r = oracle.PbfOracle(p, boxes).step(pos, vel, dom, n_steps=5)
+    # FP32 vs FP64 trajectories separate slowly; after 5 steps they agree to 1e-3 h
+    assert np.abs(x.astype(np.float64) - r["x"]).max() < 1e-3 * p.h
+
+
+def test_density_error_matches_oracle(gpe_mod, oracle, cuda_ok):
+    p, pos, vel, dom, boxes = _scene("dam")
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.step(2)
+    mx, mn = e.density_error()
+    x, _, _ = e.get_state()
+    cs = e.field(gpe_mod.PBF_FIELD_CELL_START)
+    omx, omn = oracle.PbfOracle(p, boxes).density_error(x, None, cs)
+    assert mx == pytest.approx(omx, rel=1e-4, abs=1e-5)
+    assert mn == pytest.approx(omn, rel=1e-3, abs=1e-7)
+
+
+def test_edge_cases(gpe_mod, cuda_ok):
+    from gpe import scenes
+
+    p = scenes.dam_params()
+    box = [(0.0, 0.0, 1.0, 1.0)]
+    e = gpe_mod.Pbf(p, box, capacity=16)
+    # empty state steps cleanly
+    e.set_state(np.zeros((0, 2), np.float32))
+    e.step(2)
+    assert e.n == 0
+    # a single particle falls freely (no neighbours but itself)
+    e.set_state(np.array([[0.5, 0.5]], np.float32), np.zeros((1, 2), np.float32))
+    e.step(1)
+    x, v, _ = e.get_state()
+    assert x[0, 1] < 0.5 and abs(x[0, 0] - 0.5) < 1e-6
+    # particles outside the box are clamped into edge cells and then onto the walls
+    out = np.array([[-0.2, 0.5], [1.3, 0.5], [0.5, -5.0], [0.5, 2.0], [0.999999, 0.999999]], np.float32)
+    e.set_state(out, np.zeros_like(out))
+    e.step(1)
+    x, v, _ = e.get_state()
+    assert np.all(x >= 0) and np.all(x <= 1.0)
+    # capacity and argument errors come back as status codes
+    with pytest.raises(gpe_mod.GpeError) as ei:
+        e.set_state(np.zeros((17, 2), np.float32))
+    assert ei.value.status == gpe_mod.ERR_CAPACITY
+    # non-finite input is reported by the status word
+    bad = np.array([[0.5, np.nan], [0.2, 0.2]], np.float32)
+    e.set_state(bad, np.zeros_like(bad))
+    e.step(1)
+    assert e.status() & gpe_mod.STATUS_NONFINITE
+    e.close()
