@@ -40,13 +40,28 @@ def _scene(kind):
         p = scenes.dam_params(iters=2)
         p.vort_eps = 5e-4
         pos, vel, boxes = scenes.dam_break(n_side=64)
+        # a Gaussian vortex: |omega| varies in space, so the confinement direction grad|omega| is defined
+        # (in a rigid rotation |omega| is uniform and the direction is rounding noise)
         c = pos - pos.mean(0)
-        vel = np.stack([-c[:, 1], c[:, 0]], 1).astype(np.float32) * 3.0
+        om = 3.0 * np.exp(-(c ** 2).sum(1) / 0.15 ** 2)
+        vel = (np.stack([-c[:, 1], c[:, 0]], 1) * om[:, None]).astype(np.float32)
         return p, pos, vel, None, boxes
     raise ValueError(kind)
 
 
 KINDS = ["reference", "dam", "dam_half_cell", "batched", "vortex"]
+
+
+def _well_conditioned(kind, x, p):
+    """Particles whose vorticity-confinement direction grad|omega|/|grad|omega|| is defined: at the centre of
+    the Gaussian vortex |omega| has a maximum, the direction is 0/0 there and any rounding flips it."""
+    if kind != "vortex":
+        return np.ones(len(x), bool)
+    from gpe import scenes
+
+    pos0, _, _ = scenes.dam_break(n_side=64)
+    c = pos0.mean(0)
+    return np.linalg.norm(np.asarray(x, np.float64) - c, axis=1) > 3 * p.h
 
 
 def _engine(gpe_mod, p, pos, vel, dom, boxes):
@@ -134,7 +149,8 @@ def test_xsph_stage(gpe_mod, oracle, cuda_ok, kind):
         e.stage(gpe_mod.PBF_STAGE_VORTICITY)
         got_v2 = e.field(gpe_mod.PBF_FIELD_VEL)
         want_v2 = o.vorticity(xs2, s["dom"], s["cell_start"], got_w, got)
-        _close(got_v2, want_v2, np.abs(want_v2).max(), "vorticity velocity", rel=1e-5 + ulp_v / vscale)
+        m = _well_conditioned(kind, xs2, p)
+        _close(got_v2[m], want_v2[m], np.abs(want_v2).max(), "vorticity velocity", rel=1e-5 + ulp_v / vscale)
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -150,7 +166,8 @@ def test_one_step(gpe_mod, oracle, cuda_ok, kind):
     _close(x, r["x"], np.abs(r["x"]) + 0.1 * np.abs(r["x"]).max(), "x after one step", rel=1e-5)
     vscale = np.abs(r["v"]).max()
     ulp_v = 16 * EPS32 * np.abs(r["x"]).max() / p.dt
-    _close(v, r["v"], vscale, "v after one step", rel=1e-5 + ulp_v / vscale)
+    m = _well_conditioned(kind, r["x"], p)
+    _close(v[m], r["v"][m], vscale, "v after one step", rel=1e-5 + ulp_v / vscale)
     assert e.status() == 0
 
 
