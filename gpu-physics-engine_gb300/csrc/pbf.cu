@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -1187,3 +1188,142 @@ int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
 }
 
 } // extern "C"
+
+// =====================================================================================================
+// Allocation-free predict + sort (gpe_pbf_predict_sort_noalloc)
+//
+// For callers that cannot call cudaMalloc (a host whose device memory belongs to another framework, a
+// real-time loop that must not allocate after start-up). The scratch of the sort — unsorted predictions,
+// (key, rank) pairs, cell buckets, the cell histogram and the scan's block sums — lives in one fixed
+// static device array sized for GPE_NOALLOC_MAX_PARTICLES particles and GPE_NOALLOC_MAX_CELLS cells. Every
+// GPU that loads this library holds the array until the process exits. All calls share it and each call
+// overwrites it; the histogram is cleared at the start of every call. Calls that overlap on the GPU race.
+// =====================================================================================================
+
+namespace {
+
+constexpr size_t NA_MAX_N     = (size_t)GPE_NOALLOC_MAX_PARTICLES;
+constexpr size_t NA_MAX_CELLS = (size_t)GPE_NOALLOC_MAX_CELLS;
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t NA_OFF_XS    = 0;                                                  // float2[n]
+constexpr size_t NA_OFF_KR    = na_align(NA_OFF_XS + sizeof(float2) * NA_MAX_N);    // uint2[n]
+constexpr size_t NA_OFF_BK    = na_align(NA_OFF_KR + sizeof(uint2) * NA_MAX_N);     // uint32[n]
+constexpr size_t NA_OFF_CNT   = na_align(NA_OFF_BK + sizeof(uint32_t) * NA_MAX_N);  // uint32[cells]
+constexpr size_t NA_OFF_BS    = na_align(NA_OFF_CNT + sizeof(uint32_t) * NA_MAX_CELLS);
+constexpr size_t NA_BYTES     = na_align(NA_OFF_BS + sizeof(uint32_t) * (NA_MAX_CELLS / 2048 + 1));
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+uint8_t* g_na_ptr[NA_MAX_DEVICES] = {};
+
+} // namespace
+
+static __device__ __align__(256) uint8_t gpe_noalloc_scratch[NA_BYTES];
+
+namespace {
+
+// Device address of the scratch array on the current device. In host code the symbol itself is only a
+// host-side stand-in, so the address is looked up once per device (with that device current) and cached.
+int32_t noalloc_scratch(uint8_t** out)
+{
+    int dev = 0;
+    GPE_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NA_MAX_DEVICES) {
+        gpe::set_error(GPE_ERR_DEVICE, "gpe_pbf_predict_sort_noalloc: device %d out of range", dev);
+        return GPE_ERR_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_ptr[dev]) {
+        void* p             = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, gpe_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            gpe::set_cuda_error(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress");
+            return GPE_ERR_CUDA;
+        }
+        g_na_ptr[dev] = static_cast<uint8_t*>(p);
+    }
+    *out = g_na_ptr[dev];
+    return GPE_OK;
+}
+
+} // namespace
+
+extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, const gpe_domain* domain,
+                                                const float* pos, const float* vel, int64_t n, float* pos_sorted,
+                                                float* pred_sorted, uint32_t* key_sorted, uint32_t* perm,
+                                                uint32_t* cell_start, int64_t n_cells, void* stream)
+{
+    gpe::clear_error();
+    if (!domain || !cell_start || n < 0 ||
+        (n > 0 && (!pos || !vel || !pos_sorted || !pred_sorted || !key_sorted || !perm))) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_predict_sort_noalloc: null pointer or negative size");
+        return GPE_ERR_BAD_ARG;
+    }
+    int32_t rc = validate_params(params);
+    if (rc) { return rc; }
+    if (!(domain->extent[0] > 0.f) || !(domain->extent[1] > 0.f)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_predict_sort_noalloc: non-positive scene extent");
+        return GPE_ERR_BAD_ARG;
+    }
+    const uint64_t cells = count_cells(params, domain, 1);
+    if ((int64_t)cells != n_cells) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_predict_sort_noalloc: the scene has %llu cells, not %lld",
+                       (unsigned long long)cells, (long long)n_cells);
+        return GPE_ERR_BAD_ARG;
+    }
+    if ((size_t)n > NA_MAX_N || (size_t)cells > NA_MAX_CELLS) {
+        gpe::set_error(GPE_ERR_CAPACITY,
+                       "gpe_pbf_predict_sort_noalloc: %lld particles / %llu cells exceed the static scratch "
+                       "limits of %d particles / %d cells",
+                       (long long)n, (unsigned long long)cells, GPE_NOALLOC_MAX_PARTICLES, GPE_NOALLOC_MAX_CELLS);
+        return GPE_ERR_CAPACITY;
+    }
+    uint8_t* scratch = nullptr;
+    rc               = noalloc_scratch(&scratch);
+    if (rc) { return rc; }
+    float2* xs_tmp   = reinterpret_cast<float2*>(scratch + NA_OFF_XS);
+    uint2* keyrank   = reinterpret_cast<uint2*>(scratch + NA_OFF_KR);
+    uint32_t* bucket = reinterpret_cast<uint32_t*>(scratch + NA_OFF_BK);
+    uint32_t* count  = reinterpret_cast<uint32_t*>(scratch + NA_OFF_CNT);
+    uint32_t* bsum   = reinterpret_cast<uint32_t*>(scratch + NA_OFF_BS);
+
+    // kernel constants for the one scene, as build_domains derives them for an engine
+    const float cell = params->cell > 0.f ? params->cell : params->h;
+    PbfK k           = make_k(*params);
+    DomDev d{};
+    d.ox   = domain->origin[0];
+    d.oy   = domain->origin[1];
+    d.lox  = domain->origin[0];
+    d.loy  = domain->origin[1];
+    d.hix  = (domain->origin[0] + domain->extent[0]) - params->wall_margin;
+    d.hiy  = (domain->origin[1] + domain->extent[1]) - params->wall_margin;
+    d.ncx  = cells_along(domain->extent[0], cell);
+    d.ncy  = cells_along(domain->extent[1], cell);
+    d.coff = 0;
+    k.d0   = d;
+    k.n    = (int32_t)n;
+
+    cudaStream_t st = as_stream(stream);
+    // the histogram must start at zero whatever an earlier (possibly failed) call left behind
+    GPE_TRY_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t) * cells, st));
+    if (n > 0) {
+        k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(k, nullptr, nullptr,
+                                                                reinterpret_cast<const float2*>(pos),
+                                                                reinterpret_cast<const float2*>(vel), xs_tmp,
+                                                                keyrank, count);
+        GPE_CHECK_LAUNCH("k_predict_hist (noalloc)");
+    }
+    rc = launch_exclusive_scan(count, (uint32_t)cells, bsum, cell_start, st);
+    if (rc) { return rc; }
+    if (n > 0) {
+        rc = launch_scatter(keyrank, n, cell_start, bucket, st);
+        if (rc) { return rc; }
+        k_place<<<blocks_for(n), T_PART, 0, st>>>((int32_t)n, keyrank, cell_start, bucket,
+                                                  reinterpret_cast<const float2*>(pos), xs_tmp,
+                                                  reinterpret_cast<float2*>(pos_sorted),
+                                                  reinterpret_cast<float2*>(pred_sorted), perm, key_sorted, nullptr,
+                                                  nullptr);
+        GPE_CHECK_LAUNCH("k_place (noalloc)");
+    }
+    return GPE_OK;
+}

@@ -146,6 +146,27 @@ int32_t gpe_pbf_status(gpe_pbf* pbf, uint32_t* status, void* stream);
 /* Number of kernel launches the last gpe_pbf_step issued per step. */
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* pbf, int32_t* launches);
 
+/* Allocation-free predict + cell sort for one scene. It has no counterpart in the reference (whose arenas
+ * are all allocated up front, cuda-engine.cpp:102-139); it exists for callers that cannot call cudaMalloc,
+ * such as a host whose device memory is owned by another framework, or a real-time loop that must not
+ * allocate once it is running. It runs the same kernels as GPE_PBF_STAGE_PREDICT_SORT on caller buffers
+ * and keeps its scratch in a fixed static device array (9.0 MiB, sized for the limits below, held by every
+ * GPU that loads the library until the process exits), so it never allocates.
+ *   in : pos, vel  n float2 (device pointers), one scene `domain`, `params`
+ *   out: pos_sorted, pred_sorted n float2; key_sorted, perm n uint32; cell_start n_cells + 1 uint32
+ *        (n_cells from the scene extent and the sort-cell size, as gpe_pbf_num_cells reports).
+ * Limits: n <= GPE_NOALLOC_MAX_PARTICLES and n_cells <= GPE_NOALLOC_MAX_CELLS, else GPE_ERR_CAPACITY.
+ * The first call on a device looks up the scratch array's device address (cudaGetSymbolAddress) and should
+ * come before any stream capture. All calls share the one array: calls that overlap on the GPU (on
+ * different streams, or from several host threads) race, so serialise them. */
+#define GPE_NOALLOC_MAX_PARTICLES (1 << 18)
+#define GPE_NOALLOC_MAX_CELLS (1 << 20)
+int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, const gpe_domain* domain, const float* pos,
+                                     const float* vel, int64_t n, float* pos_sorted, float* pred_sorted,
+                                     uint32_t* key_sorted, uint32_t* perm, uint32_t* cell_start, int64_t n_cells,
+                                     void* stream);
+
+
 /* ======================================================================================================
  * MLS-MPM
  * ====================================================================================================== */
