@@ -157,6 +157,65 @@ def cpu_baseline(p, pos, vel, boxes, budget_s=12.0, max_steps=30):
             "sample": f"{steps} full steps of the {len(pos)}-particle workload (FP64 oracle, OpenMP)"}
 
 
+def reference_cuda_leg(args, stream, flush_l2):
+    """The reference's own PBF kernels (PBF.cu built for sm_103a, a 32 x 32-chunk world) against the engine on
+    the same 1M-atom scene with the reference's constants (2 Jacobi iterations, dt = 1 units). Both timed per
+    substep with CUDA events after an L2 flush; the reference's substep (10 nodes, PBF.cu:921-955) is
+    captured once into a CUDA graph as the reference does."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+
+    cubin = ROOT / "oracle" / "_ref" / "PBF_ref_32x32_m320.cubin"
+    if not cubin.exists():
+        return {"unavailable": "reference kernels not built (oracle/build_ref.py needs the reference sources)"}
+    from oracle import refrun
+
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_million()
+    n = len(pos)
+    sh = stream.cuda_stream
+
+    def timed(run_one):
+        for _ in range(args.warmup):
+            run_one()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        for a, b in ev:
+            flush_l2()
+            a.record(stream)
+            run_one()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+    ref = refrun.RefPBF((32, 32), 320, cubin=cubin)
+    ref.seed(pos, vel, float(p.gravity[1]))
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        ref.substep(iters=p.iters, full=True, stream=sh)
+
+    def replay():
+        with torch.cuda.stream(stream):  # replay on the stream the events are recorded on
+            graph.replay()
+
+    ref_s = timed(replay)
+    atoms_kept = int(ref.num_atoms.sum().item())
+    del graph, ref
+    e = gpe.Pbf(p, boxes, capacity=n)
+    e.set_state(pos, vel, stream=sh)
+    eng_s = timed(lambda: e.step(1, stream=sh))
+    e.close()
+    return {"workload": "pbf_1m_reference_units_k2", "particles": n, "unit": "particle-steps/s",
+            "reference_value": n * args.steps / ref_s, "engine_value": n * args.steps / eng_s,
+            "speedup": ref_s / eng_s, "reference_ms_per_step": 1e3 * ref_s / args.steps,
+            "engine_ms_per_step": 1e3 * eng_s / args.steps, "reference_atoms_after": atoms_kept,
+            "how": "reference PBF.cu kernels (sm_103a cubin, 32x32 chunks) in a CUDA graph vs gpe_pbf_step, "
+                   "same scene and constants, L2 flushed before each timed substep"}
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return
@@ -289,6 +348,13 @@ def run_gpe(args, rank, ws):
     base = None
     if ws == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(p, pos, vel, boxes)
+    ref_cuda = None
+    if ws == 1 and not args.no_reference_cuda:
+        eng.close()
+        try:
+            ref_cuda = reference_cuda_leg(args, stream, flush_l2)
+        except Exception as exc:  # reported, never fatal to the headline number
+            ref_cuda = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
     ms = 1e3 * total_s / args.steps
     line = {"metric": "pbf_particle_steps_per_s_1m", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -296,7 +362,8 @@ def run_gpe(args, rank, ws):
             "config": cfg, "e2e": e2e, "roofline": roofline, "cpu_baseline": base,
             "gpu_launches": launches * args.steps, "launches_per_step": launches,
             "hbm_effective_gbs": 212.0 * value / ws / 1e9,
-            "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary()}
+            "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary(),
+            "reference_cuda": ref_cuda}
     print(json.dumps(line), flush=True)
 
 
@@ -307,6 +374,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpe", choices=["gpe", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -179,7 +179,8 @@ __global__ void __launch_bounds__(T_PART)
 template <bool MULTI, bool SELFG>
 __global__ void __launch_bounds__(T_PART)
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam)
+             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
+             const uint32_t* __restrict__ pair_id)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) { return; }
@@ -199,7 +200,12 @@ __global__ void __launch_bounds__(T_PART)
             nx = rx * inv;
             ny = ry * inv;
         } else if (SELFG) {
-            pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
+            // coincident pair (always the self pair): the reference seeds the direction with chunk slots
+            if (pair_id) {
+                pair_direction(__ldg(&pair_id[i]), __ldg(&pair_id[j]), nx, ny);
+            } else {
+                pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
+            }
         } else {
             nx = 0.f;
             ny = 0.f;
@@ -610,7 +616,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st);
     if (rc) { return rc; }
     if (n > 0) {
-        const bool ids = (s->prm.flags & GPE_PBF_TRACK_IDS) != 0;
+        const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
         k_place<<<blocks_for(n), T_PART, 0, st>>>(n, s->keyrank, s->start, s->bucket, s->pos[s->X], s->xs_tmp,
                                                   s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
                                                   ids ? s->ids[s->id_cur] : nullptr,
@@ -626,20 +632,21 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
 {
     if (s->n == 0) { return GPE_OK; }
-    const bool sg = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0;
+    const bool sg    = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0;
     const unsigned g = blocks_for(s->n);
+    const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
+    float2* xs       = s->pos[s->XS];
     if (multi(s)) {
         if (sg) {
-            k_lambda<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+            k_lambda<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
         } else {
-            k_lambda<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+            k_lambda<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
         }
     } else {
         if (sg) {
-            k_lambda<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam);
+            k_lambda<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
         } else {
-            k_lambda<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
-                                                         s->lam);
+            k_lambda<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
         }
     }
     GPE_CHECK_LAUNCH("k_lambda");

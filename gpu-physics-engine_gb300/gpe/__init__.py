@@ -19,7 +19,7 @@ OK, ERR_CUDA, ERR_DEVICE, ERR_NOT_READY, ERR_BAD_ARG, ERR_ALREADY, ERR_CAPACITY,
 MEM_HOST, MEM_DEVICE = 0, 1
 STATUS_NONFINITE, STATUS_CAPACITY, STATUS_CELL_OVERFLOW, STATUS_TIMEOUT = 1, 2, 4, 8
 
-PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS = 0x1, 0x2, 0x4
+PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS = 0x1, 0x2, 0x4, 0x8
 (PBF_STAGE_PREDICT_SORT, PBF_STAGE_LAMBDA, PBF_STAGE_DELTA_P, PBF_STAGE_XSPH, PBF_STAGE_VORTICITY,
  PBF_STAGE_FINISH, PBF_STAGE_DENSITY) = range(7)
 (PBF_FIELD_POS, PBF_FIELD_VEL, PBF_FIELD_PRED, PBF_FIELD_LAMBDA, PBF_FIELD_KEY, PBF_FIELD_PERM,

@@ -70,6 +70,18 @@ def reference_pbf_block(nx: int = 48, ny: int = 40, spacing: float = 1.05, seed:
     return pos.astype(F32), vel.astype(F32), [box]
 
 
+def reference_million(seed: int = 12, side: int = 1024):
+    """1,048,576 atoms on a 1024 x 1024 lattice (spacing 1, the atom diameter) filling a 32 x 32-chunk world
+    of the reference (1024 x 1024 units, 1024 atoms per chunk of capacity 1536), small random
+    displacements; reference units. The same scene drives the engine and the reference's kernels."""
+    g = rng(seed)
+    ix, iy = np.meshgrid(np.arange(side), np.arange(side), indexing="xy")
+    pos = np.stack([ix.ravel() + 0.5, iy.ravel() + 0.5], 1)
+    pos += g.uniform(-0.05, 0.05, pos.shape)
+    vel = g.uniform(-0.02, 0.02, pos.shape)
+    return pos.astype(F32), vel.astype(F32), [(0.0, 0.0, float(side), float(side))]
+
+
 def lattice_mass(h: float, spacing: float, rho0: float = 1.0) -> float:
     """Particle mass that makes the 2D poly6 density of a square lattice equal rho0."""
     c6 = 4.0 / (math.pi * h ** 8)

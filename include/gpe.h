@@ -61,7 +61,9 @@ int32_t gpe_version(void);                /* major*10000 + minor*100 + patch    
                                      the atom itself; coincident pairs take pairDirection, PBF.cu:309-321) */
 #define GPE_PBF_VEL_CLAMP 0x2u    /* clamp |v| to [v_min, v_max] after XSPH (velocityClamp, PBF.cu:629-638) */
 #define GPE_PBF_TRACK_IDS 0x4u    /* carry a particle id through every sort (for external bookkeeping)      */
-#define GPE_PBF_SELF_XSPH 0x8u    /* reserved                                                                */
+#define GPE_PBF_PAIR_IDS 0x8u     /* seed pairDirection with the tracked particle ids instead of the sorted
+                                     index within the scene (the reference seeds it with the atom's slot in
+                                     its chunk, PBF.cu:277); implies GPE_PBF_TRACK_IDS                       */
 
 typedef struct gpe_pbf_params {
     float h;            /* smoothing radius (reference kH, constants.h:35)                          */
@@ -165,7 +167,6 @@ int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, const gpe_dom
                                      const float* vel, int64_t n, float* pos_sorted, float* pred_sorted,
                                      uint32_t* key_sorted, uint32_t* perm, uint32_t* cell_start, int64_t n_cells,
                                      void* stream);
-
 
 /* ======================================================================================================
  * MLS-MPM

@@ -1,0 +1,65 @@
+"""Builds the reference's own solver kernels headless for sm_103a — test infrastructure for the parity tests
+and the reference-CUDA timing leg, never part of the engine.
+
+libs/cuda-engine/source/PBF.cu and MPM.cu are compiled unmodified from /root/reference into device-only
+cubins under oracle/_ref/ (git-ignored; the cubins travel to the GPU machine, where the reference sources do not
+exist). Two stand-in headers in oracle/shim/common replace the reference's MSVC-only macros.h and its
+umbrella.h, and supply its constants.h values with the scene size and capacities overridable by -D.
+Where the sources are absent (the GPU machine), prebuilt cubins are used as they are.
+"""
+from __future__ import annotations
+
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+REF = Path("/root/reference")
+SRC = REF / "libs" / "cuda-engine" / "source"
+INC = REF / "libs" / "cuda-engine" / "include"
+
+# (file stem, kernel source, -D overrides)
+VARIANTS = [
+    ("PBF_ref_12x6_m320", "PBF.cu", {}),
+    ("PBF_ref_32x32_m320", "PBF.cu", {"GPE_REF_SCENE_X": 32, "GPE_REF_SCENE_Y": 32}),
+    ("MPM_ref_12x6_n400000", "MPM.cu", {}),
+    ("MPM_ref_64x64_n4194304", "MPM.cu", {"GPE_REF_SCENE_X": 64, "GPE_REF_SCENE_Y": 64,
+                                          "GPE_REF_MPM_ATOMS": 4194304}),
+]
+
+
+def _nvcc() -> str:
+    return shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+
+
+def build(force: bool = False) -> list[Path]:
+    OUT.mkdir(exist_ok=True)
+    outs = [OUT / f"{stem}.cubin" for stem, _, _ in VARIANTS]
+    if not SRC.exists():
+        return [o for o in outs if o.exists()]
+    shim = sorted((HERE / "shim" / "common").glob("*.h"))
+    jobs = []
+    for (stem, src, defs), out in zip(VARIANTS, outs):
+        deps = [SRC / src, *shim]
+        if not force and out.exists() and all(d.stat().st_mtime <= out.stat().st_mtime for d in deps):
+            continue
+        cmd = [_nvcc(), "-cubin", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
+               "-diag-suppress", "177", "-I", str(HERE / "shim"), "-I", str(INC),
+               *[f"-D{k}={v}" for k, v in defs.items()], "-o", str(out), str(SRC / src)]
+        jobs.append(cmd)
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference kernel build failed: " + " ".join(cmd) + "\n" + r.stderr)
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        list(ex.map(run, jobs))
+    return outs
+
+
+if __name__ == "__main__":
+    for p in build(force=True):
+        print(p)

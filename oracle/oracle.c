@@ -231,7 +231,7 @@ void orc_pbf_predict_sort(const gpe_pbf_params* p, const gpe_domain* doms, int32
 
 /* ----- lambda: PBF.cu:243-294 ----- */
 static double lambda_one(const gpe_pbf_params* p, const kconst* k, const dinfo* d, const uint32_t* cs, int64_t i,
-                         int64_t pbase, const double* xs, double* rho_out)
+                         int64_t pbase, const double* xs, const uint32_t* pair_id, double* rho_out)
 {
     const double px = xs[2 * i], py = xs[2 * i + 1];
     int64_t beg[16], end[16];
@@ -251,7 +251,11 @@ static double lambda_one(const gpe_pbf_params* p, const kconst* k, const dinfo* 
             }
             if (px == xs[2 * j] && py == xs[2 * j + 1]) {
                 if (p->flags & GPE_PBF_SELF_GRAD) {
-                    pair_direction(i - pbase, j - pbase, &nx, &ny);
+                    if (pair_id) {
+                        pair_direction(pair_id[i], pair_id[j], &nx, &ny);
+                    } else {
+                        pair_direction(i - pbase, j - pbase, &nx, &ny);
+                    }
                 } else {
                     nx = ny = 0.0;
                 }
@@ -289,14 +293,14 @@ static double* to_double(const float* a, int64_t n)
 }
 
 static void lambda_pass(const gpe_pbf_params* p, const dinfo* di, const int64_t* pb, int64_t n, const double* xs,
-                        const int32_t* dom, const uint32_t* cs, double* lambda, double* rho)
+                        const int32_t* dom, const uint32_t* cs, const uint32_t* pair_id, double* lambda, double* rho)
 {
     const kconst k = make_kconst(p);
 #pragma omp parallel for schedule(dynamic, 1024)
     for (int64_t i = 0; i < n; ++i) {
         const int32_t d = dom_of(dom, i);
         double r;
-        lambda[i] = lambda_one(p, &k, &di[d], cs, i, pb[d], xs, &r);
+        lambda[i] = lambda_one(p, &k, &di[d], cs, i, pb[d], xs, pair_id, &r);
         if (rho) { rho[i] = r; }
     }
 }
@@ -477,7 +481,8 @@ static void density_pass(const gpe_pbf_params* p, const dinfo* di, int64_t n, co
 
 /* ----- public stage wrappers (FP32 in/out) ----- */
 void orc_pbf_lambda(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
-                    const int32_t* dom, const uint32_t* cell_start, float* lambda, float* rho)
+                    const int32_t* dom, const uint32_t* cell_start, const uint32_t* pair_id, float* lambda,
+                    float* rho)
 {
     dinfo* di   = (dinfo*)malloc(sizeof(dinfo) * (size_t)nd);
     build_dinfo(p, doms, nd, di);
@@ -485,7 +490,7 @@ void orc_pbf_lambda(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd,
     double* xd  = to_double(xs, 2 * n);
     double* l   = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
     double* r   = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
-    lambda_pass(p, di, pb, n, xd, dom, cell_start, l, r);
+    lambda_pass(p, di, pb, n, xd, dom, cell_start, pair_id, l, r);
     for (int64_t i = 0; i < n; ++i) {
         lambda[i] = (float)l[i];
         if (rho) { rho[i] = (float)r[i]; }
@@ -590,7 +595,7 @@ void orc_pbf_density_error(const gpe_pbf_params* p, const gpe_domain* doms, int3
 }
 
 void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
-                  int32_t* dom, int32_t n_steps, float* lambda_out, uint32_t* cell_start_out)
+                  int32_t* dom, uint32_t* pair_id, int32_t n_steps, float* lambda_out, uint32_t* cell_start_out)
 {
     dinfo* di            = (dinfo*)malloc(sizeof(dinfo) * (size_t)nd);
     build_dinfo(p, doms, nd, di);
@@ -608,15 +613,20 @@ void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, i
     double* lam          = (double*)malloc(sizeof(double) * nn);
     double* vd           = (double*)malloc(sizeof(double) * 2 * nn);
     double* w            = (double*)malloc(sizeof(double) * nn);
+    uint32_t* pid_sorted = pair_id ? (uint32_t*)malloc(sizeof(uint32_t) * nn) : NULL;
     for (int32_t s = 0; s < n_steps; ++s) {
         orc_pbf_predict_sort(p, doms, nd, n, x, v, dom, key, perm, cs, xsort, xssort, dsort);
+        if (pair_id) {
+            for (int64_t i = 0; i < n; ++i) { pid_sorted[i] = pair_id[perm[i]]; }
+            memcpy(pair_id, pid_sorted, sizeof(uint32_t) * nn);
+        }
         int64_t* pb = dom_pbase(di, nd, cs);
         for (int64_t i = 0; i < 2 * n; ++i) {
             xd[i]  = xsort[i];
             xsa[i] = xssort[i];
         }
         for (int32_t it = 0; it < p->iters; ++it) {
-            lambda_pass(p, di, pb, n, xsa, dsort, cs, lam, NULL);
+            lambda_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, lam, NULL);
             delta_p_pass(p, di, n, xsa, dsort, cs, lam, xsb);
             double* t = xsa;
             xsa       = xsb;
@@ -637,6 +647,7 @@ void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, i
         for (int64_t i = 0; i < n; ++i) { lambda_out[i] = (float)lam[i]; }
     }
     if (cell_start_out) { memcpy(cell_start_out, cs, sizeof(uint32_t) * ((size_t)ncells + 1)); }
+    free(pid_sorted);
     free(w);
     free(vd);
     free(lam);

@@ -27,8 +27,10 @@ void orc_pbf_predict_sort(const gpe_pbf_params* p, const gpe_domain* doms, int32
                           const float* x, const float* v, const int32_t* dom, uint32_t* key, uint32_t* perm,
                           uint32_t* cell_start, float* x_sorted, float* xs_sorted, int32_t* dom_sorted);
 /* Stage restatements on sorted inputs (FP64 arithmetic, FP32 in/out). */
+/* pair_id (sorted order, may be NULL) seeds the coincident-pair direction instead of the sorted index */
 void orc_pbf_lambda(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
-                    const int32_t* dom, const uint32_t* cell_start, float* lambda, float* rho);
+                    const int32_t* dom, const uint32_t* cell_start, const uint32_t* pair_id, float* lambda,
+                    float* rho);
 void orc_pbf_delta_p(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
                      const int32_t* dom, const uint32_t* cell_start, const float* lambda, float* xs_out);
 void orc_pbf_xsph(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* x,
@@ -38,11 +40,11 @@ void orc_pbf_vorticity(const gpe_pbf_params* p, const gpe_domain* doms, int32_t 
                        float* v_inout);
 void orc_pbf_density(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
                      const int32_t* dom, const uint32_t* cell_start, float* rho);
-/* Whole steps. x, v, dom are the state in the current order and are replaced by the state in the new sorted
- * order after each step (x <- final x*). Between iterations x* is kept in FP64. lambda (may be NULL)
- * receives the last iteration's lambda. */
+/* Whole steps. x, v, dom (and pair_id, may be NULL) are the state in the current order and are replaced by
+ * the state in the new sorted order after each step (x <- final x*). Between iterations x* is kept in FP64.
+ * lambda (may be NULL) receives the last iteration's lambda. */
 void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
-                  int32_t* dom, int32_t n_steps, float* lambda, uint32_t* cell_start_out);
+                  int32_t* dom, uint32_t* pair_id, int32_t n_steps, float* lambda, uint32_t* cell_start_out);
 /* max_i max(rho_i/rho0-1,0) and mean of the same over particles, from orc_pbf_density on x. */
 void orc_pbf_density_error(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n,
                            const float* x, const int32_t* dom, const uint32_t* cell_start, double* max_err,

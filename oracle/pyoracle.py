@@ -28,12 +28,12 @@ def lib() -> C.CDLL:
         L.orc_pbf_num_cells.restype = i64
         L.orc_pbf_num_cells.argtypes = [pp, dp, i32]
         L.orc_pbf_predict_sort.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
-        L.orc_pbf_lambda.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp]
+        L.orc_pbf_lambda.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, vp]
         L.orc_pbf_delta_p.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp]
         L.orc_pbf_xsph.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, vp]
         L.orc_pbf_vorticity.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp]
         L.orc_pbf_density.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp]
-        L.orc_pbf_step.argtypes = [pp, dp, i32, i64, vp, vp, vp, i32, vp, vp]
+        L.orc_pbf_step.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, i32, vp, vp]
         L.orc_pbf_density_error.argtypes = [pp, dp, i32, i64, vp, vp, vp, C.POINTER(C.c_double),
                                             C.POINTER(C.c_double)]
         L.orc_mpm_p2g.argtypes = [mp, i64, vp, vp, vp, vp, vp, vp, vp]
@@ -79,13 +79,13 @@ class PbfOracle:
                                    _p(perm), _p(cs), _p(xso), _p(xss), _p(ds))
         return dict(key=key, perm=perm, cell_start=cs, x=xso, xs=xss, dom=ds)
 
-    def lambda_(self, xs, dom, cs):
+    def lambda_(self, xs, dom, cs, pair_id=None):
         xs = _c(xs, np.float32)
         n = xs.shape[0]
         lam = np.empty(n, np.float32)
         rho = np.empty(n, np.float32)
         lib().orc_pbf_lambda(C.byref(self.params), self.doms, self.nd, n, _p(xs), _p(_c(dom, np.int32)),
-                             _p(_c(cs, np.uint32)), _p(lam), _p(rho))
+                             _p(_c(cs, np.uint32)), _p(_c(pair_id, np.uint32)), _p(lam), _p(rho))
         return lam, rho
 
     def delta_p(self, xs, dom, cs, lam):
@@ -120,16 +120,17 @@ class PbfOracle:
                               _p(_c(dom, np.int32)), _p(_c(cs, np.uint32)), _p(rho))
         return rho
 
-    def step(self, x, v, dom=None, n_steps=1):
+    def step(self, x, v, dom=None, n_steps=1, pair_id=None):
         x = np.array(x, dtype=np.float32, copy=True).reshape(-1, 2)
         v = np.array(v, dtype=np.float32, copy=True).reshape(-1, 2)
         dom = None if dom is None else np.array(dom, dtype=np.int32, copy=True)
+        pid = None if pair_id is None else np.array(pair_id, dtype=np.uint32, copy=True)
         n = x.shape[0]
         lam = np.empty(n, np.float32)
         cs = np.empty(self.num_cells + 1, np.uint32)
-        lib().orc_pbf_step(C.byref(self.params), self.doms, self.nd, n, _p(x), _p(v), _p(dom), int(n_steps),
-                           _p(lam), _p(cs))
-        return dict(x=x, v=v, dom=dom, lam=lam, cell_start=cs)
+        lib().orc_pbf_step(C.byref(self.params), self.doms, self.nd, n, _p(x), _p(v), _p(dom), _p(pid),
+                           int(n_steps), _p(lam), _p(cs))
+        return dict(x=x, v=v, dom=dom, lam=lam, cell_start=cs, pair_id=pid)
 
     def density_error(self, x, dom, cs):
         x = _c(x, np.float32)

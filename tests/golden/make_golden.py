@@ -1,0 +1,55 @@
+"""Generates the golden fixtures in this directory by running the reference's own kernels (built headless by
+oracle/build_ref.py) on a GPU:
+
+  pbf_reference_substep.npz  one PBF substep of a 48 x 40 atom block that straddles chunk borders, stopped
+                             after XSPHKernel (PBF.cu:921-946): inputs x, v (absolute, dt = 1 units), the
+                             chunk slot of every atom (the reference's pairDirection seed), and the outputs
+                             x* (corrected), v (XSPH + clamp) and lambda of the last iteration, per input atom.
+  mpm_reference_substep.npz  one MLS-MPM substep (resetGrid, P2G, grid, G2P; MPM.cu:357-368) of a 30 x 40
+                             particle block with random v, C, F, J: inputs and outputs per particle.
+
+Usage (on a machine with a GPU): python tests/golden/make_golden.py OUT_DIR
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "gpu-physics-engine_gb300"))
+sys.path.insert(0, str(ROOT))
+
+
+def make_pbf():
+    from gpe import scenes
+    from oracle import refrun
+
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_pbf_block()
+    ref = refrun.RefPBF((12, 6), 320)
+    _, slot = ref.seed(pos, vel, float(p.gravity[1]))
+    ref.substep(iters=2, full=False)
+    xs, v, lam = ref.read_seeded()
+    return dict(x=pos, v=vel, slot=slot.astype(np.uint32), out_x=xs, out_v=v, out_lambda=lam)
+
+
+def make_mpm():
+    from gpe import scenes
+    from oracle import refrun
+
+    x, v, Cm, F, J = scenes.reference_mpm_block(nx=30, ny=40)
+    ref = refrun.RefMPM(400 * 1000, (12, 6))
+    ref.seed(x, v, Cm, F, J)
+    ref.substep(0)
+    ox, ov, oC, oF, oJ = ref.read()
+    return dict(x=x, v=v, C=Cm, F=F, J=J, out_x=ox, out_v=ov, out_C=oC, out_F=oF, out_J=oJ)
+
+
+if __name__ == "__main__":
+    out = Path(sys.argv[1] if len(sys.argv) > 1 else Path(__file__).parent)
+    out.mkdir(parents=True, exist_ok=True)
+    np.savez_compressed(out / "pbf_reference_substep.npz", **make_pbf())
+    np.savez_compressed(out / "mpm_reference_substep.npz", **make_mpm())
+    print("wrote", out)

@@ -166,8 +166,18 @@ def test_one_step(gpe_mod, oracle, cuda_ok, kind):
     _close(x, r["x"], np.abs(r["x"]) + 0.1 * np.abs(r["x"]).max(), "x after one step", rel=1e-5)
     vscale = np.abs(r["v"]).max()
     ulp_v = 16 * EPS32 * np.abs(r["x"]).max() / p.dt
-    m = _well_conditioned(kind, r["x"], p)
-    _close(v[m], r["v"][m], vscale, "v after one step", rel=1e-5 + ulp_v / vscale)
+    if kind == "vortex":
+        # The confinement direction N = grad|omega| / |grad|omega|| is 0/0 wherever |omega| has an extremum
+        # (the vortex core and the ring where the Gaussian vortex's omega changes sign), so FP32 and FP64 may
+        # pick different N there; each such particle can differ by at most the confinement kick
+        # 2 dt eps |omega|. All other particles must meet the tight bound.
+        tol = (1e-5 + ulp_v / vscale) * vscale
+        err = np.abs(v.astype(np.float64) - r["v"]).max(1)
+        kick = 2 * p.dt * p.vort_eps * np.abs(e.field(gpe_mod.PBF_FIELD_OMEGA)).max()
+        assert (err <= tol).mean() > 0.98, f"only {(err <= tol).mean():.4f} of particles within {tol:.2e}"
+        assert err.max() <= tol + kick
+    else:
+        _close(v, r["v"], vscale, "v after one step", rel=1e-5 + ulp_v / vscale)
     assert e.status() == 0
 
 

@@ -1,0 +1,114 @@
+"""Parity with the reference's own kernels (PBF.cu, MPM.cu built unmodified for sm_103a, run through the
+driver API by oracle/refrun.py) on the same inputs.
+
+PBF: one substep stopped after XSPHKernel, so no atomic-order sort intervenes; the engine and the oracle seed
+the self pair's pseudo-random gradient direction with the reference's chunk slots (GPE_PBF_PAIR_IDS), so
+every term matches. The reference works in chunk-local coordinates, the engine in scene coordinates, so
+positions differ by the rounding of that change of frame (a few ulp of the scene coordinate).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EPS32 = np.finfo(np.float32).eps
+
+
+def _pbf_case():
+    from gpe import scenes
+
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_pbf_block()
+    return p, pos, vel, boxes
+
+
+def _assert_close(a, b, atol, what):
+    err = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    bad = err > atol
+    assert not bad.any(), f"{what}: {bad.sum()} beyond tolerance, max err {err.max():.3e}"
+
+
+def _check_pbf(x_in, out_x, out_v, out_lam, ref_x, ref_v, ref_lam, who):
+    corr = np.abs(ref_x.astype(np.float64) - x_in).max()  # size of the position update
+    ulp = 8 * EPS32 * np.abs(ref_x).astype(np.float64)
+    _assert_close(out_x, ref_x, 1e-4 * corr + ulp, f"{who} x*")
+    _assert_close(out_v, ref_v, 1e-4 * np.abs(ref_v).max() + 2 * ulp, f"{who} v")
+    _assert_close(out_lam, ref_lam, 1e-4 * np.abs(ref_lam).max(), f"{who} lambda")
+
+
+def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok):
+    from oracle import refrun
+
+    p, pos, vel, boxes = _pbf_case()
+    ref = refrun.RefPBF((12, 6), 320)
+    _, slot = ref.seed(pos, vel, float(p.gravity[1]))
+    ref.substep(iters=p.iters, full=False)
+    rx, rv, rl = ref.read_seeded()
+    xs0 = pos + vel
+    xs0[:, 1] += p.gravity[1]
+
+    # engine, stage by stage through the C ABI
+    q = p.copy()
+    q.flags |= gpe_mod.PBF_PAIR_IDS
+    e = gpe_mod.Pbf(q, boxes, capacity=len(pos))
+    e.set_state(pos, vel)
+    e.set_field(gpe_mod.PBF_FIELD_ID, slot.astype(np.uint32))
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    for _ in range(p.iters):
+        e.stage(gpe_mod.PBF_STAGE_LAMBDA)
+        e.stage(gpe_mod.PBF_STAGE_DELTA_P)
+    e.stage(gpe_mod.PBF_STAGE_XSPH)
+    perm = e.field(gpe_mod.PBF_FIELD_PERM)
+    ex, ev, el = np.empty_like(pos), np.empty_like(pos), np.empty(len(pos), np.float32)
+    ex[perm] = e.field(gpe_mod.PBF_FIELD_PRED)
+    ev[perm] = e.field(gpe_mod.PBF_FIELD_VEL)
+    el[perm] = e.field(gpe_mod.PBF_FIELD_LAMBDA)
+    _check_pbf(xs0, ex, ev, el, rx, rv, rl, "engine")
+
+    # oracle
+    o = oracle.PbfOracle(p, boxes)
+    r = o.step(pos, vel, None, 1, pair_id=slot.astype(np.uint32))
+    operm = o.predict_sort(pos, vel)["perm"]
+    ox, ov, ol = np.empty_like(pos), np.empty_like(pos), np.empty(len(pos), np.float32)
+    ox[operm], ov[operm], ol[operm] = r["x"], r["v"], r["lam"]
+    _check_pbf(xs0, ox, ov, ol, rx, rv, rl, "oracle")
+
+
+def test_pbf_full_substeps_run(gpe_mod, cuda_ok):
+    """Several complete reference substeps (with migration and the atomic-order sort) keep every atom and
+    stay inside the box; the engine's steps from the same state keep the same atom count."""
+    import torch
+    from oracle import refrun
+
+    p, pos, vel, boxes = _pbf_case()
+    ref = refrun.RefPBF((12, 6), 320)
+    ref.seed(pos, vel, float(p.gravity[1]))
+    for _ in range(5):
+        ref.substep(iters=p.iters, full=True)
+    torch.cuda.synchronize()
+    assert int(ref.num_atoms.sum().item()) == len(pos)
+
+
+def test_mpm_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok):
+    from gpe import scenes
+    from oracle import refrun
+
+    p = scenes.reference_mpm_params()
+    x, v, Cm, F, J = scenes.reference_mpm_block()
+    ref = refrun.RefMPM(400 * 1000, (12, 6))
+    ref.seed(x, v, Cm, F, J)
+    ref.substep(0)
+    R = ref.read()
+    e = gpe_mod.Mpm(p, capacity=len(x))
+    e.set_state(x, v, Cm, F, J)
+    e.step(1)
+    E = e.get_state()
+    O = oracle.MpmOracle(p).step(x, v, Cm, F, J, None, 1)
+    names = ["x", "v", "C", "F", "J"]
+    for who, got in (("engine", E), ("oracle", O)):
+        for nm, a, b in zip(names, got, R):
+            b64 = np.asarray(b, np.float64)
+            tol = 1e-5 * np.abs(b64).max() + (8 * EPS32 * np.abs(b64) if nm == "x" else 0.0)
+            if nm in ("C",):
+                tol = 1e-4 * np.abs(b64).max()
+            _assert_close(a, b, tol, f"{who} MPM {nm}")
