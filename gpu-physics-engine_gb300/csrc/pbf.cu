@@ -47,6 +47,7 @@ struct PbfK {
     DomDev d0; // the scene when there is only one
 };
 
+
 namespace {
 
 constexpr int T_PART = 256; // threads per block for the per-particle kernels
@@ -91,6 +92,7 @@ __device__ __forceinline__ void for_neighbours(const DomDev& d, const PbfK& k, c
         for (uint32_t j = b; j < e; ++j) { f(j); }
     }
 }
+
 
 // integer mixer of the reference (hash, cuda-internal.cuh:19-27)
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
@@ -187,39 +189,60 @@ __global__ void __launch_bounds__(T_PART)
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     const float2 p       = xs[i];
-    float gx = 0.f, gy = 0.f, gsq = 0.f, rho = 0.f;
+    // The reference accumulates per pair sv = -cs m (h-r)^2 r/|r|, |sv|^2 / m and m W6 (PBF.cu:264-286).
+    // Constants are hoisted: sx, sy = sum (h-r)^2 r/|r|, s4 = sum (h-r)^4 (= |sv|^2 / (cs m)^2 since r/|r| is a
+    // unit vector), s6 = sum (h^2 - r^2)^3. The self pair (r = 0) is added after the loop: it contributes
+    // h^6 to the density and, in the reference, a gradient of length cs m h^2 along pairDirection(i, i).
+    float sx = 0.f, sy = 0.f, s4 = 0.f, s6 = 0.f;
+    bool self_seen = false; // the atom's own slot can fall outside the scanned cells after large moves
+    // Branch-free body: every lane of a warp runs the same instructions for every candidate and the terms of
+    // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
+    // make each warp execute both paths on almost every iteration.
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q = __ldg(&xs[j]);
+        const float2 q  = __ldg(&xs[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2 = rx * rx + ry * ry;
-        if (r2 > k.h2) { return; }
-        const float inv  = (r2 > 1e-12f) ? rsqrtf(r2) : 0.f;
-        const float dist = (inv > 0.f) ? inv * r2 : 0.f;
-        float nx, ny;
-        if (p.x != q.x || p.y != q.y) {
-            nx = rx * inv;
-            ny = ry * inv;
-        } else if (SELFG) {
-            // coincident pair (always the self pair): the reference seeds the direction with chunk slots
+        const float r2  = rx * rx + ry * ry;
+        const bool self = j == (uint32_t)i;
+        self_seen       = self_seen || self;
+        const bool in   = (r2 <= k.h2) && !self;
+        const bool dir  = in && (r2 > 1e-12f);
+        const float qq  = in ? k.h2 - r2 : 0.f;
+        s6              = fmaf(qq * qq, qq, s6);
+        const float inv = rsqrtf(dir ? r2 : 1.f);
+        const float dif = dir ? k.h - r2 * inv : 0.f;
+        const float d2  = dif * dif;
+        const float w   = d2 * inv;
+        sx              = fmaf(w, rx, sx);
+        sy              = fmaf(w, ry, sy);
+        s4              = fmaf(d2, d2, s4);
+        if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
+            // a distinct atom at the same position: the reference's pseudo-random pair direction
+            float nx, ny;
             if (pair_id) {
                 pair_direction(__ldg(&pair_id[i]), __ldg(&pair_id[j]), nx, ny);
             } else {
                 pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
             }
-        } else {
-            nx = 0.f;
-            ny = 0.f;
+            sx = fmaf(k.h2, nx, sx);
+            sy = fmaf(k.h2, ny, sy);
+            s4 = fmaf(k.h2, k.h2, s4);
         }
-        const float diff = k.h - dist;
-        const float sc   = -k.cs * diff * diff;
-        const float svx  = sc * nx * k.mass;
-        const float svy  = sc * ny * k.mass;
-        gx += svx;
-        gy += svy;
-        gsq += k.inv_mass * (svx * svx + svy * svy);
-        const float qq = k.h2 - r2;
-        rho += k.mass * (k.c6 * qq * qq * qq);
     });
+    if (self_seen) {
+        s6 = fmaf(k.h2 * k.h2, k.h2, s6);
+        if (SELFG) {
+            float nx, ny;
+            const uint32_t a = pair_id ? __ldg(&pair_id[i]) : (uint32_t)i - pbase;
+            pair_direction(a, a, nx, ny);
+            sx = fmaf(k.h2, nx, sx);
+            sy = fmaf(k.h2, ny, sy);
+            s4 = fmaf(k.h2, k.h2, s4);
+        }
+    }
+    const float csm  = k.cs * k.mass;
+    const float rho  = k.mass * k.c6 * s6;
+    const float gx = csm * sx, gy = csm * sy;
+    const float gsq  = k.inv_mass * (csm * csm) * s4;
     const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
     const float self = k.inv_mass * (gx * gx + gy * gy);
     const float grad = k.inv_rho0 * k.inv_rho0 * (self + gsq);
@@ -235,35 +258,34 @@ __global__ void __launch_bounds__(T_PART)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) { return; }
-    const DomDev d = load_dom<MULTI>(k, doms, dom, i);
-    const float2 p = xs[i];
-    const float li = lam[i];
-    float dx = 0.f, dy = 0.f;
+    const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
+    const float2 p  = xs[i];
+    const float mli = lam[i] * k.mass;
+    // dp = omega/(m rho0) sum (m lambda_i + m lambda_j - s_corr) * (-cs (h-r)^2 r/|r|) (PBF.cu:415-437); pairs
+    // closer than 1e-6 (the self pair included) have a zero direction there and are skipped here.
+    const float c6w = k.c6 * k.inv_w_dq;
+    float sx = 0.f, sy = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q = __ldg(&xs[j]);
-        const float lj = __ldg(&lam[j]);
+        const float2 q  = __ldg(&xs[j]);
+        const float lj  = __ldg(&lam[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2 = rx * rx + ry * ry;
-        if (r2 > k.h2) { return; }
-        const float inv = (r2 > 1e-12f) ? rsqrtf(r2) : 0.f;
-        const float nx = rx * inv, ny = ry * inv;
-        float scorr = 0.f;
+        const float r2  = rx * rx + ry * ry;
+        const bool ok   = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
+        const float inv = rsqrtf(ok ? r2 : 1.f);
+        float l         = fmaf(lj, k.mass, mli);
         if (SCORR) {
-            const float qq     = k.h2 - r2;
-            const float ratio  = k.c6 * qq * qq * qq * k.inv_w_dq;
-            const float ratio2 = ratio * ratio;
-            scorr              = k.scorr_k * ratio2 * ratio2;
+            const float qq    = k.h2 - r2;
+            const float ratio = c6w * (qq * qq * qq);
+            const float r2q   = ratio * ratio;
+            l                 = fmaf(-k.scorr_k, r2q * r2q, l);
         }
-        const float l    = li * k.mass + lj * k.mass - scorr;
-        const float dist = inv * r2;
-        const float diff = k.h - dist;
-        const float sc   = -k.cs * diff * diff;
-        dx += sc * nx * l;
-        dy += sc * ny * l;
+        const float diff = k.h - r2 * inv;
+        const float w    = ok ? diff * diff * inv * l : 0.f;
+        sx               = fmaf(w, rx, sx);
+        sy               = fmaf(w, ry, sy);
     });
-    dx *= k.dp_scale;
-    dy *= k.dp_scale;
-    float ox = p.x + dx, oy = p.y + dy;
+    const float s = -k.cs * k.dp_scale;
+    float ox = fmaf(s, sx, p.x), oy = fmaf(s, sy, p.y);
     // clamp<float>(v, lb, ub), PBF.cu:496-497
     oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
     ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
@@ -296,29 +318,32 @@ __global__ void __launch_bounds__(T_PART)
     const float2 p  = xs[i];
     const float2 po = x[i];
     const float vax = (p.x - po.x) * k.inv_dt, vay = (p.y - po.y) * k.inv_dt;
+    // dv = c sum (v_j - v_i) W6 (PBF.cu:602-615) with the poly6 coefficient hoisted; the self pair adds 0.
+    // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float dvx = 0.f, dvy = 0.f, w = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
         const float2 q  = __ldg(&xs[j]);
         const float2 qo = __ldg(&x[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2 = rx * rx + ry * ry;
-        if (r2 > k.h2) { return; }
-        const float vbx = (q.x - qo.x) * k.inv_dt, vby = (q.y - qo.y) * k.inv_dt;
-        const float qq  = k.h2 - r2;
-        const float p6  = k.c6 * qq * qq * qq;
-        dvx += (vbx - vax) * p6;
-        dvy += (vby - vay) * p6;
+        const float r2  = rx * rx + ry * ry;
+        const bool in   = r2 <= k.h2; // masked, branch-free (see k_lambda)
+        const float dx = (q.x - qo.x) * k.inv_dt - vax, dy = (q.y - qo.y) * k.inv_dt - vay;
+        const float qq  = in ? k.h2 - r2 : 0.f;
+        const float p6  = qq * qq * qq;
+        dvx             = fmaf(dx, p6, dvx);
+        dvy             = fmaf(dy, p6, dvy);
         if (VORT) {
-            if (r2 > 1e-12f) {
-                const float inv  = rsqrtf(r2);
-                const float diff = k.h - r2 * inv;
-                const float gm   = k.cs * diff * diff * inv; // grad_j W_ij = +cs (h-r)^2 r_ij/|r_ij|
-                w += (vbx - vax) * (gm * ry) - (vby - vay) * (gm * rx);
-            }
+            const bool dir   = in && (r2 > 1e-12f);
+            const float inv  = rsqrtf(dir ? r2 : 1.f);
+            const float diff = k.h - r2 * inv;
+            const float gm   = dir ? diff * diff * inv : 0.f;
+            w                = fmaf(gm, dx * ry - dy * rx, w);
         }
     });
-    float vx = vax + dvx * k.xsph_c;
-    float vy = vay + dvy * k.xsph_c;
+    w *= k.cs;
+    const float cx = k.xsph_c * k.c6;
+    float vx       = fmaf(dvx, cx, vax);
+    float vy       = fmaf(dvy, cx, vay);
     if (!VORT && (k.flags & GPE_PBF_VEL_CLAMP)) { velocity_clamp(k, vx, vy); }
     if (!(isfinite(vx) && isfinite(vy) && isfinite(p.x) && isfinite(p.y))) {
         atomicOr(status, GPE_STATUS_NONFINITE);
@@ -342,17 +367,20 @@ __global__ void __launch_bounds__(T_PART)
     const float aw = fabsf(wi);
     float ex = 0.f, ey = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q = __ldg(&xs[j]);
+        const float2 q   = __ldg(&xs[j]);
+        const float wj   = __ldg(&omega[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2 = rx * rx + ry * ry;
-        if (r2 > k.h2 || r2 <= 1e-12f) { return; }
-        const float inv  = rsqrtf(r2);
+        const float r2   = rx * rx + ry * ry;
+        const bool ok    = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
+        const float inv  = rsqrtf(ok ? r2 : 1.f);
         const float diff = k.h - r2 * inv;
-        const float gm   = -k.cs * diff * diff * inv; // grad_i W_ij
-        const float dw   = fabsf(__ldg(&omega[j])) - aw;
-        ex += dw * gm * rx;
-        ey += dw * gm * ry;
+        const float dwg  = ok ? (fabsf(wj) - aw) * (diff * diff * inv) : 0.f; // grad_i W = -cs (...)
+        ex               = fmaf(dwg, rx, ex);
+        ey               = fmaf(dwg, ry, ey);
     });
+    // only the direction of eta = grad|omega| is used, so the positive factor cs drops out; the sign stays
+    ex             = -ex;
+    ey             = -ey;
     float2 vv      = v[i];
     const float e2 = ex * ex + ey * ey;
     if (e2 > 1e-40f) {
@@ -376,15 +404,15 @@ __global__ void __launch_bounds__(T_PART)
     if (i < k.n) {
         const DomDev d = load_dom<MULTI>(k, doms, dom, i);
         const float2 p = xs[i];
-        float rho      = 0.f;
+        float s6       = 0.f;
         for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
             const float2 q = __ldg(&xs[j]);
             const float rx = p.x - q.x, ry = p.y - q.y;
             const float r2 = rx * rx + ry * ry;
-            if (r2 > k.h2) { return; }
-            const float qq = k.h2 - r2;
-            rho += k.mass * (k.c6 * qq * qq * qq);
+            const float qq = (r2 <= k.h2) ? k.h2 - r2 : 0.f;
+            s6             = fmaf(qq * qq, qq, s6);
         });
+        const float rho = k.mass * k.c6 * s6;
         rho_out[i] = rho;
         e          = fmaxf(rho * k.inv_rho0 - 1.f, 0.f);
     }
@@ -629,26 +657,47 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     return GPE_OK;
 }
 
+// Template dispatch tables: [multi scene][flag]
+using LamFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                       const float2*, float*, const uint32_t*);
+template <bool M, bool S>
+void lam_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid)
+{
+    k_lambda<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, pid);
+}
+const LamFn kLam[2][2] = {{lam_launch<false, false>, lam_launch<false, true>},
+                          {lam_launch<true, false>, lam_launch<true, true>}};
+
+using DpFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                      const float2*, const float*, float2*);
+template <bool M, bool S>
+void dp_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+               const uint32_t* start, const float2* xs, const float* lam, float2* out)
+{
+    k_delta_p<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, out);
+}
+const DpFn kDp[2][2] = {{dp_launch<false, false>, dp_launch<false, true>},
+                        {dp_launch<true, false>, dp_launch<true, true>}};
+
+using XsFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                      const float2*, const float2*, float2*, float*, uint32_t*);
+template <bool M, bool V>
+void xs_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+               const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status)
+{
+    k_xsph<M, V><<<g, T_PART, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+}
+const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
+                        {xs_launch<true, false>, xs_launch<true, true>}};
+
 int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
 {
     if (s->n == 0) { return GPE_OK; }
-    const bool sg    = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0;
-    const unsigned g = blocks_for(s->n);
+    const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
-    float2* xs       = s->pos[s->XS];
-    if (multi(s)) {
-        if (sg) {
-            k_lambda<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
-        } else {
-            k_lambda<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
-        }
-    } else {
-        if (sg) {
-            k_lambda<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
-        } else {
-            k_lambda<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, xs, s->lam, pid);
-        }
-    }
+    kLam[multi(s) ? 1 : 0][sg](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
+                               pid);
     GPE_CHECK_LAUNCH("k_lambda");
     s->launches += 1;
     return GPE_OK;
@@ -657,24 +706,9 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
 int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
 {
     if (s->n > 0) {
-        const bool sc    = s->prm.scorr_k != 0.f;
-        const unsigned g = blocks_for(s->n);
-        float2* in       = s->pos[s->XS];
-        float2* out      = s->pos[s->XO];
-        if (multi(s)) {
-            if (sc) {
-                k_delta_p<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
-            } else {
-                k_delta_p<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
-            }
-        } else {
-            if (sc) {
-                k_delta_p<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam, out);
-            } else {
-                k_delta_p<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, in, s->lam,
-                                                               out);
-            }
-        }
+        const int sc = s->prm.scorr_k != 0.f ? 1 : 0;
+        kDp[multi(s) ? 1 : 0][sc](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
+                                  s->pos[s->XO]);
         GPE_CHECK_LAUNCH("k_delta_p");
         s->launches += 1;
     }
@@ -685,25 +719,9 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
 int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 {
     if (s->n == 0) { return GPE_OK; }
-    const bool vort  = s->prm.vort_eps != 0.f;
-    const unsigned g = blocks_for(s->n);
-    if (multi(s)) {
-        if (vort) {
-            k_xsph<true, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                                     s->pos[s->XS], s->vel, s->omega, s->status);
-        } else {
-            k_xsph<true, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                                      s->pos[s->XS], s->vel, s->omega, s->status);
-        }
-    } else {
-        if (vort) {
-            k_xsph<false, true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                                      s->pos[s->XS], s->vel, s->omega, s->status);
-        } else {
-            k_xsph<false, false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                                       s->pos[s->XS], s->vel, s->omega, s->status);
-        }
-    }
+    const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
+    kXs[multi(s) ? 1 : 0][vort](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+                                s->pos[s->XS], s->vel, s->omega, s->status);
     GPE_CHECK_LAUNCH("k_xsph");
     s->launches += 1;
     return GPE_OK;
