@@ -58,9 +58,39 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
         _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"])
+    build_compat(cc, flags, force)
     if verbose:
         print(f"built {LIB}", file=sys.stderr)
     return LIB
+
+
+COMPAT = PKG / "compat"
+COMPAT_LIB = PKG / "libgpe_compat.so"
+EXAMPLES = ["pbf_headless", "mpm_headless"]
+
+
+def build_compat(cc: str, flags: list[str], force: bool = False) -> None:
+    """libgpe_compat.so (the reference's cuda-engine.h on top of libgpe.so) and the headless example drivers."""
+    headers = [COMPAT / "cuda-engine" / "cuda-engine.h", *sorted((COMPAT / "common").glob("*.h")),
+               PKG.parent / "include" / "gpe.h"]
+    inc = ["-I", str(COMPAT)]
+    rpath = ["-Xlinker", "-rpath", "-Xlinker", str(PKG)]
+    src = COMPAT / "cuda-engine.cu"
+    obj = BUILD / "compat_cuda_engine.o"
+    if force or _stale(obj, [src, *headers]):
+        _run([cc, *flags, *inc, "-c", str(src), "-o", str(obj)])
+    if force or _stale(COMPAT_LIB, [obj, LIB]):
+        _run([cc, *ARCH, "-shared", "-o", str(COMPAT_LIB), str(obj), "-L", str(PKG), "-lgpe", "-lcudart", *rpath])
+    (COMPAT / "bin").mkdir(exist_ok=True)
+    jobs = []
+    for ex in EXAMPLES:
+        s = COMPAT / "examples" / f"{ex}.cpp"
+        out = COMPAT / "bin" / ex
+        if force or _stale(out, [s, COMPAT_LIB, *headers]):
+            jobs.append([cc, "-std=c++17", "-O2", *inc, "-I", str(PKG.parent / "include"), str(s), "-o", str(out),
+                         "-L", str(PKG), "-lgpe_compat", "-lgpe", "-lcudart", *rpath])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
 
 
 if __name__ == "__main__":

@@ -1,8 +1,9 @@
-// Configuration constants for the headless build of the reference's own kernels (parity tests only).
-// The reference takes these from libs/common/include/common/constants.h; the names are fixed by its sources
-// and the values are its values, except that the scene size in chunks (GPE_REF_SCENE_X/Y), the migration
-// queue depth (GPE_REF_MAX_MIGRANTS) and the MPM particle capacity (GPE_REF_MPM_ATOMS) can be raised so that
-// one build can be seeded in bulk or scaled to a million atoms.
+// common/constants.h of the headless engine: the configuration constants that code written against the
+// reference's interface compiles with (the reference's libs/common/include/common/constants.h). The names
+// are fixed by that interface and the values are the reference's, except that the scene size in chunks
+// (GPE_REF_SCENE_X/Y), the migration queue depth (GPE_REF_MAX_MIGRANTS) and the MPM particle capacity
+// (GPE_REF_MPM_ATOMS) can be set with -D. The compat layer (cuda-engine.h) sizes its arenas and its output
+// views from them, and the parity tests compile the reference's own kernels against the same file.
 #pragma once
 #include <chrono>
 #include <stddef.h>

@@ -22,6 +22,7 @@
 #include <tuple>
 #include <vector>
 
+#include "emit.cuh"
 #include "gpe_internal.h"
 
 namespace gpe {
@@ -38,7 +39,8 @@ struct MpmK {
     float k_bulk, gamma, p_min, p_max, J_min, J_max;
     float mu0, la0, theta_c, theta_s, hardening;
     float apic_s; // 4 / dx^2
-    int32_t n;
+    int32_t n;            // particle count when n_dev is null
+    const int32_t* n_dev; // device-resident count (the reference's num_points[0], MPM.cu:64)
 };
 
 namespace {
@@ -47,6 +49,8 @@ constexpr int T_MPM     = 256;
 constexpr int TILE_CAP  = 2048; // nodes of the shared-memory accumulation tile (24 KB)
 
 enum MatMode { MODE_FLUID = 0, MODE_COROT = 1, MODE_SNOW = 2, MODE_MIXED = 3 };
+
+__device__ __forceinline__ int32_t count_of(const MpmK& k) { return k.n_dev ? __ldg(k.n_dev) : k.n; }
 
 struct Stencil {
     int32_t bx, by;
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(T_MPM)
           float4* __restrict__ grid, uint32_t* status)
 {
     const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < k.n;
+    const bool valid = i < count_of(k);
     Stencil s{};
     float2 vv = make_float2(0.f, 0.f);
     float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -405,7 +409,7 @@ __global__ void __launch_bounds__(T_MPM)
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (int64_t z = i; z < zero_nodes; z += stride) { zero_grid[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
     }
-    if (i >= k.n) { return; }
+    if (i >= count_of(k)) { return; }
     const int m        = mat_of(k, MODE, mat, i);
     const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
     PState ps;
@@ -432,7 +436,7 @@ __global__ void __launch_bounds__(T_MPM)
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (int64_t z = i; z < nn; z += stride) { grid_zero[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
     }
-    const bool valid   = i < k.n;
+    const bool valid   = i < count_of(k);
     const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
     Stencil s{};
     float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(T_MPM)
               uint32_t* status)
 {
     const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid   = i < k.n;
+    const bool valid   = i < count_of(k);
     const int32_t lane = threadIdx.x & 31;
     uint32_t key       = 0xffffffffu;
     if (valid) {
@@ -476,7 +480,8 @@ __global__ void __launch_bounds__(T_MPM)
 }
 
 __global__ void __launch_bounds__(T_MPM)
-    k_mpm_gather(int32_t n, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
+    k_mpm_gather(const int32_t* __restrict__ n_dev, const uint2* __restrict__ keyrank,
+                 const uint32_t* __restrict__ start,
                  const uint32_t* __restrict__ bucket, const float2* __restrict__ x0, const float2* __restrict__ v0,
                  const float4* __restrict__ C0, const float4* __restrict__ F0, const float* __restrict__ J0,
                  const int32_t* __restrict__ m0, const uint32_t* __restrict__ id0, float2* __restrict__ x1,
@@ -484,7 +489,7 @@ __global__ void __launch_bounds__(T_MPM)
                  int32_t* __restrict__ m1, uint32_t* __restrict__ id1)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) { return; }
+    if (i >= __ldg(n_dev)) { return; }
     const uint2 kr   = keyrank[i];
     const uint32_t s = __ldg(&start[kr.x]);
     const uint32_t e = __ldg(&start[kr.x + 1]);
@@ -531,6 +536,59 @@ __global__ void k_mpm_init(int32_t n, uint32_t* __restrict__ id, float2* __restr
     if (set_m) { mat[i] = material; }
 }
 
+__global__ void k_mpm_set_count(int32_t* __restrict__ c, int32_t n)
+{
+    c[0] = n;
+    c[1] = n;
+}
+
+// hose emitter (MPMEmitterKernel, MPM.cu:380-438): appends at the device count with C = 0, F = I, J = 1
+__global__ void k_mpm_emit(const HoseK h, float2* __restrict__ x, float2* __restrict__ v, float4* __restrict__ C,
+                           float4* __restrict__ F, float* __restrict__ J, int32_t* __restrict__ mat,
+                           uint32_t* __restrict__ id, int32_t material, int32_t* __restrict__ count, int32_t cap,
+                           uint32_t* __restrict__ status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= h.count) { return; }
+    const float2 p     = hose_position(h, i);
+    const int32_t slot = append_slot(count, true);
+    if (slot < 0) { return; }
+    if (slot >= cap) {
+        atomicOr(status, GPE_STATUS_CAPACITY);
+        atomicMin(count, cap);
+        return;
+    }
+    x[slot]   = p;
+    v[slot]   = make_float2(h.vx, h.vy);
+    C[slot]   = make_float4(0.f, 0.f, 0.f, 0.f);
+    F[slot]   = make_float4(1.f, 0.f, 0.f, 1.f);
+    J[slot]   = 1.f;
+    mat[slot] = material;
+    id[slot]  = (uint32_t)slot;
+}
+
+// publish (MPMOutputKernel, MPM.cu:302-322): consecutive blocks of chunk_capacity particles, bounded by the view
+__global__ void k_mpm_publish(const gpe_view vv, const gpe_view* __restrict__ vp, const float2* __restrict__ x,
+                              const float2* __restrict__ v, int32_t* __restrict__ count)
+{
+    const gpe_view view  = vp ? *vp : vv; // vp: the struct lives in device memory and is read at run time
+    const int32_t n      = count[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) { count[1] = n; } // num_points[1] = num_points[0], MPM.cu:317
+    const int32_t chunks = view.chunks_x * view.chunks_y;
+    const int64_t limit  = (int64_t)chunks * view.chunk_capacity;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < limit; i += stride) {
+        if (i < chunks) {
+            const int64_t left = (int64_t)n - i * view.chunk_capacity;
+            view.counts[i]     = (int32_t)(left < 0 ? 0 : (left > view.chunk_capacity ? view.chunk_capacity : left));
+        }
+        if (i < n) {
+            reinterpret_cast<float2*>(view.pos)[i] = x[i];
+            reinterpret_cast<float2*>(view.vel)[i] = v[i];
+        }
+    }
+}
+
 } // namespace
 } // namespace gpe
 
@@ -563,6 +621,8 @@ struct gpe_mpm {
     uint32_t* start  = nullptr;
     uint32_t* bsum   = nullptr;
     uint32_t* status = nullptr;
+    int32_t* d_count = nullptr; // device-resident particle count
+    bool dynamic     = false;   // GPE_MPM_FLAG_DYNAMIC_COUNT: launches cover the capacity
     int cur = 0;        // which particle buffer set is current
     int ga  = 0;        // grid holding the current step's nodes; ga+1, ga+2 (mod 3) are zero between steps
     bool grids_dirty = false;
@@ -637,6 +697,20 @@ int mode_of(const gpe_mpm* s)
 
 unsigned mblocks(int64_t n) { return (unsigned)((n + T_MPM - 1) / T_MPM); }
 
+// launch size: the capacity when emitters grow the device-resident count inside replayed graphs
+int64_t lsz(const gpe_mpm* s) { return s->dynamic ? s->cap : s->n; }
+
+int32_t mpm_sync_count(gpe_mpm* s, cudaStream_t st)
+{
+    if (!s->dynamic) { return GPE_OK; }
+    int32_t c = 0;
+    GPE_TRY_CUDA(cudaMemcpyAsync(&c, s->d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    s->n   = c;
+    s->k.n = c;
+    return GPE_OK;
+}
+
 unsigned grid_blocks(int64_t nn)
 {
     const int64_t want = (nn + T_MPM - 1) / T_MPM;
@@ -648,7 +722,7 @@ template <int MODE>
 int32_t launch_p2g_t(gpe_mpm* s, float4* grid, cudaStream_t st)
 {
     const int c = s->cur;
-    k_p2g<MODE><<<mblocks(s->n), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
+    k_p2g<MODE><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
                                                   grid, s->status);
     GPE_CHECK_LAUNCH("k_p2g");
     return GPE_OK;
@@ -656,7 +730,7 @@ int32_t launch_p2g_t(gpe_mpm* s, float4* grid, cudaStream_t st)
 
 int32_t launch_p2g(gpe_mpm* s, float4* grid, cudaStream_t st)
 {
-    if (s->n == 0) { return GPE_OK; }
+    if (lsz(s) == 0) { return GPE_OK; }
     s->launches += 1;
     switch (mode_of(s)) {
         case MODE_FLUID: return launch_p2g_t<MODE_FLUID>(s, grid, st);
@@ -670,7 +744,7 @@ template <int MODE, bool RAW>
 int32_t launch_g2p_t(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
 {
     const int c      = s->cur;
-    const unsigned g = std::max(mblocks(s->n), zero ? grid_blocks(s->nn) : 1u);
+    const unsigned g = std::max(mblocks(lsz(s)), zero ? grid_blocks(s->nn) : 1u);
     k_g2p<MODE, RAW><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
                                           zero, zero ? s->nn : 0, s->status);
     GPE_CHECK_LAUNCH("k_g2p");
@@ -680,7 +754,7 @@ int32_t launch_g2p_t(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t 
 template <bool RAW>
 int32_t launch_g2p(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
 {
-    if (s->n == 0 && !zero) { return GPE_OK; }
+    if (lsz(s) == 0 && !zero) { return GPE_OK; }
     s->launches += 1;
     switch (mode_of(s)) {
         case MODE_FLUID: return launch_g2p_t<MODE_FLUID, RAW>(s, grid, zero, st);
@@ -694,7 +768,7 @@ template <int MODE>
 int32_t launch_fused_t(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero, cudaStream_t st)
 {
     const int c      = s->cur;
-    const unsigned g = std::max(mblocks(s->n), grid_blocks(s->nn));
+    const unsigned g = std::max(mblocks(lsz(s)), grid_blocks(s->nn));
     k_g2p_p2g<MODE><<<g, T_MPM, 0, st>>>(s->k, gin, gout, gzero, s->nn, s->x[c], s->F[c], s->J[c], s->mat[c],
                                          s->status);
     GPE_CHECK_LAUNCH("k_g2p_p2g");
@@ -714,15 +788,15 @@ int32_t launch_fused(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero,
 
 int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
 {
-    if (s->n <= 1) { return GPE_OK; }
+    if (lsz(s) <= 1) { return GPE_OK; }
     const int c = s->cur, o = c ^ 1;
-    k_mpm_key<<<mblocks(s->n), T_MPM, 0, st>>>(s->k, s->x[c], s->keyrank, s->count, s->status);
+    k_mpm_key<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->keyrank, s->count, s->status);
     GPE_CHECK_LAUNCH("k_mpm_key");
     int32_t rc = launch_exclusive_scan(s->count, (uint32_t)s->nn, s->bsum, s->start, st);
     if (rc) { return rc; }
-    rc = launch_scatter(s->keyrank, s->n, s->start, s->bucket, st);
+    rc = launch_scatter(s->keyrank, lsz(s), s->start, s->bucket, st, s->d_count);
     if (rc) { return rc; }
-    k_mpm_gather<<<mblocks(s->n), T_MPM, 0, st>>>((int32_t)s->n, s->keyrank, s->start, s->bucket, s->x[c], s->v[c],
+    k_mpm_gather<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->d_count, s->keyrank, s->start, s->bucket, s->x[c], s->v[c],
                                                    s->C[c], s->F[c], s->J[c], s->mat[c], s->id[c], s->x[o],
                                                    s->v[o], s->C[o], s->F[o], s->J[o], s->mat[o], s->id[o]);
     GPE_CHECK_LAUNCH("k_mpm_gather");
@@ -741,7 +815,7 @@ int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
     rc    = launch_p2g(s, s->grid[a], st);
     for (int32_t t = 1; t < n_steps && rc == GPE_OK; ++t) {
         const int b = (a + 1) % 3, z = (a + 2) % 3;
-        if (s->n > 0) {
+        if (lsz(s) > 0) {
             rc = launch_fused(s, s->grid[a], s->grid[b], s->grid[z], st);
         } else {
             k_clear<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->grid[z], s->nn);
@@ -778,6 +852,7 @@ int32_t mpm_alloc(gpe_mpm* s)
     const size_t ost = c.take<uint32_t>(M + 1);
     const size_t obs = c.take<uint32_t>(scan_blocks((uint32_t)M) + 1);
     const size_t oss = c.take<uint32_t>(4);
+    const size_t ocnt = c.take<int32_t>(2);
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -797,6 +872,8 @@ int32_t mpm_alloc(gpe_mpm* s)
     s->start   = reinterpret_cast<uint32_t*>(b + ost);
     s->bsum    = reinterpret_cast<uint32_t*>(b + obs);
     s->status  = reinterpret_cast<uint32_t*>(b + oss);
+    s->d_count = reinterpret_cast<int32_t*>(b + ocnt);
+    s->k.n_dev = s->d_count;
     return GPE_OK;
 }
 
@@ -821,6 +898,7 @@ int32_t gpe_mpm_create(const gpe_mpm_params* params, int64_t capacity, gpe_mpm**
     s->device  = dev;
     s->prm     = *params;
     s->k       = mpm_make_k(*params);
+    s->dynamic = (params->flags & GPE_MPM_FLAG_DYNAMIC_COUNT) != 0;
     s->cap     = capacity;
     s->nn      = (int64_t)params->nx * params->ny;
     rc         = mpm_alloc(s);
@@ -856,6 +934,8 @@ int32_t gpe_mpm_set_params(gpe_mpm* s, const gpe_mpm_params* params)
     const int32_t n = s->k.n;
     s->k          = mpm_make_k(*params);
     s->k.n        = n;
+    s->k.n_dev    = s->d_count;
+    s->dynamic    = (params->flags & GPE_MPM_FLAG_DYNAMIC_COUNT) != 0;
     s->drop_graphs();
     return GPE_OK;
 }
@@ -896,7 +976,9 @@ int32_t gpe_mpm_set_state(gpe_mpm* s, const float* pos, const float* vel, const 
                                                   !vel, !C, !F, !J, !material, s->prm.material);
         GPE_CHECK_LAUNCH("k_mpm_init");
     }
-    if (s->n != n) { s->drop_graphs(); }
+    k_mpm_set_count<<<1, 1, 0, st>>>(s->d_count, (int32_t)n);
+    GPE_CHECK_LAUNCH("k_mpm_set_count");
+    if (s->n != n && !s->dynamic) { s->drop_graphs(); }
     s->n                = n;
     s->k.n              = (int32_t)n;
     s->have_state       = true;
@@ -910,12 +992,15 @@ int32_t gpe_mpm_get_state(gpe_mpm* s, float* pos, float* vel, float* C, float* F
                           void* stream)
 {
     gpe::clear_error();
-    if (!s || n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    const int32_t rc = mpm_sync_count(s, st);
+    if (rc) { return rc; }
+    if (n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_get_state: n must equal the particle count");
         return GPE_ERR_BAD_ARG;
     }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
-    cudaStream_t st = as_stream(stream);
     if (n > 0) {
         // particles are returned at their original indices
         const int c = s->cur, o = c ^ 1;
@@ -935,6 +1020,9 @@ int32_t gpe_mpm_get_state(gpe_mpm* s, float* pos, float* vel, float* C, float* F
 int32_t gpe_mpm_count(const gpe_mpm* s, int64_t* n)
 {
     if (!s || !n) { return GPE_ERR_BAD_ARG; }
+    // with a device-resident count the host copy is refreshed first (a cached value, hence the cast)
+    const int32_t rc = mpm_sync_count(const_cast<gpe_mpm*>(s), nullptr);
+    if (rc) { return rc; }
     *n = s->n;
     return GPE_OK;
 }
@@ -1042,6 +1130,86 @@ int32_t gpe_mpm_launches_per_step(const gpe_mpm* s, int32_t* launches)
     if (!s || !launches) { return GPE_ERR_BAD_ARG; }
     *launches = 1;
     return GPE_OK;
+}
+
+int32_t gpe_mpm_emit(gpe_mpm* s, const gpe_hose* hose, uint64_t seed, int32_t* requested, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !hose || !(hose->spacing > 0.f) || hose->steps_per_call < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->dynamic) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_emit: needs GPE_MPM_FLAG_DYNAMIC_COUNT");
+        return GPE_ERR_NOT_READY;
+    }
+    HoseK h{};
+    const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
+    if (requested) { *requested = cnt; }
+    cudaStream_t st = as_stream(stream);
+    if (cnt > 0) {
+        const int c = s->cur;
+        k_mpm_emit<<<mblocks(cnt), T_MPM, 0, st>>>(h, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c], s->id[c],
+                                                    s->prm.material, s->d_count, (int32_t)s->cap, s->status);
+        GPE_CHECK_LAUNCH("k_mpm_emit");
+    }
+    s->have_state = true;
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_publish(gpe_mpm* s, const gpe_view* view, int32_t view_mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !view || (view_mem != GPE_MEM_HOST && view_mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    if (view_mem == GPE_MEM_HOST && (!view->pos || !view->vel || !view->counts || view->chunks_x <= 0 ||
+                                     view->chunks_y <= 0 || view->chunk_capacity <= 0)) {
+        return GPE_ERR_BAD_ARG;
+    }
+    if (s->prm.sort_interval > 0) {
+        // publish order is the storage order; re-sorting would shuffle it between ticks
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_publish: needs sort_interval == 0");
+        return GPE_ERR_NOT_READY;
+    }
+    cudaStream_t st = as_stream(stream);
+    gpe_view vv{};
+    const gpe_view* vp = nullptr;
+    unsigned blocks    = (unsigned)gpe::sm_count() * 8;
+    if (view_mem == GPE_MEM_HOST) {
+        vv     = *view;
+        blocks = grid_blocks((int64_t)vv.chunks_x * vv.chunks_y * vv.chunk_capacity);
+    } else {
+        vp = view;
+    }
+    k_mpm_publish<<<blocks, T_MPM, 0, st>>>(vv, vp, s->x[s->cur], s->v[s->cur], s->d_count);
+    GPE_CHECK_LAUNCH("k_mpm_publish");
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_buffers(gpe_mpm* s, float** pos, float** vel, float** C, float** F, float** J, int32_t** count)
+{
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    const int c = s->cur;
+    if (pos) { *pos = reinterpret_cast<float*>(s->x[c]); }
+    if (vel) { *vel = reinterpret_cast<float*>(s->v[c]); }
+    if (C) { *C = reinterpret_cast<float*>(s->C[c]); }
+    if (F) { *F = reinterpret_cast<float*>(s->F[c]); }
+    if (J) { *J = s->J[c]; }
+    if (count) { *count = s->d_count; }
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_enqueue(gpe_mpm* s, int32_t n_steps, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    if (n_steps == 0) { return GPE_OK; }
+    // the recorded sequence starts from cleared grids and grid 0, whatever the previous sequence left
+    for (int q = 0; q < 3; ++q) { GPE_TRY_CUDA(cudaMemsetAsync(s->grid[q], 0, sizeof(float4) * (size_t)s->nn, st)); }
+    s->ga          = 2; // mpm_run scatters the first step into grid (ga + 1) % 3 == 0
+    s->grids_dirty = false;
+    const int32_t rc = mpm_run(s, n_steps, false, st);
+    s->ga            = 2;
+    s->grids_dirty   = true; // the next engine-owned step clears the grids again
+    return rc;
 }
 
 } // extern "C"

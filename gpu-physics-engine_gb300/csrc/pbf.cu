@@ -24,6 +24,7 @@
 #include <tuple>
 #include <vector>
 
+#include "emit.cuh"
 #include "gpe_internal.h"
 
 namespace gpe {
@@ -43,7 +44,9 @@ struct PbfK {
     float eps, scorr_k, dp_scale, c_min, xsph_c, vort_eps, v_max, v_min2, vort_dt;
     int32_t R;
     uint32_t flags;
-    int32_t n;
+    float margin;             // wall margin (positions stay below the box's upper edge by this much)
+    int32_t n;                // particle count when n_dev is null
+    const int32_t* n_dev;     // device-resident particle count (emitters append on the device)
     DomDev d0; // the scene when there is only one
 };
 
@@ -51,6 +54,10 @@ struct PbfK {
 namespace {
 
 constexpr int T_PART = 256; // threads per block for the per-particle kernels
+
+// particle count of a launch: the device counter when there is one (the reference keeps num_atoms on the
+// device too, cuda-engine.h:133), else the value passed by the host
+__device__ __forceinline__ int32_t count_of(const PbfK& k) { return k.n_dev ? __ldg(k.n_dev) : k.n; }
 
 __device__ __forceinline__ int32_t cell_coord(float pos, float org, float inv, int32_t nc)
 {
@@ -126,7 +133,7 @@ __global__ void __launch_bounds__(T_PART)
                    uint2* __restrict__ keyrank, uint32_t* __restrict__ count)
 {
     const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid   = i < k.n;
+    const bool valid   = i < count_of(k);
     const int32_t lane = threadIdx.x & 31;
     uint32_t key       = 0xffffffffu;
     float2 ps          = make_float2(0.f, 0.f);
@@ -156,13 +163,15 @@ __global__ void __launch_bounds__(T_PART)
 // The atomic ranks are unique but depend on warp scheduling; the stable slot of particle i is the number of
 // entries of its cell's bucket with a smaller pre-sort index.
 __global__ void __launch_bounds__(T_PART)
-    k_place(int32_t n, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
+    k_place(int32_t n_host, const int32_t* __restrict__ n_dev, const uint2* __restrict__ keyrank,
+            const uint32_t* __restrict__ start,
             const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
             const float2* __restrict__ xs_tmp, float2* __restrict__ x_out, float2* __restrict__ xs_out,
             uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
             uint32_t* __restrict__ id_out)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t n = n_dev ? __ldg(n_dev) : n_host;
     if (i >= n) { return; }
     const uint2 kr   = keyrank[i];
     const uint32_t s = __ldg(&start[kr.x]);
@@ -185,7 +194,7 @@ __global__ void __launch_bounds__(T_PART)
              const uint32_t* __restrict__ pair_id)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) { return; }
+    if (i >= count_of(k)) { return; }
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     const float2 p       = xs[i];
@@ -257,7 +266,7 @@ __global__ void __launch_bounds__(T_PART)
               float2* __restrict__ xs_out)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) { return; }
+    if (i >= count_of(k)) { return; }
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float2 p  = xs[i];
     const float mli = lam[i] * k.mass;
@@ -313,7 +322,7 @@ __global__ void __launch_bounds__(T_PART)
            float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) { return; }
+    if (i >= count_of(k)) { return; }
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float2 p  = xs[i];
     const float2 po = x[i];
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(T_PART)
                 const float* __restrict__ omega, float2* __restrict__ v)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) { return; }
+    if (i >= count_of(k)) { return; }
     const DomDev d = load_dom<MULTI>(k, doms, dom, i);
     const float2 p = xs[i];
     const float wi = omega[i];
@@ -401,7 +410,7 @@ __global__ void __launch_bounds__(T_PART)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float e         = 0.f;
-    if (i < k.n) {
+    if (i < count_of(k)) {
         const DomDev d = load_dom<MULTI>(k, doms, dom, i);
         const float2 p = xs[i];
         float s6       = 0.f;
@@ -446,6 +455,75 @@ __global__ void k_check_domains(const int32_t* __restrict__ dom, int32_t n, int3
     if (i >= n) { return; }
     const int32_t d = dom[i];
     if (d < 0 || d >= nd || (i + 1 < n && dom[i + 1] < d)) { atomicOr(status, GPE_STATUS_CAPACITY); }
+}
+
+__global__ void k_set_count(int32_t* __restrict__ c, int32_t n) { *c = n; }
+
+// ----- hose emitter (emitterKernel, PBF.cu:968-1032): appends at the device count -------------------------
+__global__ void k_pbf_emit(const PbfK k, const HoseK h, float2* __restrict__ x, float2* __restrict__ v,
+                           int32_t* __restrict__ count, int32_t cap, uint32_t* __restrict__ ids,
+                           uint32_t* __restrict__ status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= h.count) { return; }
+    float2 p = hose_position(h, i);
+    // atoms outside the scene are dropped (PBF.cu:1014-1016); the rest are kept inside the walls
+    const DomDev& d = k.d0;
+    const bool in   = p.x >= d.lox && p.y >= d.loy && p.x < d.hix + k.margin && p.y < d.hiy + k.margin;
+    p.x             = fminf(p.x, d.hix);
+    p.y             = fminf(p.y, d.hiy);
+    float vx = h.vx, vy = h.vy;
+    if (k.flags & GPE_PBF_VEL_CLAMP) {
+        // velocityClamp, as emitterKernel applies to the stream velocity (PBF.cu:990-991)
+        const float v2  = vx * vx + vy * vy;
+        const float inv = (v2 < k.v_min2 || v2 == 0.f) ? 0.f : rsqrtf(v2);
+        const float sp  = fminf(v2 * inv, k.v_max);
+        vx *= inv * sp;
+        vy *= inv * sp;
+    }
+    const int32_t slot = append_slot(count, in);
+    if (slot < 0) { return; }
+    if (slot >= cap) {
+        atomicOr(status, GPE_STATUS_CAPACITY);
+        atomicMin(count, cap);
+        return;
+    }
+    x[slot] = p;
+    v[slot] = make_float2(vx, vy);
+    if (ids) { ids[slot] = (uint32_t)slot; }
+}
+
+// ----- publish to a chunk-major view (PBFOutputKernel, PBF.cu:861-896) ------------------------------------
+// The target is `vv`, or the struct at `vp` in device memory when vp is set (read when the kernel runs).
+__global__ void k_view_zero(const gpe_view* __restrict__ vp)
+{
+    const gpe_view view = *vp;
+    const int32_t nc    = view.chunks_x * view.chunks_y;
+    for (int32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        view.counts[c] = 0;
+    }
+}
+
+__global__ void k_pbf_publish(const PbfK k, const gpe_view vv, const gpe_view* __restrict__ vp,
+                              const float2* __restrict__ x, const float2* __restrict__ v, uint32_t* __restrict__ status)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count_of(k)) { return; }
+    const gpe_view view = vp ? *vp : vv;
+    const float2 p   = x[i];
+    const float inv  = 1.f / view.chunk_dim;
+    const int32_t cx = min(max((int32_t)floorf((p.x - k.d0.ox) * inv), 0), view.chunks_x - 1);
+    const int32_t cy = min(max((int32_t)floorf((p.y - k.d0.oy) * inv), 0), view.chunks_y - 1);
+    const int32_t c  = cx + cy * view.chunks_x;
+    const int32_t s  = atomicAdd(&view.counts[c], 1);
+    if (s >= view.chunk_capacity) {
+        atomicOr(status, GPE_STATUS_CAPACITY);
+        atomicSub(&view.counts[c], 1);
+        return;
+    }
+    const size_t o                            = (size_t)c * (size_t)view.chunk_capacity + (size_t)s;
+    reinterpret_cast<float2*>(view.pos)[o] = p;
+    reinterpret_cast<float2*>(view.vel)[o] = v[i];
 }
 
 __global__ void k_iota(uint32_t* __restrict__ a, int32_t n)
@@ -498,6 +576,8 @@ struct gpe_pbf {
     uint32_t* ids[2]  = {};
     uint32_t* status  = nullptr;
     float* red        = nullptr;
+    int32_t* d_count  = nullptr; // device-resident particle count
+    bool dynamic      = false;   // GPE_PBF_DYNAMIC_COUNT: launches cover the capacity
 
     // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
     int X = 0, SX = -1, XS = -1, XO = -1;
@@ -570,6 +650,7 @@ PbfK make_k(const gpe_pbf_params& p)
     int32_t R        = (int32_t)std::ceil(p.h / cell - 1e-4f);
     k.R              = R < 1 ? 1 : R;
     k.flags          = p.flags;
+    k.margin         = p.wall_margin;
     return k;
 }
 
@@ -598,9 +679,25 @@ void build_domains(gpe_pbf* s)
         o.coff    = (uint32_t)off;
         off += (uint64_t)o.ncx * (uint64_t)o.ncy;
     }
-    s->ncells = (uint32_t)off;
-    s->k      = make_k(s->prm);
-    s->k.d0   = s->domdev[0];
+    s->ncells  = (uint32_t)off;
+    s->k       = make_k(s->prm);
+    s->k.d0    = s->domdev[0];
+    s->k.n_dev = s->d_count;
+}
+
+// Launch size: with a device-resident count that emitters can grow inside a captured graph, every launch
+// covers the capacity and the kernels read the live count; otherwise the host count.
+int64_t lsize(const gpe_pbf* s) { return s->dynamic ? s->cap : s->n; }
+
+// Refreshes the host copy of the particle count from the device (only needed with a dynamic count).
+int32_t sync_count(gpe_pbf* s, cudaStream_t st)
+{
+    if (!s->dynamic) { return GPE_OK; }
+    int32_t c = 0;
+    GPE_TRY_CUDA(cudaMemcpyAsync(&c, s->d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    s->n = c;
+    return GPE_OK;
 }
 
 uint64_t count_cells(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd)
@@ -619,7 +716,7 @@ unsigned blocks_for(int64_t n) { return (unsigned)((n + T_PART - 1) / T_PART); }
 
 int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 {
-    const int32_t n = (int32_t)s->n;
+    const int32_t n = (int32_t)lsize(s);
     // roles for this step: the three buffers other than X, in order
     int fr[3], c = 0;
     for (int b = 0; b < 4; ++b) {
@@ -628,7 +725,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     s->SX = fr[0];
     s->XS = fr[1];
     s->XO = fr[2];
-    s->k.n = n;
+    s->k.n = (int32_t)s->n;
     if (n > 0) {
         if (multi(s)) {
             k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X], s->vel,
@@ -641,11 +738,12 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     }
     int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st);
     if (rc) { return rc; }
-    rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st);
+    rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st, s->d_count);
     if (rc) { return rc; }
     if (n > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
-        k_place<<<blocks_for(n), T_PART, 0, st>>>(n, s->keyrank, s->start, s->bucket, s->pos[s->X], s->xs_tmp,
+        k_place<<<blocks_for(n), T_PART, 0, st>>>(n, s->d_count, s->keyrank, s->start, s->bucket, s->pos[s->X],
+                                                  s->xs_tmp,
                                                   s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
                                                   ids ? s->ids[s->id_cur] : nullptr,
                                                   ids ? s->ids[s->id_cur ^ 1] : nullptr);
@@ -693,10 +791,10 @@ const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
 
 int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
 {
-    if (s->n == 0) { return GPE_OK; }
+    if (lsize(s) == 0) { return GPE_OK; }
     const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
-    kLam[multi(s) ? 1 : 0][sg](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
+    kLam[multi(s) ? 1 : 0][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
                                pid);
     GPE_CHECK_LAUNCH("k_lambda");
     s->launches += 1;
@@ -705,9 +803,9 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
 
 int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
 {
-    if (s->n > 0) {
+    if (lsize(s) > 0) {
         const int sc = s->prm.scorr_k != 0.f ? 1 : 0;
-        kDp[multi(s) ? 1 : 0][sc](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
+        kDp[multi(s) ? 1 : 0][sc](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
                                   s->pos[s->XO]);
         GPE_CHECK_LAUNCH("k_delta_p");
         s->launches += 1;
@@ -718,9 +816,9 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
 
 int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 {
-    if (s->n == 0) { return GPE_OK; }
+    if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
-    kXs[multi(s) ? 1 : 0][vort](blocks_for(s->n), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+    kXs[multi(s) ? 1 : 0][vort](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
                                 s->pos[s->XS], s->vel, s->omega, s->status);
     GPE_CHECK_LAUNCH("k_xsph");
     s->launches += 1;
@@ -729,8 +827,8 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 
 int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 {
-    if (s->n == 0 || s->prm.vort_eps == 0.f) { return GPE_OK; }
-    const unsigned g = blocks_for(s->n);
+    if (lsize(s) == 0 || s->prm.vort_eps == 0.f) { return GPE_OK; }
+    const unsigned g = blocks_for(lsize(s));
     if (multi(s)) {
         k_vorticity<true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega, s->vel);
     } else {
@@ -787,6 +885,7 @@ int32_t alloc_buffers(gpe_pbf* s)
     const size_t o_id1   = c.take<uint32_t>(N);
     const size_t o_stat  = c.take<uint32_t>(4);
     const size_t o_red   = c.take<float>(8);
+    const size_t o_cnt1  = c.take<int32_t>(1);
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -809,6 +908,8 @@ int32_t alloc_buffers(gpe_pbf* s)
     s->ids[1]  = reinterpret_cast<uint32_t*>(b + o_id1);
     s->status  = reinterpret_cast<uint32_t*>(b + o_stat);
     s->red     = reinterpret_cast<float*>(b + o_red);
+    s->d_count = reinterpret_cast<int32_t*>(b + o_cnt1);
+    s->k.n_dev = s->d_count;
     GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
     return GPE_OK;
 }
@@ -855,6 +956,7 @@ int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, 
     s->prm     = *params;
     s->nd      = n_domains;
     s->doms.assign(domains, domains + n_domains);
+    s->dynamic = (params->flags & GPE_PBF_DYNAMIC_COUNT) != 0;
     s->cap = capacity;
     build_domains(s);
     rc = alloc_buffers(s);
@@ -888,7 +990,8 @@ int32_t gpe_pbf_set_params(gpe_pbf* s, const gpe_pbf_params* params)
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_params: the sort-cell size is fixed at creation");
         return GPE_ERR_BAD_ARG;
     }
-    s->prm = *params;
+    s->prm     = *params;
+    s->dynamic = (params->flags & GPE_PBF_DYNAMIC_COUNT) != 0;
     build_domains(s);
     GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
     s->drop_graphs();
@@ -958,7 +1061,9 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
         k_iota<<<blocks_for(n), T_PART, 0, st>>>(s->ids[0], (int32_t)n);
         GPE_CHECK_LAUNCH("k_iota");
     }
-    if (s->n != n) { s->drop_graphs(); }
+    k_set_count<<<1, 1, 0, st>>>(s->d_count, (int32_t)n);
+    GPE_CHECK_LAUNCH("k_set_count");
+    if (s->n != n && !s->dynamic) { s->drop_graphs(); }
     s->n          = n;
     s->have_state = true;
     s->have_sort  = false;
@@ -969,12 +1074,15 @@ int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id
                           void* stream)
 {
     gpe::clear_error();
-    if (!s || n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+    if (!s) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    int32_t rc      = sync_count(s, st);
+    if (rc) { return rc; }
+    if (n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_state: n must equal the particle count");
         return GPE_ERR_BAD_ARG;
     }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
-    cudaStream_t st = as_stream(stream);
     if (n > 0) {
         if (pos) { GPE_TRY_CUDA(cudaMemcpyAsync(pos, s->pos[s->X], sizeof(float2) * (size_t)n, kind_out(mem), st)); }
         if (vel) { GPE_TRY_CUDA(cudaMemcpyAsync(vel, s->vel, sizeof(float2) * (size_t)n, kind_out(mem), st)); }
@@ -996,6 +1104,9 @@ int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id
 int32_t gpe_pbf_count(const gpe_pbf* s, int64_t* n)
 {
     if (!s || !n) { return GPE_ERR_BAD_ARG; }
+    // with a device-resident count the host copy is refreshed first (a cached value, hence the cast)
+    const int32_t rc = sync_count(const_cast<gpe_pbf*>(s), nullptr);
+    if (rc) { return rc; }
     *n = s->n;
     return GPE_OK;
 }
@@ -1095,10 +1206,10 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
             if (s->n > 0) {
                 s->k.n = (int32_t)s->n;
                 if (multi(s)) {
-                    k_density<true><<<blocks_for(s->n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                    k_density<true><<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
                                                                          s->pos[s->X], s->rho, s->red);
                 } else {
-                    k_density<false><<<blocks_for(s->n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                    k_density<false><<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
                                                                           s->pos[s->X], s->rho, s->red);
                 }
                 GPE_CHECK_LAUNCH("k_density");
@@ -1116,6 +1227,8 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
 int32_t gpe_pbf_density_error(gpe_pbf* s, float* max_err, float* mean_err, void* stream)
 {
     if (!s || !max_err || !mean_err) { return GPE_ERR_BAD_ARG; }
+    const int32_t rcn = sync_count(s, as_stream(stream));
+    if (rcn) { return rcn; }
     int32_t rc = gpe_pbf_stage(s, GPE_PBF_STAGE_DENSITY, stream);
     if (rc) { return rc; }
     float red[8];
@@ -1156,6 +1269,8 @@ int32_t gpe_pbf_get_field(gpe_pbf* s, int32_t field, void* dst, int64_t n_elems,
 {
     gpe::clear_error();
     if (!s || !dst || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    const int32_t rcn = sync_count(s, as_stream(stream));
+    if (rcn) { return rcn; }
     void* p;
     size_t es;
     int64_t cnt;
@@ -1213,6 +1328,87 @@ int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
 }
 
 } // extern "C"
+
+
+extern "C" int32_t gpe_pbf_emit(gpe_pbf* s, const gpe_hose* hose, uint64_t seed, int32_t* requested, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !hose || !(hose->spacing > 0.f) || hose->steps_per_call < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->dynamic || s->nd != 1) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_emit: needs GPE_PBF_DYNAMIC_COUNT and a single scene");
+        return GPE_ERR_NOT_READY;
+    }
+    if (s->SX >= 0) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_emit: a step is in progress (stage API)");
+        return GPE_ERR_NOT_READY;
+    }
+    HoseK h{};
+    const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
+    if (requested) { *requested = cnt; }
+    cudaStream_t st = as_stream(stream);
+    if (cnt > 0) {
+        const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
+        k_pbf_emit<<<blocks_for(cnt), T_PART, 0, st>>>(s->k, h, s->pos[s->X], s->vel, s->d_count, (int32_t)s->cap,
+                                                       ids ? s->ids[s->id_cur] : nullptr, s->status);
+        GPE_CHECK_LAUNCH("k_pbf_emit");
+    }
+    s->have_state = true;
+    return GPE_OK;
+}
+
+extern "C" int32_t gpe_pbf_publish(gpe_pbf* s, const gpe_view* view, int32_t view_mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !view || (view_mem != GPE_MEM_HOST && view_mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    if (view_mem == GPE_MEM_HOST && (!view->pos || !view->vel || !view->counts || view->chunks_x <= 0 ||
+                                     view->chunks_y <= 0 || !(view->chunk_dim > 0.f) || view->chunk_capacity <= 0)) {
+        return GPE_ERR_BAD_ARG;
+    }
+    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st = as_stream(stream);
+    const gpe_view* vp = nullptr;
+    gpe_view vv{};
+    if (view_mem == GPE_MEM_HOST) {
+        vv = *view;
+        GPE_TRY_CUDA(cudaMemsetAsync(vv.counts, 0, sizeof(int32_t) * (size_t)vv.chunks_x * vv.chunks_y, st));
+    } else {
+        vp = view;
+        k_view_zero<<<(unsigned)sm_count(), T_PART, 0, st>>>(vp);
+        GPE_CHECK_LAUNCH("k_view_zero");
+    }
+    if (lsize(s) > 0) {
+        k_pbf_publish<<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, vv, vp, s->pos[s->X], s->vel, s->status);
+        GPE_CHECK_LAUNCH("k_pbf_publish");
+    }
+    return GPE_OK;
+}
+
+extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
+{
+    gpe::clear_error();
+    if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    cudaStream_t st   = as_stream(stream);
+    const int X0      = s->X;
+    const int id0     = s->id_cur;
+    int32_t rc        = GPE_OK;
+    for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, st); }
+    if (rc) { return rc; }
+    // return the buffer roles to where they started, so the recorded sequence can be replayed
+    const size_t n = (size_t)lsize(s);
+    if (s->X != X0 && n > 0) {
+        GPE_TRY_CUDA(cudaMemcpyAsync(s->pos[X0], s->pos[s->X], sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    if (s->id_cur != id0 && n > 0) {
+        GPE_TRY_CUDA(cudaMemcpyAsync(s->ids[id0], s->ids[s->id_cur], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
+                                     st));
+    }
+    s->X         = X0;
+    s->id_cur    = id0;
+    s->have_sort = true;
+    return GPE_OK;
+}
 
 // =====================================================================================================
 // Allocation-free predict + sort (gpe_pbf_predict_sort_noalloc)
@@ -1343,7 +1539,7 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     if (n > 0) {
         rc = launch_scatter(keyrank, n, cell_start, bucket, st);
         if (rc) { return rc; }
-        k_place<<<blocks_for(n), T_PART, 0, st>>>((int32_t)n, keyrank, cell_start, bucket,
+        k_place<<<blocks_for(n), T_PART, 0, st>>>((int32_t)n, nullptr, keyrank, cell_start, bucket,
                                                   reinterpret_cast<const float2*>(pos), xs_tmp,
                                                   reinterpret_cast<float2*>(pos_sorted),
                                                   reinterpret_cast<float2*>(pred_sorted), perm, key_sorted, nullptr,

@@ -119,10 +119,11 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = bsum[blockIdx.x] + total; }
 }
 
-__global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n, const uint32_t* __restrict__ start,
-                          uint32_t* __restrict__ bucket)
+__global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n_host, const int32_t* __restrict__ n_dev,
+                          const uint32_t* __restrict__ start, uint32_t* __restrict__ bucket)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = n_dev ? (int64_t)__ldg(n_dev) : n_host;
     if (i >= n) { return; }
     const uint2 kr                  = keyrank[i];
     bucket[__ldg(&start[kr.x]) + kr.y] = (uint32_t)i;
@@ -146,11 +147,12 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
     return GPE_OK;
 }
 
-int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, cudaStream_t st)
+int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, cudaStream_t st,
+                       const int32_t* n_dev)
 {
     if (n <= 0) { return GPE_OK; }
     const int T = 256;
-    k_scatter<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(keyrank, n, start, bucket);
+    k_scatter<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(keyrank, n, n_dev, start, bucket);
     GPE_CHECK_LAUNCH("k_scatter");
     return GPE_OK;
 }

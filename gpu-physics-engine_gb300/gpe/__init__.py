@@ -19,7 +19,7 @@ OK, ERR_CUDA, ERR_DEVICE, ERR_NOT_READY, ERR_BAD_ARG, ERR_ALREADY, ERR_CAPACITY,
 MEM_HOST, MEM_DEVICE = 0, 1
 STATUS_NONFINITE, STATUS_CAPACITY, STATUS_CELL_OVERFLOW, STATUS_TIMEOUT = 1, 2, 4, 8
 
-PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS = 0x1, 0x2, 0x4, 0x8
+PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS, PBF_DYNAMIC_COUNT = 0x1, 0x2, 0x4, 0x8, 0x10
 (PBF_STAGE_PREDICT_SORT, PBF_STAGE_LAMBDA, PBF_STAGE_DELTA_P, PBF_STAGE_XSPH, PBF_STAGE_VORTICITY,
  PBF_STAGE_FINISH, PBF_STAGE_DENSITY) = range(7)
 (PBF_FIELD_POS, PBF_FIELD_VEL, PBF_FIELD_PRED, PBF_FIELD_LAMBDA, PBF_FIELD_KEY, PBF_FIELD_PERM,
@@ -27,7 +27,7 @@ PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS = 0x1, 0x2, 0x4, 0x8
 
 MPM_MAT_FLUID, MPM_MAT_COROTATED, MPM_MAT_SNOW = 0, 1, 2
 MPM_BC_SLIP, MPM_BC_STICKY = 0, 1
-MPM_FLAG_PER_PARTICLE_MATERIAL, MPM_FLAG_FLUID_F = 0x1, 0x2
+MPM_FLAG_PER_PARTICLE_MATERIAL, MPM_FLAG_FLUID_F, MPM_FLAG_DYNAMIC_COUNT = 0x1, 0x2, 0x4
 MPM_STAGE_CLEAR, MPM_STAGE_P2G, MPM_STAGE_GRID, MPM_STAGE_G2P, MPM_STAGE_SORT = range(5)
 
 
@@ -63,6 +63,24 @@ class MpmParams(C.Structure):
         o = MpmParams()
         C.pointer(o)[0] = self
         return o
+
+
+class Hose(C.Structure):
+    _fields_ = [("origin", C.c_float * 2), ("velocity", C.c_float * 2), ("nozzle_width", C.c_float),
+                ("spacing", C.c_float), ("jitter", C.c_float), ("steps_per_call", C.c_int32)]
+
+
+class View(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("counts", C.c_void_p), ("chunks_x", C.c_int32),
+                ("chunks_y", C.c_int32), ("chunk_dim", C.c_float), ("chunk_capacity", C.c_int32)]
+
+
+def make_hose(origin, velocity, nozzle_width, spacing, jitter=0.0, steps_per_call=1) -> Hose:
+    h = Hose()
+    h.origin[0], h.origin[1] = origin
+    h.velocity[0], h.velocity[1] = velocity
+    h.nozzle_width, h.spacing, h.jitter, h.steps_per_call = nozzle_width, spacing, jitter, steps_per_call
+    return h
 
 
 def make_domains(boxes) -> "C.Array":
@@ -124,6 +142,14 @@ def lib() -> C.CDLL:
             "gpe_mpm_get_grid": [vp, vp, i64, i32, vp],
             "gpe_mpm_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_mpm_launches_per_step": [vp, C.POINTER(i32)],
+            "gpe_pbf_emit": [vp, C.POINTER(Hose), C.c_uint64, C.POINTER(i32), vp],
+            "gpe_pbf_publish": [vp, vp, i32, vp],
+            "gpe_pbf_enqueue": [vp, i32, vp],
+            "gpe_mpm_emit": [vp, C.POINTER(Hose), C.c_uint64, C.POINTER(i32), vp],
+            "gpe_mpm_publish": [vp, vp, i32, vp],
+            "gpe_mpm_enqueue": [vp, i32, vp],
+            "gpe_mpm_buffers": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                                C.POINTER(vp)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -278,6 +304,18 @@ class Pbf:
         check(lib().gpe_pbf_launches_per_step(self.h, C.byref(v)), "gpe_pbf_launches_per_step")
         return v.value
 
+    def emit(self, hose: Hose, seed: int = 0, stream=None) -> int:
+        req = C.c_int32()
+        check(lib().gpe_pbf_emit(self.h, C.byref(hose), int(seed), C.byref(req), stream), "gpe_pbf_emit")
+        return req.value
+
+    def publish(self, view: View, view_mem: int = MEM_HOST, stream=None) -> None:
+        ptr = C.addressof(view) if view_mem == MEM_HOST else int(view)
+        check(lib().gpe_pbf_publish(self.h, ptr, view_mem, stream), "gpe_pbf_publish")
+
+    def enqueue(self, n_steps: int, stream=None) -> None:
+        check(lib().gpe_pbf_enqueue(self.h, int(n_steps), stream), "gpe_pbf_enqueue")
+
 
 # ----- MPM ----------------------------------------------------------------------------------------------
 class Mpm:
@@ -355,3 +393,20 @@ class Mpm:
         v = C.c_uint32()
         check(lib().gpe_mpm_status(self.h, C.byref(v), stream), "gpe_mpm_status")
         return v.value
+
+    def emit(self, hose: Hose, seed: int = 0, stream=None) -> int:
+        req = C.c_int32()
+        check(lib().gpe_mpm_emit(self.h, C.byref(hose), int(seed), C.byref(req), stream), "gpe_mpm_emit")
+        return req.value
+
+    def publish(self, view: View, view_mem: int = MEM_HOST, stream=None) -> None:
+        ptr = C.addressof(view) if view_mem == MEM_HOST else int(view)
+        check(lib().gpe_mpm_publish(self.h, ptr, view_mem, stream), "gpe_mpm_publish")
+
+    def enqueue(self, n_steps: int, stream=None) -> None:
+        check(lib().gpe_mpm_enqueue(self.h, int(n_steps), stream), "gpe_mpm_enqueue")
+
+    def buffers(self) -> dict:
+        ptrs = [C.c_void_p() for _ in range(6)]
+        check(lib().gpe_mpm_buffers(self.h, *[C.byref(p) for p in ptrs]), "gpe_mpm_buffers")
+        return dict(zip(["pos", "vel", "C", "F", "J", "count"], [p.value for p in ptrs]))

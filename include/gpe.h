@@ -61,6 +61,10 @@ int32_t gpe_version(void);                /* major*10000 + minor*100 + patch    
                                      the atom itself; coincident pairs take pairDirection, PBF.cu:309-321) */
 #define GPE_PBF_VEL_CLAMP 0x2u    /* clamp |v| to [v_min, v_max] after XSPH (velocityClamp, PBF.cu:629-638) */
 #define GPE_PBF_TRACK_IDS 0x4u    /* carry a particle id through every sort (for external bookkeeping)      */
+#define GPE_PBF_DYNAMIC_COUNT 0x10u /* keep the particle count on the device: launches cover the capacity and
+                                       read the live count, so emitters (gpe_pbf_emit) can add particles
+                                       between steps of a replayed graph, as the reference's hosePipe does
+                                       through its migration queues (PBF.cu:1021-1030); one scene only       */
 #define GPE_PBF_PAIR_IDS 0x8u     /* seed pairDirection with the tracked particle ids instead of the sorted
                                      index within the scene (the reference seeds it with the atom's slot in
                                      its chunk, PBF.cu:277); implies GPE_PBF_TRACK_IDS                       */
@@ -148,6 +152,46 @@ int32_t gpe_pbf_status(gpe_pbf* pbf, uint32_t* status, void* stream);
 /* Number of kernel launches the last gpe_pbf_step issued per step. */
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* pbf, int32_t* launches);
 
+/* A "hose pipe" source (hosePipe, PBF.cu:1033-1065 and MPM.cu:439-473): rows of particles on a square lattice
+ * behind a nozzle, moving with `velocity`, optionally jittered by a Gaussian of standard deviation `jitter`
+ * drawn with curand's Philox generator seeded by (seed, particle index) as the reference does. Emits
+ * width x rows particles with width = max(1, round(nozzle_width / spacing)) and
+ * rows = max(1, round(|velocity| * dt * steps_per_call / spacing)). */
+typedef struct gpe_hose {
+    float origin[2];        /* nozzle centre                                                     */
+    float velocity[2];      /* particle velocity in the engine's units                           */
+    float nozzle_width;     /* width of the stream                                               */
+    float spacing;          /* lattice spacing of the emitted particles                          */
+    float jitter;           /* standard deviation of the position jitter; 0 = none               */
+    int32_t steps_per_call; /* solver steps between calls (the reference's tick = 20 substeps)  */
+} gpe_hose;
+
+/* Output target for publishing a step's particles to a renderer (the reference's View, cuda-engine.h:51-57):
+ * chunk-major arrays of chunks_x * chunks_y chunks with chunk_capacity slots each; counts receives the
+ * number of particles written per chunk. All pointers are device pointers. */
+typedef struct gpe_view {
+    float* pos;             /* float2[chunks * chunk_capacity], positions in scene coordinates   */
+    float* vel;             /* float2[chunks * chunk_capacity]                                   */
+    int32_t* counts;        /* int32[chunks]                                                     */
+    int32_t chunks_x, chunks_y;
+    float chunk_dim;        /* chunk edge (kChunkDim, constants.h:48)                            */
+    int32_t chunk_capacity; /* slots per chunk (kMaxAtoms, constants.h:50)                       */
+} gpe_view;
+
+/* Appends the hose's particles (needs GPE_PBF_DYNAMIC_COUNT). Particles outside the scene are dropped, as
+ * in emitterKernel (PBF.cu:1014-1016); beyond the capacity they are dropped and GPE_STATUS_CAPACITY is set.
+ * *requested receives width x rows (the reference's return value). */
+int32_t gpe_pbf_emit(gpe_pbf* pbf, const gpe_hose* hose, uint64_t seed, int32_t* requested, void* stream);
+/* Writes every particle into the chunk of its position (PBFOutputKernel, PBF.cu:861-896). view_mem says
+ * where the gpe_view struct itself lives: GPE_MEM_HOST (read now) or GPE_MEM_DEVICE (read by the kernels
+ * when they run, so a captured graph follows later updates of the struct, as the reference's __constant__
+ * c_output does, PBF.cu:29 and TickStaging::outputTargetUpload, PBF.cu:50-55). */
+int32_t gpe_pbf_publish(gpe_pbf* pbf, const gpe_view* view, int32_t view_mem, void* stream);
+/* Issues n_steps steps on the stream without an engine-owned graph, so that they can be recorded into the
+ * caller's own stream capture (the reference's instantiatePBFGraph builds one graph per tick, PBF.cu:901-961).
+ * Buffer roles are returned to their starting state at the end, so a captured sequence can be replayed. */
+int32_t gpe_pbf_enqueue(gpe_pbf* pbf, int32_t n_steps, void* stream);
+
 /* Allocation-free predict + cell sort for one scene. It has no counterpart in the reference (whose arenas
  * are all allocated up front, cuda-engine.cpp:102-139); it exists for callers that cannot call cudaMalloc,
  * such as a host whose device memory is owned by another framework, or a real-time loop that must not
@@ -180,6 +224,9 @@ int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, const gpe_dom
 #define GPE_MPM_BC_STICKY 1      /* zero the whole node velocity inside the wall band                      */
 
 #define GPE_MPM_FLAG_PER_PARTICLE_MATERIAL 0x1u /* read a material id per particle instead of params.material */
+#define GPE_MPM_FLAG_DYNAMIC_COUNT 0x4u /* keep the particle count on the device (the reference's num_points,
+                                           cuda-engine.h:206-208) so gpe_mpm_emit can add particles between
+                                           steps of a replayed graph; launches cover the capacity        */
 #define GPE_MPM_FLAG_FLUID_F 0x2u /* keep updating F for fluid particles, as the reference does although nothing
                                      reads it (MPM.cu:258-263, cuda-engine.h:203); off saves 32 B/particle */
 
@@ -232,6 +279,21 @@ int32_t gpe_mpm_stage(gpe_mpm* mpm, int32_t stage, void* stream);
 int32_t gpe_mpm_get_grid(gpe_mpm* mpm, float* dst, int64_t n_nodes, int32_t mem, void* stream);
 int32_t gpe_mpm_status(gpe_mpm* mpm, uint32_t* status, void* stream);
 int32_t gpe_mpm_launches_per_step(const gpe_mpm* mpm, int32_t* launches);
+/* Appends the hose's particles at the live count (MPMEmitterKernel, MPM.cu:380-438): C = 0, F = I, J = 1
+ * and the engine's material; needs GPE_MPM_FLAG_DYNAMIC_COUNT. *requested receives width x rows. */
+int32_t gpe_mpm_emit(gpe_mpm* mpm, const gpe_hose* hose, uint64_t seed, int32_t* requested, void* stream);
+/* Copies the particles into the view in blocks of chunk_capacity consecutive particles (MPMOutputKernel,
+ * MPM.cu:302-322); writes stop at the view's capacity, which the reference's kernel can overrun. view_mem as
+ * for gpe_pbf_publish. */
+int32_t gpe_mpm_publish(gpe_mpm* mpm, const gpe_view* view, int32_t view_mem, void* stream);
+/* Issues n_steps steps on the stream without an engine-owned graph (see gpe_pbf_enqueue); the sequence
+ * starts by clearing the node grids so that a captured sequence can be replayed. No spatial re-sort runs. */
+int32_t gpe_mpm_enqueue(gpe_mpm* mpm, int32_t n_steps, void* stream);
+/* Device pointers of the particle arrays in storage order (valid while sort_interval == 0, since a re-sort
+ * moves the particles to the other buffer set) and of the device count: count[0] is the live count,
+ * count[1] the count at the last publish (the reference's num_points, cuda-engine.h:206-208). Any pointer
+ * argument may be NULL. */
+int32_t gpe_mpm_buffers(gpe_mpm* mpm, float** pos, float** vel, float** C, float** F, float** J, int32_t** count);
 
 #ifdef __cplusplus
 }

@@ -3,8 +3,9 @@ and the reference-CUDA timing leg, never part of the engine.
 
 libs/cuda-engine/source/PBF.cu and MPM.cu are compiled unmodified from /root/reference into device-only
 cubins under oracle/_ref/ (git-ignored; the cubins travel to the GPU machine, where the reference sources do not
-exist). Two stand-in headers in oracle/shim/common replace the reference's MSVC-only macros.h and its
-umbrella.h, and supply its constants.h values with the scene size and capacities overridable by -D.
+exist). The engine's headless common/ headers (gpu-physics-engine_gb300/compat/common) replace the
+reference's MSVC-only macros.h and its umbrella.h and supply its constants.h values, with the scene size and
+capacities overridable by -D.
 Where the sources are absent (the GPU machine), prebuilt cubins are used as they are.
 """
 from __future__ import annotations
@@ -39,14 +40,22 @@ def build(force: bool = False) -> list[Path]:
     outs = [OUT / f"{stem}.cubin" for stem, _, _ in VARIANTS]
     if not SRC.exists():
         return [o for o in outs if o.exists()]
-    shim = sorted((HERE / "shim" / "common").glob("*.h"))
+    # an include root holding only common/ (the package's compat/ also holds a cuda-engine/cuda-engine.h
+    # that must not shadow the reference's own)
+    shim = sorted((HERE.parent / "gpu-physics-engine_gb300" / "compat" / "common").glob("*.h"))
+    common = OUT / "inc"
+    (common / "common").mkdir(parents=True, exist_ok=True)
+    for h in shim:
+        dst = common / "common" / h.name
+        if not dst.exists() or dst.read_bytes() != h.read_bytes():
+            shutil.copyfile(h, dst)
     jobs = []
     for (stem, src, defs), out in zip(VARIANTS, outs):
         deps = [SRC / src, *shim]
         if not force and out.exists() and all(d.stat().st_mtime <= out.stat().st_mtime for d in deps):
             continue
         cmd = [_nvcc(), "-cubin", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
-               "-diag-suppress", "177", "-I", str(HERE / "shim"), "-I", str(INC),
+               "-diag-suppress", "177", "-I", str(common), "-I", str(INC),
                *[f"-D{k}={v}" for k, v in defs.items()], "-o", str(out), str(SRC / src)]
         jobs.append(cmd)
 
