@@ -2,9 +2,13 @@
 
 A step is one PBF solver step (the reference's substep: predict + sort, 4 x (lambda, delta p), velocity +
 XSPH) over the 1M-particle scene (a 960 x 1024 lattice block plus a 65,536-particle splash, 20.48 x 20.48
-domain, h = 0.02, dt = 1/120). Inputs are resident in HBM when the timed region starts; L2 is flushed (a
-256 MiB memset) before every timed step, since the working set (~60 MB) would otherwise stay in the 129 MB
-L2 across steps.
+domain, h = 0.02, dt = 1/2000: the 10 m deep block needs an effective sound speed K dx / dt well above
+sqrt(g H), and the plain 4-iteration form diverges at 1/240 and above). Inputs are resident in HBM when the
+timed region starts; L2 is flushed (a 256 MiB memset) before every timed step, since the working set
+(~60 MB) would otherwise stay in the 129 MB L2 across steps.
+
+learned: the network-warm-started 2-iteration step against the plain forms on the same scene (its network
+       trained on the GPU first, untimed), with the density error each reaches.
 
 value: particle-steps/s through the graph-launched step (gpe_pbf_step), CUDA events on the launch stream.
 e2e:   the same metric through the C ABI with host buffers: per step set_state from pinned host memory,
@@ -128,16 +132,76 @@ def allmax(x: float, ws: int) -> float:
     return float(t.item())
 
 
-def workload():
+DT = 1.0 / 2000.0  # the step at which the plain 4-iteration solver is stable on this 10 m deep scene
+
+
+def workload(iters: int = 4):
     from gpe import scenes
 
-    p = scenes.dam_params(iters=4)
+    p = scenes.dam_params(iters=iters)
+    p.dt = DT
     pos, vel, boxes = scenes.million()
-    cfg = {"workload": "pbf_1m_plain_k4", "particles": int(len(pos)), "iters": 4, "h": 0.02,
-           "dt": "1/120", "domain": "20.48 x 20.48 (4 x 4 chunks of 5.12)", "cells": 1024 * 1024,
+    cfg = {"workload": "pbf_1m_plain_k4", "particles": int(len(pos)), "iters": iters, "h": 0.02,
+           "dt": "1/2000", "domain": "20.48 x 20.48 (4 x 4 chunks of 5.12)", "cells": 1024 * 1024,
            "scene": "960x1024 lattice block + 256x256 splash |v|~U(0,2), seed 2",
            "l2": "flushed before every timed step (256 MiB memset)"}
     return p, pos, vel, boxes, cfg
+
+
+def learned_leg(args, stream, flush_l2):
+    """The learned warm start against the plain form on the same scene: the network is trained first (pairs
+    from 41 plain 20-iteration steps, every 20th particle, 30 epochs on the GPU; untimed), then the
+    network-warm-started 2-iteration step and the plain 2-iteration step are timed like the headline."""
+    import torch
+
+    import gpe
+
+    sh = stream.cuda_stream
+    p20, pos, vel, boxes, _ = workload(iters=20)
+    n = len(pos)
+    e = gpe.Pbf(p20, boxes, capacity=n)
+    e.set_state(pos, vel, stream=sh)
+    net = gpe.Mlp(max_pairs=2_200_000, seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.collect(e, n_steps=41, stride=20, seed=3, stream=sh)
+    t_col = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tl, vl = net.train(gpe.make_train_params(epochs=30, batch=8192, lr=2e-3, val_fraction=0.1, seed=1), stream=sh)
+    t_tr = time.perf_counter() - t0
+    pairs = net.num_pairs
+    e.close()
+
+    def timed(iters, warm):
+        p, _, _, _, _ = workload(iters=iters)
+        eng = gpe.Pbf(p, boxes, capacity=n)
+        eng.set_state(pos, vel, stream=sh)
+        if warm:
+            eng.set_warm_start(gpe.WARM_MLP, net)
+        for _ in range(args.warmup):  # with the network, the first of these starts the multiplier memory
+            eng.step(1, stream=sh)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            flush_l2()
+            a.record(stream)
+            eng.step(1, stream=sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+        s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        dmax, dmean = eng.density_error(stream=sh)
+        st = eng.status()
+        eng.close()
+        return {"value": n * args.steps / s, "ms_per_step": 1e3 * s / args.steps, "iters": iters,
+                "density_error": {"max": dmax, "mean": dmean}, "status": st}
+
+    learned = timed(2, True)
+    plain2 = timed(2, False)
+    learned.update({"plain_k2": plain2,
+                    "train": {"pairs": pairs, "train_loss": tl, "val_loss": vl, "collect_s": t_col, "train_s": t_tr,
+                              "how": "pairs from 41 plain 20-iteration steps (every 20th particle), 30 epochs, "
+                                     "batch 8192, AdamW lr 2e-3, standardised MSE"}})
+    return learned
 
 
 def cpu_baseline(p, pos, vel, boxes, budget_s=12.0, max_steps=30):
@@ -348,9 +412,18 @@ def run_gpe(args, rank, ws):
     base = None
     if ws == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(p, pos, vel, boxes)
+    eng.close()
+    learned = None
+    if ws == 1 and not args.no_learned:
+        try:
+            learned = learned_leg(args, stream, flush_l2)
+            learned["speedup_vs_plain_k4"] = learned["value"] / (n * args.steps / total_s)
+            learned["target"] = {"density_error_max_le_1pct": learned["density_error"]["max"] <= 0.01,
+                                 "speedup_ge_2x": learned["speedup_vs_plain_k4"] >= 2.0}
+        except Exception as exc:  # reported, never fatal to the headline number
+            learned = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
     ref_cuda = None
     if ws == 1 and not args.no_reference_cuda:
-        eng.close()
         try:
             ref_cuda = reference_cuda_leg(args, stream, flush_l2)
         except Exception as exc:  # reported, never fatal to the headline number
@@ -363,7 +436,7 @@ def run_gpe(args, rank, ws):
             "gpu_launches": launches * args.steps, "launches_per_step": launches,
             "hbm_effective_gbs": 212.0 * value / ws / 1e9,
             "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary(),
-            "reference_cuda": ref_cuda}
+            "learned": learned, "reference_cuda": ref_cuda}
     print(json.dumps(line), flush=True)
 
 
@@ -375,6 +448,7 @@ def main():
     ap.add_argument("--impl", default="gpe", choices=["gpe", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgpe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "sort.cu", "pbf.cu", "mpm.cu"]
+SOURCES = ["capi.cu", "sort.cu", "pbf.cu", "mpm.cu", "mlp.cu"]
 
 
 def nvcc() -> str:
@@ -42,7 +42,7 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.h")) + [PKG.parent / "include" / "gpe.h"]
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "gpe.h"]
     cc = nvcc()
     flags = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
              "-I", str(PKG.parent / "include")]

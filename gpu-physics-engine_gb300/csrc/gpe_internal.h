@@ -65,4 +65,21 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
 int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket,
                        cudaStream_t st, const int32_t* n_dev = nullptr);
 
+// ----- warm-start network (mlp.cu) as the PBF engine sees it -----
+struct MlpDev;
+// Pair set of a network: features [cap][12] and targets [cap]; idx = the particle's sorted index when the
+// pair was taken; cnt[0] = pairs written (appended with atomics), cnt[1] = pairs whose target is written.
+struct MlpData {
+    float* X;
+    float* T;
+    int32_t* idx;
+    int32_t* cnt;
+    int64_t cap;
+};
+const MlpDev* mlp_device(const gpe_mlp* m);
+MlpData mlp_data(gpe_mlp* m);
+// iterations per step of the plain solve whose pairs the network learned (20 unless collected otherwise)
+int32_t mlp_pair_iters(const gpe_mlp* m);
+void mlp_set_pair_iters(gpe_mlp* m, int32_t iters);
+
 } // namespace gpe

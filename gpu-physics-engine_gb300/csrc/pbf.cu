@@ -17,6 +17,7 @@
 // lands in another cell range at the next sort.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -26,6 +27,7 @@
 
 #include "emit.cuh"
 #include "gpe_internal.h"
+#include "mlp.cuh"
 
 namespace gpe {
 
@@ -168,7 +170,8 @@ __global__ void __launch_bounds__(T_PART)
             const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
             const float2* __restrict__ xs_tmp, float2* __restrict__ x_out, float2* __restrict__ xs_out,
             uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
-            uint32_t* __restrict__ id_out)
+            uint32_t* __restrict__ id_out, const float* __restrict__ acc_in, float* __restrict__ prev_out,
+            float* __restrict__ lam_out)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t n = n_dev ? __ldg(n_dev) : n_host;
@@ -184,14 +187,27 @@ __global__ void __launch_bounds__(T_PART)
     perm[dst]          = (uint32_t)i;
     key_out[dst]       = kr.x;
     if (id_in) { id_out[dst] = id_in[i]; }
+    if (acc_in) {
+        // the previous step's summed multiplier follows the particle into the new order
+        const float a = acc_in[i];
+        prev_out[dst] = a;
+        if (lam_out) { lam_out[dst] = a; }
+    }
 }
 
 // ----- lambda (PBF.cu:243-294) --------------------------------------------------------------------------
-template <bool MULTI, bool SELFG>
+// ACC_NONE: the reference's lambda, recomputed from scratch in every iteration.
+// ACC_SUM:  the same, also added to the step's summed multiplier (training-pair collection).
+// ACC_PROJ: a later iteration of a GPE_WARM_PREV step. The summed multiplier L (acc) is updated by the
+//           projected increment L <- min(L - C_raw / (|grad C|^2 + eps), 0) with C_raw = rho/rho0 - 1
+//           unclamped, and the pass moves the particles by the change of L; a sum that overshot is relaxed
+//           again and L never turns into a pull (accumulated-multiplier clamping).
+enum { ACC_NONE = 0, ACC_SUM = 1, ACC_PROJ = 2 };
+template <bool MULTI, bool SELFG, int ACC>
 __global__ void __launch_bounds__(T_PART)
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
              const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
-             const uint32_t* __restrict__ pair_id)
+             const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count_of(k)) { return; }
@@ -255,21 +271,34 @@ __global__ void __launch_bounds__(T_PART)
     const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
     const float self = k.inv_mass * (gx * gx + gy * gy);
     const float grad = k.inv_rho0 * k.inv_rho0 * (self + gsq);
-    lam[i]           = -C / (grad + k.eps);
+    if (ACC == ACC_PROJ) {
+        const float lraw = -(rho * k.inv_rho0 - 1.f) / (grad + k.eps);
+        const float a    = acc[i];
+        const float an   = fminf(a + lraw, 0.f);
+        lam[i]           = an - a;
+        acc[i]           = an;
+    } else {
+        const float l = -C / (grad + k.eps);
+        lam[i]        = l;
+        if (ACC == ACC_SUM) { acc[i] += l; }
+    }
 }
 
 // ----- delta p with artificial pressure and over-relaxation, then walls (PBF.cu:398-447, 471-499) -------
-template <bool MULTI, bool SCORR>
+// ACCINIT: this pass applies the warm start; its multiplier starts the step's running sum.
+template <bool MULTI, bool SCORR, bool ACCINIT>
 __global__ void __launch_bounds__(T_PART)
     k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
               const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
-              float2* __restrict__ xs_out)
+              float2* __restrict__ xs_out, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count_of(k)) { return; }
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float2 p  = xs[i];
-    const float mli = lam[i] * k.mass;
+    const float li  = lam[i];
+    if (ACCINIT) { acc[i] = li; }
+    const float mli = li * k.mass;
     // dp = omega/(m rho0) sum (m lambda_i + m lambda_j - s_corr) * (-cs (h-r)^2 r/|r|) (PBF.cu:415-437); pairs
     // closer than 1e-6 (the self pair included) have a zero direction there and are skipped here.
     const float c6w = k.c6 * k.inv_w_dq;
@@ -299,6 +328,180 @@ __global__ void __launch_bounds__(T_PART)
     oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
     ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
     xs_out[i] = make_float2(ox, oy);
+}
+
+// ----- warm start: features of the first lambda pass ------------------------------------------------------
+// The lambda sums of k_lambda plus the neighbour count and the poly6-weighted sum of the neighbours'
+// lambda_prev; returns the cold first-iteration lambda and fills the network's 12 features (the order is
+// the one documented with gpe_pbf_set_warm_start).
+template <bool MULTI, bool SELFG>
+__device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, const uint32_t* __restrict__ start,
+                                               const float2* __restrict__ xs, const float2* __restrict__ xsorted,
+                                               const float* __restrict__ prev, const uint32_t* __restrict__ pair_id,
+                                               int32_t i, uint32_t pbase, float (&f)[MLP_F])
+{
+    const float2 p = xs[i];
+    float sx = 0.f, sy = 0.f, s4 = 0.f, s6 = 0.f, swl = 0.f;
+    int32_t nn     = 0;
+    bool self_seen = false;
+    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+        const float2 q  = __ldg(&xs[j]);
+        const float lp  = __ldg(&prev[j]);
+        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float r2  = rx * rx + ry * ry;
+        const bool self = j == (uint32_t)i;
+        self_seen       = self_seen || self;
+        const bool in   = (r2 <= k.h2) && !self;
+        const bool dir  = in && (r2 > 1e-12f);
+        const float qq  = in ? k.h2 - r2 : 0.f;
+        s6              = fmaf(qq * qq, qq, s6); // as in k_lambda, so the cold lambda is bit-identical
+        swl             = fmaf(qq * qq * qq, lp, swl);
+        nn += in ? 1 : 0;
+        const float inv = rsqrtf(dir ? r2 : 1.f);
+        const float dif = dir ? k.h - r2 * inv : 0.f;
+        const float d2  = dif * dif;
+        const float w   = d2 * inv;
+        sx              = fmaf(w, rx, sx);
+        sy              = fmaf(w, ry, sy);
+        s4              = fmaf(d2, d2, s4);
+        if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
+            float nx, ny;
+            if (pair_id) {
+                pair_direction(__ldg(&pair_id[i]), __ldg(&pair_id[j]), nx, ny);
+            } else {
+                pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
+            }
+            sx = fmaf(k.h2, nx, sx);
+            sy = fmaf(k.h2, ny, sy);
+            s4 = fmaf(k.h2, k.h2, s4);
+        }
+    });
+    const float lpi = prev[i];
+    if (self_seen) {
+        s6  = fmaf(k.h2 * k.h2, k.h2, s6);
+        swl = fmaf(k.h2 * k.h2 * k.h2, lpi, swl);
+        if (SELFG) {
+            float nx, ny;
+            const uint32_t a = pair_id ? __ldg(&pair_id[i]) : (uint32_t)i - pbase;
+            pair_direction(a, a, nx, ny);
+            sx = fmaf(k.h2, nx, sx);
+            sy = fmaf(k.h2, ny, sy);
+            s4 = fmaf(k.h2, k.h2, s4);
+        }
+    }
+    const float csm  = k.cs * k.mass;
+    const float rho  = k.mass * k.c6 * s6;
+    const float gx = csm * sx, gy = csm * sy;
+    const float gsq  = k.inv_mass * (csm * csm) * s4;
+    const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
+    const float self = k.inv_mass * (gx * gx + gy * gy);
+    const float grad = k.inv_rho0 * k.inv_rho0 * (self + gsq);
+    const float lam  = -C / (grad + k.eps);
+    const float2 po  = xsorted[i];
+    const float ddx = p.x - po.x, ddy = p.y - po.y;
+    const float inv_h = 1.f / k.h;
+    const float wall  = fminf(fminf(p.x - d.lox, d.hix - p.x), fminf(p.y - d.loy, d.hiy - p.y)) * inv_h;
+    f[0]  = (float)nn;
+    f[1]  = lpi;
+    f[2]  = rho * k.inv_rho0 - 1.f;
+    f[3]  = C;
+    f[4]  = sqrtf(ddx * ddx + ddy * ddy) * inv_h;
+    f[5]  = -gx * k.inv_rho0; // dC_i/dx_i = -(cs m / rho0) sum (h-r)^2 r/|r|
+    f[6]  = -gy * k.inv_rho0;
+    f[7]  = sqrtf(f[5] * f[5] + f[6] * f[6]);
+    f[8]  = grad;
+    f[9]  = lam;
+    f[10] = fminf(fmaxf(wall, 0.f), 4.f);
+    f[11] = s6 > 0.f ? swl / s6 : 0.f;
+    return lam;
+}
+
+// First lambda pass of a GPE_WARM_MLP step: features, then the network on the tensor cores for a tile of
+// 128 particles per iteration of a persistent loop; lambda = lambda_prev + r.
+template <bool MULTI, bool SELFG>
+__global__ void __launch_bounds__(MLP_TILE)
+    k_lambda_mlp(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                 const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float2* __restrict__ xsorted,
+                 const float* __restrict__ prev, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
+                 const MlpDev* __restrict__ mlp, uint32_t* __restrict__ status)
+{
+    __shared__ MlpFwdSmem S;
+    const int32_t n      = count_of(k);
+    const int32_t ntiles = (n + MLP_TILE - 1) / MLP_TILE;
+    if ((int32_t)blockIdx.x >= ntiles) { return; } // uniform over the CTA, before any barrier
+    mlp_fwd_setup(S, mlp);
+    const float ymu = mlp->ymu, ysd = mlp->ysd;
+    uint32_t phase  = 0;
+    bool ok         = true;
+    for (int32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int32_t i  = tile * MLP_TILE + (int32_t)threadIdx.x;
+        const bool valid = i < n;
+        float f[MLP_F];
+#pragma unroll
+        for (int q = 0; q < MLP_F; ++q) { f[q] = 0.f; }
+        if (valid) {
+            const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
+            const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
+            warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+        }
+        const float y = mlp_fwd_tile(S, f, phase, ok);
+        if (valid) { lam[i] = fminf(f[1] + fmaf(y, ysd, ymu), 0.f); } // a summed multiplier only pushes
+    }
+    if (!ok) { atomicOr(status, GPE_STATUS_TIMEOUT); }
+    mlp_fwd_teardown(S);
+}
+
+// Training-pair collection: the first lambda pass of a plain (cold) step, which also appends the features
+// of the particles that a seeded hash selects (probability 1/stride; none when stride is 0); the step's
+// summed multiplier over its params.iters iterations becomes their target.
+struct CollectK {
+    float* X;
+    float* T;
+    int32_t* idx;
+    int32_t* cnt;
+    int32_t cap;
+    uint32_t salt;
+    uint32_t stride;
+};
+
+template <bool MULTI, bool SELFG>
+__global__ void __launch_bounds__(T_PART)
+    k_lambda_collect(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                     const uint32_t* __restrict__ start, const float2* __restrict__ xs,
+                     const float2* __restrict__ xsorted, const float* __restrict__ prev, float* __restrict__ lam,
+                     const uint32_t* __restrict__ pair_id, const CollectK col)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count_of(k)) { return; }
+    const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
+    const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
+    float f[MLP_F];
+    lam[i] = warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    if (col.stride != 0u && mix32((uint32_t)i * 0x9E3779B9u ^ col.salt) % col.stride == 0u) {
+        const int32_t slot = atomicAdd(&col.cnt[0], 1);
+        if (slot < col.cap) {
+#pragma unroll
+            for (int q = 0; q < MLP_F; ++q) { col.X[(size_t)slot * MLP_F + q] = f[q]; }
+            col.idx[slot] = i;
+        }
+    }
+}
+
+// Targets of the pairs taken this step: the step's summed multiplier minus lambda_prev.
+__global__ void k_collect_targets(const int32_t* __restrict__ cnt, const float* __restrict__ X, float* __restrict__ T,
+                                  const int32_t* __restrict__ idx, const float* __restrict__ acc, int32_t cap)
+{
+    const int32_t slot = cnt[1] + (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int32_t end  = min(cnt[0], cap);
+    if (slot >= end) { return; }
+    T[slot] = acc[idx[slot]] - X[(size_t)slot * MLP_F + 1];
+}
+
+__global__ void k_collect_advance(int32_t* __restrict__ cnt, int32_t cap)
+{
+    const int32_t c = min(cnt[0], cap);
+    cnt[0]          = c;
+    cnt[1]          = c;
 }
 
 // velocityClamp, PBF.cu:629-638
@@ -578,6 +781,15 @@ struct gpe_pbf {
     float* red        = nullptr;
     int32_t* d_count  = nullptr; // device-resident particle count
     bool dynamic      = false;   // GPE_PBF_DYNAMIC_COUNT: launches cover the capacity
+    float* acc        = nullptr; // summed multiplier of the current step (sorted order of the step)
+    float* prev       = nullptr; // the previous step's sum, carried into the current sorted order
+    int32_t warm      = GPE_WARM_NONE;
+    const gpe_mlp* mlp = nullptr;
+    bool collecting   = false;   // gpe_mlp_collect: cold solve with summed multipliers and pair capture
+    CollectK col{};
+    bool pending_accinit = false; // stage API: the next DELTA_P starts the running sum
+    bool mem_valid    = false;    // the multiplier memory holds a previous step's sums (else it is 0)
+    int32_t lam_grid  = 0;        // persistent grid of k_lambda_mlp
 
     // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
     int X = 0, SX = -1, XS = -1, XO = -1;
@@ -599,6 +811,8 @@ struct gpe_pbf {
 namespace {
 
 bool multi(const gpe_pbf* s) { return s->nd > 1; }
+// steps that keep the summed multiplier: warm-started steps and training-pair collection
+bool accumulating(const gpe_pbf* s) { return s->warm != GPE_WARM_NONE || s->collecting; }
 
 int32_t validate_params(const gpe_pbf_params* p)
 {
@@ -746,7 +960,9 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
                                                   s->xs_tmp,
                                                   s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
                                                   ids ? s->ids[s->id_cur] : nullptr,
-                                                  ids ? s->ids[s->id_cur ^ 1] : nullptr);
+                                                  ids ? s->ids[s->id_cur ^ 1] : nullptr,
+                                                  accumulating(s) ? s->acc : nullptr, s->prev,
+                                                  (s->warm == GPE_WARM_PREV && !s->collecting) ? s->lam : nullptr);
         GPE_CHECK_LAUNCH("k_place");
         if (ids) { s->id_cur ^= 1; }
     }
@@ -755,28 +971,57 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     return GPE_OK;
 }
 
-// Template dispatch tables: [multi scene][flag]
+// Template dispatch tables: [multi scene][flag][accumulation mode]
 using LamFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                       const float2*, float*, const uint32_t*);
-template <bool M, bool S>
+                       const float2*, float*, const uint32_t*, float*);
+template <bool M, bool S, int A>
 void lam_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid)
+                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc)
 {
-    k_lambda<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, pid);
+    k_lambda<M, S, A><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
 }
-const LamFn kLam[2][2] = {{lam_launch<false, false>, lam_launch<false, true>},
-                          {lam_launch<true, false>, lam_launch<true, true>}};
+#define GPE_LAM3(M, S) {lam_launch<M, S, ACC_NONE>, lam_launch<M, S, ACC_SUM>, lam_launch<M, S, ACC_PROJ>}
+const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
+                             {GPE_LAM3(true, false), GPE_LAM3(true, true)}};
+#undef GPE_LAM3
 
 using DpFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                      const float2*, const float*, float2*);
-template <bool M, bool S>
+                      const float2*, const float*, float2*, float*);
+template <bool M, bool S, bool A>
 void dp_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-               const uint32_t* start, const float2* xs, const float* lam, float2* out)
+               const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc)
 {
-    k_delta_p<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, out);
+    k_delta_p<M, S, A><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
 }
-const DpFn kDp[2][2] = {{dp_launch<false, false>, dp_launch<false, true>},
-                        {dp_launch<true, false>, dp_launch<true, true>}};
+const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, false, true>},
+                            {dp_launch<false, true, false>, dp_launch<false, true, true>}},
+                           {{dp_launch<true, false, false>, dp_launch<true, false, true>},
+                            {dp_launch<true, true, false>, dp_launch<true, true, true>}}};
+
+using WarmFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                        const float2*, const float2*, const float*, float*, const uint32_t*, const MlpDev*,
+                        uint32_t*);
+template <bool M, bool S>
+void mlp_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+                const uint32_t* start, const float2* xs, const float2* xo, const float* prev, float* lam,
+                const uint32_t* pid, const MlpDev* mlp, uint32_t* status)
+{
+    k_lambda_mlp<M, S><<<g, MLP_TILE, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, mlp, status);
+}
+const WarmFn kMlp[2][2] = {{mlp_launch<false, false>, mlp_launch<false, true>},
+                           {mlp_launch<true, false>, mlp_launch<true, true>}};
+
+using ColFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                       const float2*, const float2*, const float*, float*, const uint32_t*, const CollectK&);
+template <bool M, bool S>
+void col_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+                const uint32_t* start, const float2* xs, const float2* xo, const float* prev, float* lam,
+                const uint32_t* pid, const CollectK& col)
+{
+    k_lambda_collect<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, col);
+}
+const ColFn kCol[2][2] = {{col_launch<false, false>, col_launch<false, true>},
+                          {col_launch<true, false>, col_launch<true, true>}};
 
 using XsFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                       const float2*, const float2*, float2*, float*, uint32_t*);
@@ -789,24 +1034,56 @@ void xs_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, c
 const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
                         {xs_launch<true, false>, xs_launch<true, true>}};
 
-int32_t stage_lambda(gpe_pbf* s, cudaStream_t st)
+// accumulation mode of the lambda passes after the first in the engine's current mode
+int acc_mode(const gpe_pbf* s)
+{
+    if (s->collecting || s->warm == GPE_WARM_MLP) { return ACC_SUM; }
+    return s->warm == GPE_WARM_PREV ? ACC_PROJ : ACC_NONE;
+}
+
+int32_t stage_lambda(gpe_pbf* s, cudaStream_t st, int acc)
 {
     if (lsize(s) == 0) { return GPE_OK; }
     const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
-    kLam[multi(s) ? 1 : 0][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
-                               pid);
+    kLam[multi(s) ? 1 : 0][sg][acc](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
+                                    s->lam, pid, s->acc);
     GPE_CHECK_LAUNCH("k_lambda");
     s->launches += 1;
     return GPE_OK;
 }
 
-int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st)
+// First lambda pass of an accumulating step: the network (GPE_WARM_MLP), the cold pass with pair capture
+// (collection) or nothing (GPE_WARM_PREV: the sort already placed lambda_prev into lambda).
+int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
+{
+    if (lsize(s) == 0 || (s->warm == GPE_WARM_PREV && !s->collecting)) { return GPE_OK; }
+    // a network step needs the memory of a previous step; the first step after a reset runs the plain pass
+    // (no pairs taken) and starts the memory
+    const int mi        = multi(s) ? 1 : 0;
+    const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
+    const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
+    if (s->warm == GPE_WARM_MLP && s->mem_valid && !s->collecting) {
+        const int64_t tiles = (lsize(s) + MLP_TILE - 1) / MLP_TILE;
+        const unsigned g    = (unsigned)std::min<int64_t>(tiles, s->lam_grid);
+        kMlp[mi][sg](g, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX], s->prev, s->lam, pid,
+                     gpe::mlp_device(s->mlp), s->status);
+        GPE_CHECK_LAUNCH("k_lambda_mlp");
+    } else {
+        kCol[mi][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
+                     s->prev, s->lam, pid, s->col);
+        GPE_CHECK_LAUNCH("k_lambda_collect");
+    }
+    s->launches += 1;
+    return GPE_OK;
+}
+
+int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
 {
     if (lsize(s) > 0) {
         const int sc = s->prm.scorr_k != 0.f ? 1 : 0;
-        kDp[multi(s) ? 1 : 0][sc](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->lam,
-                                  s->pos[s->XO]);
+        kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start,
+                                                   s->pos[s->XS], s->lam, s->pos[s->XO], s->acc);
         GPE_CHECK_LAUNCH("k_delta_p");
         s->launches += 1;
     }
@@ -849,14 +1126,28 @@ int32_t stage_finish(gpe_pbf* s)
 
 int32_t run_step(gpe_pbf* s, cudaStream_t st)
 {
-    int32_t rc = stage_predict_sort(s, st);
+    const bool acc = accumulating(s);
+    int32_t rc     = stage_predict_sort(s, st);
     for (int32_t it = 0; it < s->prm.iters && rc == GPE_OK; ++it) {
-        rc = stage_lambda(s, st);
-        if (rc == GPE_OK) { rc = stage_delta_p(s, st); }
+        if (it == 0 && acc) {
+            rc = stage_lambda_warm(s, st);
+            if (rc == GPE_OK) { rc = stage_delta_p(s, st, true); }
+        } else {
+            rc = stage_lambda(s, st, acc_mode(s));
+            if (rc == GPE_OK) { rc = stage_delta_p(s, st, false); }
+        }
     }
     if (rc == GPE_OK) { rc = stage_xsph(s, st); }
     if (rc == GPE_OK) { rc = stage_vorticity(s, st); }
+    if (rc == GPE_OK && s->collecting && s->col.stride != 0u && lsize(s) > 0) {
+        k_collect_targets<<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->col.cnt, s->col.X, s->col.T, s->col.idx,
+                                                                s->acc, s->col.cap);
+        GPE_CHECK_LAUNCH("k_collect_targets");
+        k_collect_advance<<<1, 1, 0, st>>>(s->col.cnt, s->col.cap);
+        GPE_CHECK_LAUNCH("k_collect_advance");
+    }
     if (rc == GPE_OK) { rc = stage_finish(s); }
+    if (rc == GPE_OK && acc && s->prm.iters > 0) { s->mem_valid = true; }
     return rc;
 }
 
@@ -886,6 +1177,8 @@ int32_t alloc_buffers(gpe_pbf* s)
     const size_t o_stat  = c.take<uint32_t>(4);
     const size_t o_red   = c.take<float>(8);
     const size_t o_cnt1  = c.take<int32_t>(1);
+    const size_t o_acc   = c.take<float>(N);
+    const size_t o_prev  = c.take<float>(N);
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -909,6 +1202,8 @@ int32_t alloc_buffers(gpe_pbf* s)
     s->status  = reinterpret_cast<uint32_t*>(b + o_stat);
     s->red     = reinterpret_cast<float*>(b + o_red);
     s->d_count = reinterpret_cast<int32_t*>(b + o_cnt1);
+    s->acc     = reinterpret_cast<float*>(b + o_acc);
+    s->prev    = reinterpret_cast<float*>(b + o_prev);
     s->k.n_dev = s->d_count;
     GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
     return GPE_OK;
@@ -1063,10 +1358,13 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
     }
     k_set_count<<<1, 1, 0, st>>>(s->d_count, (int32_t)n);
     GPE_CHECK_LAUNCH("k_set_count");
+    // a new particle set has no previous multipliers
+    GPE_TRY_CUDA(cudaMemsetAsync(s->acc, 0, sizeof(float) * (size_t)s->cap, st));
     if (s->n != n && !s->dynamic) { s->drop_graphs(); }
     s->n          = n;
     s->have_state = true;
     s->have_sort  = false;
+    s->mem_valid  = false;
     return GPE_OK;
 }
 
@@ -1128,6 +1426,19 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
     }
     if (n_steps == 0) { return GPE_OK; }
     cudaStream_t st = as_stream(stream);
+    if (s->warm == GPE_WARM_MLP && !s->mem_valid) {
+        // The step that starts the multiplier memory is a plain step with the iteration count of the solve
+        // the network was trained on, so that the memory holds what the network expects as lambda_prev (a
+        // memory started by a short solve would be carried forward at that solve's level). It differs from
+        // the later steps and runs outside the graph.
+        const int32_t iters = s->prm.iters;
+        s->prm.iters        = gpe::mlp_pair_iters(s->mlp);
+        s->launches         = 0;
+        const int32_t rc    = run_step(s, st);
+        s->prm.iters        = iters;
+        if (rc) { return rc; }
+        if (--n_steps == 0) { return GPE_OK; }
+    }
     // the step sequence is captured once per (steps, starting buffer roles) and replayed as one graph
     const auto key = std::make_tuple(n_steps, s->X, s->id_cur);
     auto it        = s->graphs.find(key);
@@ -1187,10 +1498,17 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
             return stage_predict_sort(s, st);
         case GPE_PBF_STAGE_LAMBDA:
             if (!in_step) { break; }
-            return stage_lambda(s, st);
-        case GPE_PBF_STAGE_DELTA_P:
+            return stage_lambda(s, st, acc_mode(s));
+        case GPE_PBF_STAGE_WARM_LAMBDA:
+            if (!in_step || !accumulating(s)) { break; }
+            s->pending_accinit = true;
+            return stage_lambda_warm(s, st);
+        case GPE_PBF_STAGE_DELTA_P: {
             if (!in_step) { break; }
-            return stage_delta_p(s, st);
+            const bool ai      = s->pending_accinit;
+            s->pending_accinit = false;
+            return stage_delta_p(s, st, ai);
+        }
         case GPE_PBF_STAGE_XSPH:
             if (!in_step) { break; }
             return stage_xsph(s, st);
@@ -1260,6 +1578,8 @@ static int32_t field_ptr(gpe_pbf* s, int32_t field, void** p, size_t* esize, int
         case GPE_PBF_FIELD_DENSITY: *p = s->rho; *esize = 4; break;
         case GPE_PBF_FIELD_ID: *p = s->ids[s->id_cur]; *esize = 4; break;
         case GPE_PBF_FIELD_OMEGA: *p = s->omega; *esize = 4; break;
+        case GPE_PBF_FIELD_LAMBDA_PREV: *p = s->prev; *esize = 4; break;
+        case GPE_PBF_FIELD_LAMBDA_SUM: *p = s->acc; *esize = 4; break;
         default: return GPE_ERR_BAD_ARG;
     }
     return GPE_OK;
@@ -1307,6 +1627,7 @@ int32_t gpe_pbf_set_field(gpe_pbf* s, int32_t field, const void* src, int64_t n_
     cudaStream_t st = as_stream(stream);
     if (cnt > 0) { GPE_TRY_CUDA(cudaMemcpyAsync(p, src, es * (size_t)cnt, kind_in(mem), st)); }
     if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    if (field == GPE_PBF_FIELD_LAMBDA_SUM) { s->mem_valid = true; } // the caller supplied the memory
     return GPE_OK;
 }
 
@@ -1323,7 +1644,8 @@ int32_t gpe_pbf_status(gpe_pbf* s, uint32_t* status, void* stream)
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
 {
     if (!s || !launches) { return GPE_ERR_BAD_ARG; }
-    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0);
+    const bool skip_first = s->warm == GPE_WARM_PREV && s->prm.iters > 0; // lambda_prev is placed by the sort
+    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0) - (skip_first ? 1 : 0);
     return GPE_OK;
 }
 
@@ -1389,6 +1711,10 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
     if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
     if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (s->warm == GPE_WARM_MLP && !s->mem_valid) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_enqueue: run one gpe_pbf_step first to start the multiplier memory");
+        return GPE_ERR_NOT_READY;
+    }
     cudaStream_t st   = as_stream(stream);
     const int X0      = s->X;
     const int id0     = s->id_cur;
@@ -1406,6 +1732,76 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
     }
     s->X         = X0;
     s->id_cur    = id0;
+    s->have_sort = true;
+    return GPE_OK;
+}
+
+// =====================================================================================================
+// Warm start and training-pair collection
+// =====================================================================================================
+
+extern "C" int32_t gpe_pbf_set_warm_start(gpe_pbf* s, int32_t mode, const gpe_mlp* mlp)
+{
+    gpe::clear_error();
+    if (!s || mode < GPE_WARM_NONE || mode > GPE_WARM_MLP || (mode == GPE_WARM_MLP && !mlp)) {
+        return GPE_ERR_BAD_ARG;
+    }
+    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (mode == GPE_WARM_MLP) {
+        // persistent grid: every CTA resident at once (each holds 64 TMEM columns of the SM's 512)
+        // the kernel's tiles live in shared memory: prefer the largest carveout so that 7 CTAs fit per SM
+        const void* fns[4] = {reinterpret_cast<const void*>(k_lambda_mlp<false, false>),
+                              reinterpret_cast<const void*>(k_lambda_mlp<false, true>),
+                              reinterpret_cast<const void*>(k_lambda_mlp<true, false>),
+                              reinterpret_cast<const void*>(k_lambda_mlp<true, true>)};
+        for (const void* f : fns) {
+            GPE_TRY_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                              (int)cudaSharedmemCarveoutMaxShared));
+        }
+        // grid: as many CTAs per SM as TMEM holds (512 columns / 64); CTAs beyond those resident queue,
+        // and no CTA can wait for TMEM
+        s->lam_grid = (int32_t)(512 / MLP_FWD_TMEM_COLS) * gpe::sm_count();
+    }
+    s->warm = mode;
+    s->mlp  = mode == GPE_WARM_MLP ? mlp : nullptr;
+    s->mem_valid = false;
+    GPE_TRY_CUDA(cudaMemset(s->acc, 0, sizeof(float) * (size_t)s->cap));
+    GPE_TRY_CUDA(cudaDeviceSynchronize());
+    s->drop_graphs();
+    return GPE_OK;
+}
+
+extern "C" int32_t gpe_mlp_collect(gpe_mlp* m, gpe_pbf* s, int32_t n_steps, int32_t stride, uint64_t seed,
+                                   void* stream)
+{
+    gpe::clear_error();
+    if (!m || !s || n_steps < 0 || stride < 1) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state) { return GPE_ERR_NOT_READY; }
+    if (s->warm != GPE_WARM_NONE || s->SX >= 0) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_mlp_collect: the engine must be in GPE_WARM_NONE between steps");
+        return GPE_ERR_NOT_READY;
+    }
+    cudaStream_t st       = as_stream(stream);
+    const gpe::MlpData md = gpe::mlp_data(m);
+    GPE_TRY_CUDA(cudaMemsetAsync(s->acc, 0, sizeof(float) * (size_t)s->cap, st));
+    uint64_t rs   = seed;
+    int32_t rc    = GPE_OK;
+    s->collecting = true;
+    for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) {
+        // SplitMix64 (Steele, Lea & Flood 2014) step for the per-step selection salt
+        uint64_t z = (rs += 0x9E3779B97F4A7C15ull);
+        z          = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z          = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        // the first step has no previous multipliers to learn from: it only starts the sums
+        s->col = CollectK{md.X, md.T, md.idx, md.cnt, (int32_t)md.cap, (uint32_t)z, k == 0 ? 0u : (uint32_t)stride};
+        rc     = run_step(s, st);
+    }
+    s->collecting = false;
+    s->col        = CollectK{};
+    gpe::mlp_set_pair_iters(m, s->prm.iters);
+    if (rc) { return rc; }
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
     s->have_sort = true;
     return GPE_OK;
 }
@@ -1543,7 +1939,7 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
                                                   reinterpret_cast<const float2*>(pos), xs_tmp,
                                                   reinterpret_cast<float2*>(pos_sorted),
                                                   reinterpret_cast<float2*>(pred_sorted), perm, key_sorted, nullptr,
-                                                  nullptr);
+                                                  nullptr, nullptr, nullptr, nullptr);
         GPE_CHECK_LAUNCH("k_place (noalloc)");
     }
     return GPE_OK;

@@ -21,9 +21,12 @@ STATUS_NONFINITE, STATUS_CAPACITY, STATUS_CELL_OVERFLOW, STATUS_TIMEOUT = 1, 2, 
 
 PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS, PBF_DYNAMIC_COUNT = 0x1, 0x2, 0x4, 0x8, 0x10
 (PBF_STAGE_PREDICT_SORT, PBF_STAGE_LAMBDA, PBF_STAGE_DELTA_P, PBF_STAGE_XSPH, PBF_STAGE_VORTICITY,
- PBF_STAGE_FINISH, PBF_STAGE_DENSITY) = range(7)
+ PBF_STAGE_FINISH, PBF_STAGE_DENSITY, PBF_STAGE_WARM_LAMBDA) = range(8)
 (PBF_FIELD_POS, PBF_FIELD_VEL, PBF_FIELD_PRED, PBF_FIELD_LAMBDA, PBF_FIELD_KEY, PBF_FIELD_PERM,
- PBF_FIELD_CELL_START, PBF_FIELD_DOMAIN, PBF_FIELD_DENSITY, PBF_FIELD_ID, PBF_FIELD_OMEGA) = range(11)
+ PBF_FIELD_CELL_START, PBF_FIELD_DOMAIN, PBF_FIELD_DENSITY, PBF_FIELD_ID, PBF_FIELD_OMEGA,
+ PBF_FIELD_LAMBDA_PREV, PBF_FIELD_LAMBDA_SUM) = range(13)
+WARM_NONE, WARM_PREV, WARM_MLP = 0, 1, 2
+MLP_FEATURES, MLP_HIDDEN, MLP_NUM_WEIGHTS, MLP_BLOB_FLOATS = 12, 64, 5057, 5083
 
 MPM_MAT_FLUID, MPM_MAT_COROTATED, MPM_MAT_SNOW = 0, 1, 2
 MPM_BC_SLIP, MPM_BC_STICKY = 0, 1
@@ -73,6 +76,17 @@ class Hose(C.Structure):
 class View(C.Structure):
     _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("counts", C.c_void_p), ("chunks_x", C.c_int32),
                 ("chunks_y", C.c_int32), ("chunk_dim", C.c_float), ("chunk_capacity", C.c_int32)]
+
+
+class TrainParams(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("weight_decay", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("adam_eps", C.c_float), ("val_fraction", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+def make_train_params(epochs=20, batch=8192, lr=2e-3, weight_decay=1e-4, beta1=0.9, beta2=0.999, adam_eps=1e-8,
+                      val_fraction=0.1, seed=0) -> TrainParams:
+    return TrainParams(epochs, batch, lr, weight_decay, beta1, beta2, adam_eps, val_fraction, seed)
 
 
 def make_hose(origin, velocity, nozzle_width, spacing, jitter=0.0, steps_per_call=1) -> Hose:
@@ -142,6 +156,18 @@ def lib() -> C.CDLL:
             "gpe_mpm_get_grid": [vp, vp, i64, i32, vp],
             "gpe_mpm_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_mpm_launches_per_step": [vp, C.POINTER(i32)],
+            "gpe_pbf_set_warm_start": [vp, i32, vp],
+            "gpe_mlp_create": [i64, C.c_uint64, C.POINTER(vp)],
+            "gpe_mlp_destroy": [vp],
+            "gpe_mlp_get_blob": [vp, vp, i64],
+            "gpe_mlp_set_blob": [vp, vp, i64],
+            "gpe_mlp_collect": [vp, vp, i32, i32, C.c_uint64, vp],
+            "gpe_mlp_num_pairs": [vp, C.POINTER(i64)],
+            "gpe_mlp_get_pairs": [vp, vp, vp, vp, i64, i32, vp],
+            "gpe_mlp_set_pairs": [vp, vp, vp, i64, i32, vp],
+            "gpe_mlp_train": [vp, C.POINTER(TrainParams), C.POINTER(C.c_float), C.POINTER(C.c_float), vp],
+            "gpe_mlp_infer": [vp, vp, vp, i64, i32, vp],
+            "gpe_mlp_gradient": [vp, vp, vp, i64, vp, C.POINTER(C.c_float), i32, vp],
             "gpe_pbf_emit": [vp, C.POINTER(Hose), C.c_uint64, C.POINTER(i32), vp],
             "gpe_pbf_publish": [vp, vp, i32, vp],
             "gpe_pbf_enqueue": [vp, i32, vp],
@@ -200,7 +226,8 @@ def _f32(a, shape_last: int) -> np.ndarray:
 _FIELD_DT = {PBF_FIELD_POS: (np.float32, 2), PBF_FIELD_VEL: (np.float32, 2), PBF_FIELD_PRED: (np.float32, 2),
              PBF_FIELD_LAMBDA: (np.float32, 1), PBF_FIELD_KEY: (np.uint32, 1), PBF_FIELD_PERM: (np.uint32, 1),
              PBF_FIELD_CELL_START: (np.uint32, 1), PBF_FIELD_DOMAIN: (np.int32, 1),
-             PBF_FIELD_DENSITY: (np.float32, 1), PBF_FIELD_ID: (np.uint32, 1), PBF_FIELD_OMEGA: (np.float32, 1)}
+             PBF_FIELD_DENSITY: (np.float32, 1), PBF_FIELD_ID: (np.uint32, 1), PBF_FIELD_OMEGA: (np.float32, 1),
+             PBF_FIELD_LAMBDA_PREV: (np.float32, 1), PBF_FIELD_LAMBDA_SUM: (np.float32, 1)}
 
 
 class Pbf:
@@ -316,8 +343,88 @@ class Pbf:
     def enqueue(self, n_steps: int, stream=None) -> None:
         check(lib().gpe_pbf_enqueue(self.h, int(n_steps), stream), "gpe_pbf_enqueue")
 
+    def set_warm_start(self, mode: int, mlp: "Mlp | None" = None) -> None:
+        check(lib().gpe_pbf_set_warm_start(self.h, int(mode), None if mlp is None else mlp.h),
+              "gpe_pbf_set_warm_start")
+        self._mlp = mlp  # keep the network alive while the engine uses it
+
 
 # ----- MPM ----------------------------------------------------------------------------------------------
+class Mlp:
+    """The warm-start network (gpe_mlp): parameters, training pairs, GPU training and inference."""
+
+    def __init__(self, max_pairs: int = 0, seed: int = 0):
+        h = C.c_void_p()
+        check(lib().gpe_mlp_create(int(max_pairs), int(seed), C.byref(h)), "gpe_mlp_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().gpe_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def blob(self) -> np.ndarray:
+        b = np.empty(MLP_BLOB_FLOATS, np.float32)
+        check(lib().gpe_mlp_get_blob(self.h, b.ctypes.data, b.size), "gpe_mlp_get_blob")
+        return b
+
+    def set_blob(self, blob) -> None:
+        b = np.ascontiguousarray(blob, dtype=np.float32).reshape(-1)
+        check(lib().gpe_mlp_set_blob(self.h, b.ctypes.data, b.size), "gpe_mlp_set_blob")
+
+    def collect(self, pbf: Pbf, n_steps: int, stride: int = 1, seed: int = 0, stream=None) -> None:
+        check(lib().gpe_mlp_collect(self.h, pbf.h, int(n_steps), int(stride), int(seed), stream), "gpe_mlp_collect")
+
+    @property
+    def num_pairs(self) -> int:
+        v = C.c_int64()
+        check(lib().gpe_mlp_num_pairs(self.h, C.byref(v)), "gpe_mlp_num_pairs")
+        return v.value
+
+    def pairs(self):
+        n = self.num_pairs
+        X = np.empty((n, MLP_FEATURES), np.float32)
+        T = np.empty(n, np.float32)
+        idx = np.empty(n, np.int32)
+        check(lib().gpe_mlp_get_pairs(self.h, X.ctypes.data, T.ctypes.data, idx.ctypes.data, n, MEM_HOST, None),
+              "gpe_mlp_get_pairs")
+        return X, T, idx
+
+    def set_pairs(self, X, T) -> None:
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1)
+        check(lib().gpe_mlp_set_pairs(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], MEM_HOST, None),
+              "gpe_mlp_set_pairs")
+
+    def train(self, params: TrainParams | None = None, stream=None) -> tuple[float, float]:
+        params = params or make_train_params()
+        tl, vl = C.c_float(), C.c_float()
+        check(lib().gpe_mlp_train(self.h, C.byref(params), C.byref(tl), C.byref(vl), stream), "gpe_mlp_train")
+        return tl.value, vl.value
+
+    def infer(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        out = np.empty(X.shape[0], np.float32)
+        check(lib().gpe_mlp_infer(self.h, X.ctypes.data, out.ctypes.data, X.shape[0], MEM_HOST, None),
+              "gpe_mlp_infer")
+        return out
+
+    def gradient(self, X, T) -> tuple[np.ndarray, float]:
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1)
+        g = np.empty(MLP_NUM_WEIGHTS, np.float32)
+        loss = C.c_float()
+        check(lib().gpe_mlp_gradient(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], g.ctypes.data, C.byref(loss),
+                                     MEM_HOST, None), "gpe_mlp_gradient")
+        return g, loss.value
+
+
 class Mpm:
     """One MLS-MPM engine handle (gpe_mpm)."""
 

@@ -112,6 +112,8 @@ typedef struct gpe_pbf gpe_pbf;
 #define GPE_PBF_STAGE_VORTICITY 4    /* vorticity confinement (Macklin & Mueller 2013 eq. 15-16)              */
 #define GPE_PBF_STAGE_FINISH 5       /* x <- x*, publish the step                                             */
 #define GPE_PBF_STAGE_DENSITY 6      /* recompute rho for the density-error metric (not part of a step)       */
+#define GPE_PBF_STAGE_WARM_LAMBDA 7  /* first lambda of a warm-started step (gpe_pbf_set_warm_start); the next
+                                        DELTA_P starts the step's multiplier sum from it                        */
 
 /* Fields that can be read or written for inspection (element types in brackets). All are in the current
  * sorted order; n_elems counts elements of the field's type. */
@@ -126,6 +128,8 @@ typedef struct gpe_pbf gpe_pbf;
 #define GPE_PBF_FIELD_DENSITY 8    /* rho from the last DENSITY stage [float]              */
 #define GPE_PBF_FIELD_ID 9         /* particle id (GPE_PBF_TRACK_IDS) [uint32]             */
 #define GPE_PBF_FIELD_OMEGA 10     /* vorticity from the last XSPH stage [float]           */
+#define GPE_PBF_FIELD_LAMBDA_PREV 11 /* previous step's summed multiplier, sorted [float]   */
+#define GPE_PBF_FIELD_LAMBDA_SUM 12  /* this step's summed multiplier so far [float]        */
 
 int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, int32_t n_domains,
                        int64_t capacity, gpe_pbf** out);
@@ -191,6 +195,94 @@ int32_t gpe_pbf_publish(gpe_pbf* pbf, const gpe_view* view, int32_t view_mem, vo
  * caller's own stream capture (the reference's instantiatePBFGraph builds one graph per tick, PBF.cu:901-961).
  * Buffer roles are returned to their starting state at the end, so a captured sequence can be replayed. */
 int32_t gpe_pbf_enqueue(gpe_pbf* pbf, int32_t n_steps, void* stream);
+
+/* ======================================================================================================
+ * Learned warm start of the PBF constraint solve
+ * ======================================================================================================
+ * The Jacobi solve computes in every iteration a multiplier lambda_i = -C_i / (|grad C|^2 + eps) per particle
+ * (lambdaKernel, PBF.cu:243-294) and moves the particles by it (posCorrectionKernel, PBF.cu:395-438). Summed
+ * over a plain solve of many iterations it is Lambda_i, the multiplier the converged solve applies. A
+ * warm-started step uses a prediction of Lambda_i in its first delta-p pass instead of the cold
+ * first-iteration lambda; its other iters - 1 passes are the plain iteration, which stays the fallback and
+ * decides the result. Each particle keeps a multiplier memory carried through the sorts, lambda_prev.
+ *
+ *   GPE_WARM_MLP   Lambda = min(lambda_prev + r, 0), r from a 12 -> 64 -> 64 -> 1 ReLU network run on the
+ *                  tensor cores (BF16 operands, FP32 accumulation) inside the first lambda pass; the later
+ *                  passes are the reference's iteration; the memory keeps Lambda plus their lambdas, the
+ *                  step's total multiplier, as in the training pairs. The first step after a reset has no
+ *                  memory and runs the plain first pass instead (gpe_pbf_enqueue wants one step before).
+ *   GPE_WARM_PREV  Lambda = lambda_prev, no network: the non-learned warm start. The later passes move the
+ *                  summed multiplier by the unclamped lambda, projected to <= 0, and the memory keeps that
+ *                  sum. Carrying a position-based multiplier across steps counts the last step's correction
+ *                  twice (it is already in the velocity); this mode is kept as the ablation it is, not as a
+ *                  stable solver.
+ *
+ * Network features, per particle, from the sorted predicted positions x* of the step:
+ *    0 neighbours within h (self excluded)           6 dC/dy
+ *    1 lambda_prev                                    7 |grad C|
+ *    2 rho* / rho0 - 1                                  8 the lambda denominator without eps
+ *    3 C = max(rho* / rho0 - 1, c_min)                  9 the cold first-iteration lambda
+ *    4 |x* - x| / h                                  10 distance to the nearest wall / h, at most 4
+ *    5 dC/dx                                         11 poly6-weighted mean of the neighbours' lambda_prev
+ * Training pairs are (features, Lambda - lambda_prev) from the plain solver run with many iterations, whose
+ * own Lambda is lambda_prev of its next step; the network is trained on the GPU (forward and backward
+ * products on the tensor cores, AdamW) on standardised features and targets. */
+typedef struct gpe_mlp gpe_mlp;
+#define GPE_MLP_FEATURES 12
+#define GPE_MLP_HIDDEN 64
+/* parameter vector, row-major [out][in]: W1[64][12], b1[64], W2[64][64], b2[64], w3[64], b3 */
+#define GPE_MLP_NUM_WEIGHTS 5057
+/* blob: parameters, feature mean[12], feature std[12], target mean, target std */
+#define GPE_MLP_BLOB_FLOATS 5083
+
+typedef struct gpe_mlp_train_params {
+    int32_t epochs;
+    int32_t batch;       /* pairs per optimiser step                                                    */
+    float lr;            /* AdamW (Loshchilov & Hutter 2019) step size                                 */
+    float weight_decay;  /* decoupled decay of W1, W2, w3                                              */
+    float beta1, beta2, adam_eps;
+    float val_fraction;  /* the last pairs of the set are held out for the validation loss             */
+    uint64_t seed;       /* shuffling of the training pairs                                            */
+} gpe_mlp_train_params;
+
+#define GPE_WARM_NONE 0
+#define GPE_WARM_PREV 1
+#define GPE_WARM_MLP 2
+
+/* A network with seeded uniform He initialisation, room for max_pairs training pairs, identity
+ * standardisation. */
+int32_t gpe_mlp_create(int64_t max_pairs, uint64_t seed, gpe_mlp** out);
+int32_t gpe_mlp_destroy(gpe_mlp* mlp);
+/* Save / load: n must be GPE_MLP_BLOB_FLOATS. */
+int32_t gpe_mlp_get_blob(const gpe_mlp* mlp, float* blob, int64_t n);
+int32_t gpe_mlp_set_blob(gpe_mlp* mlp, const float* blob, int64_t n);
+/* Runs n_steps plain steps of pbf (params.iters iterations each) that also sum their multipliers, and
+ * appends, from every step after the first, a pair for each particle that a seeded hash selects with
+ * probability 1/stride. pbf must be in GPE_WARM_NONE. Pairs beyond max_pairs are dropped. */
+int32_t gpe_mlp_collect(gpe_mlp* mlp, gpe_pbf* pbf, int32_t n_steps, int32_t stride, uint64_t seed, void* stream);
+int32_t gpe_mlp_num_pairs(const gpe_mlp* mlp, int64_t* n);
+/* features [n][12], targets [n], index [n] (the particle's sorted index when the pair was taken); any
+ * output may be NULL. n must equal the pair count. */
+int32_t gpe_mlp_get_pairs(const gpe_mlp* mlp, float* features, float* targets, int32_t* index, int64_t n,
+                          int32_t mem, void* stream);
+int32_t gpe_mlp_set_pairs(gpe_mlp* mlp, const float* features, const float* targets, int64_t n, int32_t mem,
+                          void* stream);
+/* Sets the standardisation from the training part of the pair set, then trains. train_loss / val_loss
+ * (may be NULL) receive the mean squared error of the standardised target over the last epoch and over
+ * the held-out pairs. */
+int32_t gpe_mlp_train(gpe_mlp* mlp, const gpe_mlp_train_params* params, float* train_loss, float* val_loss,
+                      void* stream);
+/* r for n raw feature vectors (features [n][12] -> out [n], de-standardised). */
+int32_t gpe_mlp_infer(const gpe_mlp* mlp, const float* features, float* out, int64_t n, int32_t mem,
+                      void* stream);
+/* Gradient of the mean over the n pairs of (y - t)^2, y the network output and t the standardised target,
+ * with respect to the parameter vector (grad [GPE_MLP_NUM_WEIGHTS]); *loss receives that mean. Device
+ * memory of the network is unchanged. */
+int32_t gpe_mlp_gradient(gpe_mlp* mlp, const float* features, const float* targets, int64_t n, float* grad,
+                         float* loss, int32_t mem, void* stream);
+/* Selects the warm start of pbf's later steps; mlp is required for GPE_WARM_MLP and must outlive its use.
+ * Resets lambda_prev to 0. */
+int32_t gpe_pbf_set_warm_start(gpe_pbf* pbf, int32_t mode, const gpe_mlp* mlp);
 
 /* Allocation-free predict + cell sort for one scene. It has no counterpart in the reference (whose arenas
  * are all allocated up front, cuda-engine.cpp:102-139); it exists for callers that cannot call cudaMalloc,

@@ -231,7 +231,8 @@ void orc_pbf_predict_sort(const gpe_pbf_params* p, const gpe_domain* doms, int32
 
 /* ----- lambda: PBF.cu:243-294 ----- */
 static double lambda_one(const gpe_pbf_params* p, const kconst* k, const dinfo* d, const uint32_t* cs, int64_t i,
-                         int64_t pbase, const double* xs, const uint32_t* pair_id, double* rho_out)
+                         int64_t pbase, const double* xs, const uint32_t* pair_id, double* rho_out,
+                         double* lraw_out)
 {
     const double px = xs[2 * i], py = xs[2 * i + 1];
     int64_t beg[16], end[16];
@@ -275,6 +276,7 @@ static double lambda_one(const gpe_pbf_params* p, const kconst* k, const dinfo* 
     const double self = (gx * gx + gy * gy) / m;
     const double grad = (self + gsq) / ((double)p->rho0 * p->rho0);
     if (rho_out) { *rho_out = rho; }
+    if (lraw_out) { *lraw_out = -(rho / p->rho0 - 1.0) / (grad + p->eps); } /* unclamped C */
     return -C / (grad + p->eps);
 }
 
@@ -300,8 +302,27 @@ static void lambda_pass(const gpe_pbf_params* p, const dinfo* di, const int64_t*
     for (int64_t i = 0; i < n; ++i) {
         const int32_t d = dom_of(dom, i);
         double r;
-        lambda[i] = lambda_one(p, &k, &di[d], cs, i, pb[d], xs, pair_id, &r);
+        lambda[i] = lambda_one(p, &k, &di[d], cs, i, pb[d], xs, pair_id, &r, NULL);
         if (rho) { rho[i] = r; }
+    }
+}
+
+/* A later iteration of a warm-started step (the device's k_lambda with ACC): the summed multiplier moves by
+ * the unclamped lambda and is projected to <= 0; delta receives the change, which the delta-p pass applies. */
+static void lambda_proj_pass(const gpe_pbf_params* p, const dinfo* di, const int64_t* pb, int64_t n, const double* xs,
+                             const int32_t* dom, const uint32_t* cs, const uint32_t* pair_id, double* sum,
+                             double* delta)
+{
+    const kconst k = make_kconst(p);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t d = dom_of(dom, i);
+        double lraw;
+        (void)lambda_one(p, &k, &di[d], cs, i, pb[d], xs, pair_id, NULL, &lraw);
+        double an = sum[i] + lraw;
+        if (an > 0.0) { an = 0.0; }
+        delta[i] = an - sum[i];
+        sum[i]   = an;
     }
 }
 
@@ -650,6 +671,341 @@ void orc_pbf_step(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, i
     free(pid_sorted);
     free(w);
     free(vd);
+    free(lam);
+    free(xsb);
+    free(xsa);
+    free(xd);
+    free(dsort);
+    free(xssort);
+    free(xsort);
+    free(cs);
+    free(perm);
+    free(key);
+    free(di);
+}
+
+/* ===================================================================================================== */
+/* PBF warm start: features, the network (with the device's BF16 operand roundings), warm-started steps     */
+/* ===================================================================================================== */
+
+/* FP32 value of v rounded to the nearest BF16, ties to even (the operand rounding of the tensor-core path) */
+static double bf16r(double v)
+{
+    float f = (float)v;
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) { return f; }
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+#define NF GPE_MLP_FEATURES
+#define NH GPE_MLP_HIDDEN
+enum { W1 = 0, B1 = W1 + NH * NF, W2 = B1 + NH, B2 = W2 + NH * NH, W3 = B2 + NH, B3 = W3 + NH, NW = B3 + 1 };
+
+/* The 12 features of particle i (the device's warm_features) and the cold first-iteration lambda. */
+static double features_one(const gpe_pbf_params* p, const kconst* k, const dinfo* d, const uint32_t* cs, int64_t i,
+                           int64_t pbase, const double* xs, const double* x, const double* prev,
+                           const uint32_t* pair_id, double f[NF])
+{
+    const double px = xs[2 * i], py = xs[2 * i + 1];
+    int64_t beg[16], end[16];
+    const int32_t nr = scan_rows(d, k, cs, (float)px, (float)py, beg, end);
+    const double m   = p->mass;
+    double gx = 0, gy = 0, gsq = 0, rho = 0, sw = 0, swl = 0;
+    int64_t nn = 0;
+    for (int32_t r = 0; r < nr; ++r) {
+        for (int64_t j = beg[r]; j < end[r]; ++j) {
+            const double rx = px - xs[2 * j], ry = py - xs[2 * j + 1];
+            const double r2 = rx * rx + ry * ry;
+            if (r2 > k->h2) { continue; }
+            if (j != i) { ++nn; }
+            double dist = 0.0, nx = 0.0, ny = 0.0;
+            if (r2 > 1e-12) {
+                dist = sqrt(r2);
+                nx   = rx / dist;
+                ny   = ry / dist;
+            }
+            if (px == xs[2 * j] && py == xs[2 * j + 1]) {
+                if (p->flags & GPE_PBF_SELF_GRAD) {
+                    if (pair_id) {
+                        pair_direction(pair_id[i], pair_id[j], &nx, &ny);
+                    } else {
+                        pair_direction(i - pbase, j - pbase, &nx, &ny);
+                    }
+                } else {
+                    nx = ny = 0.0;
+                }
+            }
+            const double diff = k->h - dist;
+            const double sc   = -k->cs * diff * diff;
+            const double svx  = sc * nx * m, svy = sc * ny * m;
+            gx += svx;
+            gy += svy;
+            gsq += (svx * svx + svy * svy) / m;
+            const double q  = k->h2 - r2;
+            const double w6 = q * q * q;
+            rho += m * k->c6 * w6;
+            sw += w6;
+            swl += w6 * prev[j];
+        }
+    }
+    double C = rho / p->rho0 - 1.0;
+    if (C < p->c_min) { C = p->c_min; }
+    const double self = (gx * gx + gy * gy) / m;
+    const double grad = (self + gsq) / ((double)p->rho0 * p->rho0);
+    const double lam  = -C / (grad + p->eps);
+    const double dx = px - x[2 * i], dy = py - x[2 * i + 1];
+    double wall = px - d->lox;
+    if (d->hix - px < wall) { wall = d->hix - px; }
+    if (py - d->loy < wall) { wall = py - d->loy; }
+    if (d->hiy - py < wall) { wall = d->hiy - py; }
+    wall /= (double)p->h;
+    f[0]  = (double)nn;
+    f[1]  = prev[i];
+    f[2]  = rho / p->rho0 - 1.0;
+    f[3]  = C;
+    f[4]  = sqrt(dx * dx + dy * dy) / (double)p->h;
+    f[5]  = gx / p->rho0;
+    f[6]  = gy / p->rho0;
+    f[7]  = sqrt(f[5] * f[5] + f[6] * f[6]);
+    f[8]  = grad;
+    f[9]  = lam;
+    f[10] = wall < 0.0 ? 0.0 : (wall > 4.0 ? 4.0 : wall);
+    f[11] = sw > 0.0 ? swl / sw : 0.0;
+    return lam;
+}
+
+static void features_pass(const gpe_pbf_params* p, const dinfo* di, const int64_t* pb, int64_t n, const double* xs,
+                          const double* x, const double* prev, const int32_t* dom, const uint32_t* cs,
+                          const uint32_t* pair_id, double* feat, double* lam)
+{
+    const kconst k = make_kconst(p);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t d = dom_of(dom, i);
+        double f[NF];
+        const double l = features_one(p, &k, &di[d], cs, i, pb[d], xs, x, prev, pair_id, f);
+        if (feat) { memcpy(&feat[i * NF], f, sizeof(f)); }
+        if (lam) { lam[i] = l; }
+    }
+}
+
+void orc_pbf_features(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
+                      const float* x, const float* prev, const int32_t* dom, const uint32_t* cell_start,
+                      const uint32_t* pair_id, float* features)
+{
+    dinfo* di     = (dinfo*)malloc(sizeof(dinfo) * (size_t)nd);
+    build_dinfo(p, doms, nd, di);
+    int64_t* pb   = dom_pbase(di, nd, cell_start);
+    double* xsd   = to_double(xs, 2 * n);
+    double* xd    = to_double(x, 2 * n);
+    double* pd    = to_double(prev, n);
+    double* f     = (double*)malloc(sizeof(double) * NF * (size_t)(n > 0 ? n : 1));
+    features_pass(p, di, pb, n, xsd, xd, pd, dom, cell_start, pair_id, f, NULL);
+    for (int64_t q = 0; q < NF * n; ++q) { features[q] = (float)f[q]; }
+    free(f);
+    free(pd);
+    free(xd);
+    free(xsd);
+    free(pb);
+    free(di);
+}
+
+/* Network restated from its parameter blob (layout in gpe.h); operands rounded to BF16 where the device
+ * feeds the tensor cores, everything else in FP64. */
+typedef struct {
+    double w1[NH][NF], b1[NH], w2[NH][NH], b2[NH], w3[NH], b3;
+    double mu[NF], isd[NF], ymu, ysd;
+    int rnd; /* 1: BF16 operand roundings of the device; 0: plain FP64 (for finite-difference checks) */
+} mlpnet;
+
+static double opr(const mlpnet* m, double v) { return m->rnd ? bf16r(v) : v; }
+
+static void mlp_load(const float* blob, mlpnet* m, int rnd)
+{
+    m->rnd = rnd;
+    for (int i = 0; i < NH; ++i) {
+        for (int f = 0; f < NF; ++f) { m->w1[i][f] = opr(m, blob[W1 + i * NF + f]); }
+        m->b1[i] = blob[B1 + i];
+        for (int q = 0; q < NH; ++q) { m->w2[i][q] = opr(m, blob[W2 + i * NH + q]); }
+        m->b2[i] = blob[B2 + i];
+        m->w3[i] = blob[W3 + i];
+    }
+    m->b3 = blob[B3];
+    for (int f = 0; f < NF; ++f) {
+        m->mu[f]        = blob[NW + f];
+        const float sd  = blob[NW + NF + f];
+        m->isd[f]       = sd > 0.f ? (double)(1.0f / sd) : 0.0;
+    }
+    m->ymu = blob[NW + 2 * NF];
+    m->ysd = blob[NW + 2 * NF + 1];
+}
+
+/* forward for one standardised-and-rounded input; returns y (standardised) and the layer values */
+static double mlp_fwd(const mlpnet* m, const double* xin, double xb[NF], double z1[NH], double a1b[NH],
+                      double z2[NH])
+{
+    for (int f = 0; f < NF; ++f) { xb[f] = opr(m, (xin[f] - m->mu[f]) * m->isd[f]); }
+    for (int i = 0; i < NH; ++i) {
+        double s = 0.0;
+        for (int f = 0; f < NF; ++f) { s += m->w1[i][f] * xb[f]; }
+        z1[i]  = s + m->b1[i];
+        a1b[i] = opr(m, z1[i] > 0.0 ? z1[i] : 0.0);
+    }
+    double y = m->b3;
+    for (int j = 0; j < NH; ++j) {
+        double s = 0.0;
+        for (int i = 0; i < NH; ++i) { s += m->w2[j][i] * a1b[i]; }
+        z2[j] = s + m->b2[j];
+        y += (z2[j] > 0.0 ? z2[j] : 0.0) * m->w3[j];
+    }
+    return y;
+}
+
+void orc_mlp_forward(const float* blob, int64_t n, const float* X, float* out, int32_t bf16)
+{
+    mlpnet* m = (mlpnet*)malloc(sizeof(mlpnet));
+    mlp_load(blob, m, bf16);
+#pragma omp parallel for schedule(static)
+    for (int64_t s = 0; s < n; ++s) {
+        double xin[NF], xb[NF], z1[NH], a1b[NH], z2[NH];
+        for (int f = 0; f < NF; ++f) { xin[f] = X[s * NF + f]; }
+        const double y = mlp_fwd(m, xin, xb, z1, a1b, z2);
+        out[s]         = (float)(y * m->ysd + m->ymu);
+    }
+    free(m);
+}
+
+void orc_mlp_gradient(const float* blob, int64_t n, const float* X, const float* T, double* grad, double* loss,
+                      int32_t bf16)
+{
+    mlpnet* m = (mlpnet*)malloc(sizeof(mlpnet));
+    mlp_load(blob, m, bf16);
+    memset(grad, 0, sizeof(double) * NW);
+    const double iysd = m->ysd > 0.0 ? (double)(1.0f / (float)m->ysd) : 0.0;
+    double L          = 0.0;
+    for (int64_t s = 0; s < n; ++s) {
+        double xin[NF], xb[NF], z1[NH], a1b[NH], z2[NH], dz2b[NH], dz1b[NH];
+        for (int f = 0; f < NF; ++f) { xin[f] = X[s * NF + f]; }
+        const double y  = mlp_fwd(m, xin, xb, z1, a1b, z2);
+        const double tn = ((double)T[s] - m->ymu) * iysd;
+        const double e  = y - tn;
+        const double dy = 2.0 * e / (double)n;
+        L += e * e;
+        for (int j = 0; j < NH; ++j) {
+            const double a2 = z2[j] > 0.0 ? z2[j] : 0.0;
+            grad[W3 + j] += dy * a2;
+            dz2b[j] = opr(m, z2[j] > 0.0 ? dy * m->w3[j] : 0.0);
+            grad[B2 + j] += dz2b[j];
+            for (int i = 0; i < NH; ++i) { grad[W2 + j * NH + i] += dz2b[j] * a1b[i]; }
+        }
+        grad[B3] += dy;
+        for (int i = 0; i < NH; ++i) {
+            double da = 0.0;
+            for (int j = 0; j < NH; ++j) { da += dz2b[j] * m->w2[j][i]; }
+            dz1b[i] = opr(m, z1[i] > 0.0 ? da : 0.0);
+            grad[B1 + i] += dz1b[i];
+            for (int f = 0; f < NF; ++f) { grad[W1 + i * NF + f] += dz1b[i] * xb[f]; }
+        }
+    }
+    *loss = n > 0 ? L / (double)n : 0.0;
+    free(m);
+}
+
+/* Warm-started steps (mode GPE_WARM_PREV / GPE_WARM_MLP) or cold steps that keep the summed multipliers
+ * (GPE_WARM_NONE). acc holds the previous step's sums in the current order and receives this step's sums
+ * in the new sorted order. blob is the network for GPE_WARM_MLP. */
+void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
+                       int32_t* dom, uint32_t* pair_id, float* acc, int32_t mode, const float* blob,
+                       int32_t n_steps)
+{
+    dinfo* di            = (dinfo*)malloc(sizeof(dinfo) * (size_t)nd);
+    build_dinfo(p, doms, nd, di);
+    const int64_t ncells = orc_pbf_num_cells(p, doms, nd);
+    const size_t nn      = (size_t)(n > 0 ? n : 1);
+    uint32_t* key        = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* perm       = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    uint32_t* cs         = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)ncells + 1));
+    float* xsort         = (float*)malloc(sizeof(float) * 2 * nn);
+    float* xssort        = (float*)malloc(sizeof(float) * 2 * nn);
+    int32_t* dsort       = (int32_t*)malloc(sizeof(int32_t) * nn);
+    double* xd           = (double*)malloc(sizeof(double) * 2 * nn);
+    double* xsa          = (double*)malloc(sizeof(double) * 2 * nn);
+    double* xsb          = (double*)malloc(sizeof(double) * 2 * nn);
+    double* lam          = (double*)malloc(sizeof(double) * nn);
+    double* sum          = (double*)malloc(sizeof(double) * nn);
+    double* prev         = (double*)malloc(sizeof(double) * nn);
+    double* feat         = (double*)malloc(sizeof(double) * NF * nn);
+    double* vd           = (double*)malloc(sizeof(double) * 2 * nn);
+    double* w            = (double*)malloc(sizeof(double) * nn);
+    uint32_t* pid_sorted = pair_id ? (uint32_t*)malloc(sizeof(uint32_t) * nn) : NULL;
+    mlpnet* net          = NULL;
+    if (mode == GPE_WARM_MLP) {
+        net = (mlpnet*)malloc(sizeof(mlpnet));
+        mlp_load(blob, net, 1);
+    }
+    for (int32_t s = 0; s < n_steps; ++s) {
+        orc_pbf_predict_sort(p, doms, nd, n, x, v, dom, key, perm, cs, xsort, xssort, dsort);
+        if (pair_id) {
+            for (int64_t i = 0; i < n; ++i) { pid_sorted[i] = pair_id[perm[i]]; }
+            memcpy(pair_id, pid_sorted, sizeof(uint32_t) * nn);
+        }
+        for (int64_t i = 0; i < n; ++i) { prev[i] = acc[perm[i]]; }
+        int64_t* pb = dom_pbase(di, nd, cs);
+        for (int64_t i = 0; i < 2 * n; ++i) {
+            xd[i]  = xsort[i];
+            xsa[i] = xssort[i];
+        }
+        for (int32_t it = 0; it < p->iters; ++it) {
+            if (it == 0) {
+                if (mode == GPE_WARM_MLP) {
+                    features_pass(p, di, pb, n, xsa, xd, prev, dsort, cs, pid_sorted, feat, NULL);
+#pragma omp parallel for schedule(static)
+                    for (int64_t i = 0; i < n; ++i) {
+                        double xb[NF], z1[NH], a1b[NH], z2[NH];
+                        const double y = mlp_fwd(net, &feat[i * NF], xb, z1, a1b, z2);
+                        const double l = prev[i] + (y * net->ysd + net->ymu);
+                        lam[i]         = l < 0.0 ? l : 0.0;
+                    }
+                } else if (mode == GPE_WARM_PREV) {
+                    memcpy(lam, prev, sizeof(double) * nn);
+                } else {
+                    lambda_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, lam, NULL);
+                }
+                memcpy(sum, lam, sizeof(double) * nn);
+            } else if (mode == GPE_WARM_PREV) {
+                lambda_proj_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, sum, lam);
+            } else {
+                lambda_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, lam, NULL);
+                for (int64_t i = 0; i < n; ++i) { sum[i] += lam[i]; }
+            }
+            delta_p_pass(p, di, n, xsa, dsort, cs, lam, xsb);
+            double* t = xsa;
+            xsa       = xsb;
+            xsb       = t;
+        }
+        xsph_pass(p, di, n, xd, xsa, dsort, cs, vd, w);
+        if (p->vort_eps != 0.f) { vorticity_pass(p, di, n, xsa, dsort, cs, w, vd); }
+        for (int64_t i = 0; i < 2 * n; ++i) {
+            x[i] = (float)xsa[i];
+            v[i] = (float)vd[i];
+        }
+        for (int64_t i = 0; i < n; ++i) { acc[i] = p->iters > 0 ? (float)sum[i] : 0.f; }
+        if (dom) {
+            for (int64_t i = 0; i < n; ++i) { dom[i] = dsort[i]; }
+        }
+        free(pb);
+    }
+    free(net);
+    free(pid_sorted);
+    free(w);
+    free(vd);
+    free(feat);
+    free(prev);
+    free(sum);
     free(lam);
     free(xsb);
     free(xsa);

@@ -50,6 +50,30 @@ void orc_pbf_density_error(const gpe_pbf_params* p, const gpe_domain* doms, int3
                            const float* x, const int32_t* dom, const uint32_t* cell_start, double* max_err,
                            double* mean_err);
 
+/* ---------- PBF warm start ---------- */
+/* The 12 warm-start features (gpe.h) of every sorted particle: xs = sorted x*, x = sorted x, prev = the
+ * previous step's summed multipliers in sorted order. features: n x 12. */
+void orc_pbf_features(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, const float* xs,
+                      const float* x, const float* prev, const int32_t* dom, const uint32_t* cell_start,
+                      const uint32_t* pair_id, float* features);
+/* The network from its blob (GPE_MLP_BLOB_FLOATS): out = de-standardised prediction of n raw feature rows.
+ * bf16 = 1 rounds the tensor-core operands (standardised features, W1, W2, hidden layer 1, and in the
+ * gradient dZ2 and dZ1) to BF16 as the device does; 0 computes in plain FP64. */
+void orc_mlp_forward(const float* blob, int64_t n, const float* X, float* out, int32_t bf16);
+/* Gradient (GPE_MLP_NUM_WEIGHTS) of mean((y - t_std)^2) over n pairs; loss receives that mean. */
+void orc_mlp_gradient(const float* blob, int64_t n, const float* X, const float* T, double* grad, double* loss,
+                      int32_t bf16);
+/* Steps that keep a per-particle multiplier memory (acc: in the current order in, in the new order out):
+ *   GPE_WARM_NONE  the plain step (a pair-collecting step); acc <- the sum of its iterations' lambdas
+ *   GPE_WARM_PREV  first delta-p pass with lambda_prev, later iterations update the sum by the unclamped
+ *                  lambda projected to <= 0 and apply the change; acc <- that sum
+ *   GPE_WARM_MLP   first delta-p pass with L = min(lambda_prev + r, 0), r from the network blob, later
+ *                  iterations plain; acc <- L plus the later iterations' lambdas
+ * Other arguments as orc_pbf_step. */
+void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
+                       int32_t* dom, uint32_t* pair_id, float* acc, int32_t mode, const float* blob,
+                       int32_t n_steps);
+
 /* ---------- MLS-MPM ---------- */
 /* grid: nx*ny*3 doubles (momentum x, momentum y, mass) */
 void orc_mpm_p2g(const gpe_mpm_params* p, int64_t n, const float* x, const float* v, const float* C,

@@ -36,6 +36,10 @@ def lib() -> C.CDLL:
         L.orc_pbf_step.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, i32, vp, vp]
         L.orc_pbf_density_error.argtypes = [pp, dp, i32, i64, vp, vp, vp, C.POINTER(C.c_double),
                                             C.POINTER(C.c_double)]
+        L.orc_pbf_features.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, vp, vp]
+        L.orc_mlp_forward.argtypes = [vp, i64, vp, vp, i32]
+        L.orc_mlp_gradient.argtypes = [vp, i64, vp, vp, vp, vp, i32]
+        L.orc_pbf_step_warm.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, i32, vp, i32]
         L.orc_mpm_p2g.argtypes = [mp, i64, vp, vp, vp, vp, vp, vp, vp]
         L.orc_mpm_grid_update.argtypes = [mp, vp]
         L.orc_mpm_g2p.argtypes = [mp, i64, vp, vp, vp, vp, vp, vp, vp]
@@ -132,6 +136,26 @@ class PbfOracle:
                            int(n_steps), _p(lam), _p(cs))
         return dict(x=x, v=v, dom=dom, lam=lam, cell_start=cs, pair_id=pid)
 
+    def features(self, xs, x, prev, dom, cs, pair_id=None):
+        xs = _c(xs, np.float32)
+        n = xs.shape[0]
+        f = np.empty((n, 12), np.float32)
+        lib().orc_pbf_features(C.byref(self.params), self.doms, self.nd, n, _p(xs), _p(_c(x, np.float32)),
+                               _p(_c(prev, np.float32)), _p(_c(dom, np.int32)), _p(_c(cs, np.uint32)),
+                               _p(_c(pair_id, np.uint32)), _p(f))
+        return f
+
+    def step_warm(self, x, v, acc, mode, blob=None, dom=None, n_steps=1, pair_id=None):
+        """Steps that keep the summed multipliers (mode 0 cold, 1 previous sum, 2 network blob)."""
+        x = np.array(x, dtype=np.float32, copy=True).reshape(-1, 2)
+        v = np.array(v, dtype=np.float32, copy=True).reshape(-1, 2)
+        acc = np.array(acc, dtype=np.float32, copy=True).reshape(-1)
+        dom = None if dom is None else np.array(dom, dtype=np.int32, copy=True)
+        pid = None if pair_id is None else np.array(pair_id, dtype=np.uint32, copy=True)
+        lib().orc_pbf_step_warm(C.byref(self.params), self.doms, self.nd, x.shape[0], _p(x), _p(v), _p(dom), _p(pid),
+                                _p(acc), int(mode), _p(_c(blob, np.float32)), int(n_steps))
+        return dict(x=x, v=v, acc=acc, dom=dom, pair_id=pid)
+
     def density_error(self, x, dom, cs):
         x = _c(x, np.float32)
         mx, mn = C.c_double(), C.c_double()
@@ -168,6 +192,23 @@ class MpmOracle:
         lib().orc_mpm_step(C.byref(self.params), x.shape[0], _p(x), _p(v), _p(Cm), _p(F), _p(J),
                            _p(_c(mat, np.int32)), int(n_steps))
         return x, v, Cm, F, J
+
+
+def mlp_forward(blob, X, bf16=True):
+    X = _c(X, np.float32).reshape(-1, 12)
+    out = np.empty(X.shape[0], np.float32)
+    lib().orc_mlp_forward(_p(_c(blob, np.float32)), X.shape[0], _p(X), _p(out), int(bool(bf16)))
+    return out
+
+
+def mlp_gradient(blob, X, T, bf16=True):
+    X = _c(X, np.float32).reshape(-1, 12)
+    T = _c(T, np.float32).reshape(-1)
+    g = np.empty(5057, np.float64)
+    loss = C.c_double()
+    lib().orc_mlp_gradient(_p(_c(blob, np.float32)), X.shape[0], _p(X), _p(T), _p(g), C.byref(loss),
+                           int(bool(bf16)))
+    return g, loss.value
 
 
 def num_threads() -> int:
