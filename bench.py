@@ -197,7 +197,15 @@ def learned_leg(args, stream, flush_l2):
 
     learned = timed(2, True)
     plain2 = timed(2, False)
-    learned.update({"plain_k2": plain2,
+    # the cheapest plain form that reaches the learned form's density error, for the equal-error comparison
+    plain_k = {}
+    for k in (6, 8, 12):
+        plain_k[f"k{k}"] = timed(k, False)
+    reach = [v for v in plain_k.values() if v["density_error"]["max"] <= max(learned["density_error"]["max"], 0.01)]
+    cheapest = min(reach, key=lambda v: v["ms_per_step"]) if reach else None
+    learned.update({"plain_k2": plain2, "plain_more_iters": plain_k,
+                    "speedup_vs_cheapest_plain_at_equal_error": (learned["value"] / cheapest["value"]) if cheapest
+                    else None,
                     "train": {"pairs": pairs, "train_loss": tl, "val_loss": vl, "collect_s": t_col, "train_s": t_tr,
                               "how": "pairs from 41 plain 20-iteration steps (every 20th particle), 30 epochs, "
                                      "batch 8192, AdamW lr 2e-3, standardised MSE"}})

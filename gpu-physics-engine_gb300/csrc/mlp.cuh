@@ -158,6 +158,17 @@ __device__ __forceinline__ uint32_t lane_addr(uint32_t base, uint32_t col)
     return base + ((uint32_t)((threadIdx.x >> 5) * 32u) << 16) + col;
 }
 
+// Bulk copy (the TMA engine, untiled) of `bytes` from global to this CTA's shared memory; completion is
+// signalled on the mbarrier as transaction bytes. Both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
 {
     const __nv_bfloat162 h = __floats2bfloat162_rn(a, b); // a -> low half (lower address)
@@ -168,15 +179,18 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
 
 // ----- inference: the forward pass over one tile --------------------------------------------------------
 struct __align__(128) MlpFwdSmem {
-    uint16_t a1[MLP_TILE * MLP_FP]; // layer-1 A: standardised features
-    uint16_t a2[MLP_TILE * MLP_H];  // layer-2 A: hidden layer 1
+    uint16_t a1[2][MLP_TILE * MLP_FP]; // layer-1 A: standardised features (two buffers for streamed tiles)
+    uint16_t a2[MLP_TILE * MLP_H];     // layer-2 A: hidden layer 1
     uint16_t w1[MLP_H * MLP_FP];
     uint16_t w2[MLP_H * MLP_H];
     float b1[MLP_H], b2[MLP_H], w3[MLP_H], mu[MLP_FP], isd[MLP_FP];
     float b3;
-    uint64_t bar;
+    uint64_t bar;      // tensor-core completion
+    uint64_t ldbar[2]; // bulk-copy completion of a1[0], a1[1]
     uint32_t tmem;
 };
+// Bytes of one streamed layer-1 tile (128 rows x 16 BF16 in the K-major layout)
+constexpr uint32_t MLP_A1_TILE_BYTES = MLP_TILE * MLP_FP * 2;
 constexpr uint32_t MLP_FWD_TMEM_COLS = 64;
 
 // All 128 threads: stage the weights, set up the barrier, allocate TMEM.
@@ -201,6 +215,8 @@ __device__ __forceinline__ void mlp_fwd_setup(MlpFwdSmem& S, const MlpDev* __res
     if (t == 0) {
         S.b3 = m->b3;
         tc::mbar_init(&S.bar, 1);
+        tc::mbar_init(&S.ldbar[0], 1);
+        tc::mbar_init(&S.ldbar[1], 1);
     }
     if (t < 32) { tc::tmem_alloc(&S.tmem, MLP_FWD_TMEM_COLS); }
     tc::fence_async_smem();
@@ -219,33 +235,49 @@ __device__ __forceinline__ void mlp_fwd_teardown(MlpFwdSmem& S)
     }
 }
 
+// The standardised features of one row as its two 16-byte chunks of the layer-1 A tile (k = 0..7, 8..15).
+__device__ __forceinline__ void mlp_pack_row(const float (&f)[MLP_F], const float* mu, const float* isd, uint4& c0,
+                                             uint4& c1)
+{
+    float z[MLP_FP];
+#pragma unroll
+    for (int q = 0; q < MLP_FP; ++q) { z[q] = q < MLP_F ? (f[q < MLP_F ? q : 0] - mu[q]) * isd[q] : 0.f; }
+    c0.x = tc::pack_bf16(z[0], z[1]);
+    c0.y = tc::pack_bf16(z[2], z[3]);
+    c0.z = tc::pack_bf16(z[4], z[5]);
+    c0.w = tc::pack_bf16(z[6], z[7]);
+    c1.x = tc::pack_bf16(z[8], z[9]);
+    c1.y = tc::pack_bf16(z[10], z[11]);
+    c1.z = tc::pack_bf16(z[12], z[13]);
+    c1.w = tc::pack_bf16(z[14], z[15]);
+}
+
+__device__ __forceinline__ float mlp_fwd_core(MlpFwdSmem& S, int buf, uint32_t& phase, bool& ok);
+
 // Every thread of the CTA: the standardised network output for this thread's features f (any values for
 // rows without a sample). `phase` is the barrier parity, flipped per wait; `ok` turns false on a timeout.
 __device__ __forceinline__ float mlp_fwd_tile(MlpFwdSmem& S, const float (&f)[MLP_F], uint32_t& phase, bool& ok)
 {
     const uint32_t r = threadIdx.x;
-    constexpr uint32_t ID = tc::idesc_bf16(128, 64);
-    // layer-1 A row: 16 BF16 = two 16-byte chunks (k = 0..7, 8..15)
-    {
-        float z[MLP_FP];
-#pragma unroll
-        for (int q = 0; q < MLP_FP; ++q) { z[q] = q < MLP_F ? (f[q < MLP_F ? q : 0] - S.mu[q]) * S.isd[q] : 0.f; }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            uint4 u;
-            u.x = tc::pack_bf16(z[8 * c + 0], z[8 * c + 1]);
-            u.y = tc::pack_bf16(z[8 * c + 2], z[8 * c + 3]);
-            u.z = tc::pack_bf16(z[8 * c + 4], z[8 * c + 5]);
-            u.w = tc::pack_bf16(z[8 * c + 6], z[8 * c + 7]);
-            *reinterpret_cast<uint4*>(&S.a1[kmajor(r, 8 * c, MLP_FP)]) = u;
-        }
-    }
+    uint4 c0, c1;
+    mlp_pack_row(f, S.mu, S.isd, c0, c1);
+    *reinterpret_cast<uint4*>(&S.a1[0][kmajor(r, 0, MLP_FP)]) = c0;
+    *reinterpret_cast<uint4*>(&S.a1[0][kmajor(r, 8, MLP_FP)]) = c1;
     tc::fence_async_smem();
     __syncthreads();
+    return mlp_fwd_core(S, 0, phase, ok);
+}
+
+// The two layers from a layer-1 tile already in S.a1[buf] (written and fenced, or landed by a bulk copy whose
+// barrier every thread has passed).
+__device__ __forceinline__ float mlp_fwd_core(MlpFwdSmem& S, int buf, uint32_t& phase, bool& ok)
+{
+    const uint32_t r = threadIdx.x;
+    constexpr uint32_t ID = tc::idesc_bf16(128, 64);
     if (r == 0) {
         tc::fence_after();
-        tc::mma(S.tmem, tc::sdesc(tc::saddr(S.a1), 128, MLP_FP * 16), tc::sdesc(tc::saddr(S.w1), 128, MLP_FP * 16),
-                ID, 0u);
+        tc::mma(S.tmem, tc::sdesc(tc::saddr(S.a1[buf]), 128, MLP_FP * 16),
+                tc::sdesc(tc::saddr(S.w1), 128, MLP_FP * 16), ID, 0u);
         tc::commit(&S.bar);
     }
     ok = tc::mbar_wait(&S.bar, phase) && ok;

@@ -416,14 +416,43 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
     return lam;
 }
 
-// First lambda pass of a GPE_WARM_MLP step: features, then the network on the tensor cores for a tile of
-// 128 particles per iteration of a persistent loop; lambda = lambda_prev + r.
+// First lambda pass of a GPE_WARM_MLP step, part 1: the features at full occupancy (one thread per
+// particle), standardised and rounded to BF16, written as the network's layer-1 A operand: tile t of 128
+// particles is 4 KB at feat + t * 2048 in the tensor cores' K-major layout, so part 2 moves it to shared
+// memory with one bulk copy. (Computing the features inside the tensor-core kernel caps the neighbour loop
+// at the 7 CTAs of 4 warps that fit an SM beside their TMEM and operand tiles: 126 us against about 50 us
+// here at 1M particles.)
 template <bool MULTI, bool SELFG>
+__global__ void __launch_bounds__(T_PART)
+    k_lambda_feat(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                  const uint32_t* __restrict__ start, const float2* __restrict__ xs,
+                  const float2* __restrict__ xsorted, const float* __restrict__ prev,
+                  const uint32_t* __restrict__ pair_id, const MlpDev* __restrict__ mlp, uint16_t* __restrict__ feat)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count_of(k)) { return; }
+    const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
+    const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
+    float f[MLP_F];
+    (void)warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    float mu[MLP_FP], isd[MLP_FP];
+#pragma unroll
+    for (int q = 0; q < MLP_FP; ++q) {
+        mu[q]  = __ldg(&mlp->mu[q]);
+        isd[q] = __ldg(&mlp->isd[q]);
+    }
+    uint4 c0, c1;
+    mlp_pack_row(f, mu, isd, c0, c1);
+    uint16_t* tile                                              = feat + (size_t)(i >> 7) * (MLP_TILE * MLP_FP);
+    *reinterpret_cast<uint4*>(&tile[kmajor(i & 127, 0, MLP_FP)]) = c0;
+    *reinterpret_cast<uint4*>(&tile[kmajor(i & 127, 8, MLP_FP)]) = c1;
+}
+
+// Part 2: the network on the tensor cores, persistent over tiles; each tile's operand arrives by a bulk
+// copy issued one tile ahead into the other buffer. lambda = min(lambda_prev + r, 0).
 __global__ void __launch_bounds__(MLP_TILE)
-    k_lambda_mlp(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                 const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float2* __restrict__ xsorted,
-                 const float* __restrict__ prev, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
-                 const MlpDev* __restrict__ mlp, uint32_t* __restrict__ status)
+    k_mlp_apply(const PbfK k, const uint16_t* __restrict__ feat, const float* __restrict__ prev, float* __restrict__ lam,
+                const MlpDev* __restrict__ mlp, uint32_t* __restrict__ status)
 {
     __shared__ MlpFwdSmem S;
     const int32_t n      = count_of(k);
@@ -431,21 +460,24 @@ __global__ void __launch_bounds__(MLP_TILE)
     if ((int32_t)blockIdx.x >= ntiles) { return; } // uniform over the CTA, before any barrier
     mlp_fwd_setup(S, mlp);
     const float ymu = mlp->ymu, ysd = mlp->ysd;
-    uint32_t phase  = 0;
-    bool ok         = true;
-    for (int32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int32_t i  = tile * MLP_TILE + (int32_t)threadIdx.x;
-        const bool valid = i < n;
-        float f[MLP_F];
-#pragma unroll
-        for (int q = 0; q < MLP_F; ++q) { f[q] = 0.f; }
-        if (valid) {
-            const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
-            const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
-            warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    uint32_t phase = 0, ldph[2] = {0u, 0u};
+    bool ok        = true;
+    if (threadIdx.x == 0) {
+        tc::bulk_g2s(S.a1[0], feat + (size_t)blockIdx.x * (MLP_TILE * MLP_FP), MLP_A1_TILE_BYTES, &S.ldbar[0]);
+    }
+    int b = 0;
+    for (int32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, b ^= 1) {
+        const int32_t next = tile + (int32_t)gridDim.x;
+        if (threadIdx.x == 0 && next < ntiles) {
+            // the other buffer was read by the previous tile's MMA, which has completed
+            tc::bulk_g2s(S.a1[b ^ 1], feat + (size_t)next * (MLP_TILE * MLP_FP), MLP_A1_TILE_BYTES, &S.ldbar[b ^ 1]);
         }
-        const float y = mlp_fwd_tile(S, f, phase, ok);
-        if (valid) { lam[i] = fminf(f[1] + fmaf(y, ysd, ymu), 0.f); } // a summed multiplier only pushes
+        ok = tc::mbar_wait(&S.ldbar[b], ldph[b]) && ok;
+        ldph[b] ^= 1u;
+        __syncthreads(); // every thread has read the previous tile's accumulators before the MMA overwrites them
+        const float y   = mlp_fwd_core(S, b, phase, ok);
+        const int32_t i = tile * MLP_TILE + (int32_t)threadIdx.x;
+        if (i < n) { lam[i] = fminf(__ldg(&prev[i]) + fmaf(y, ysd, ymu), 0.f); } // a summed multiplier only pushes
     }
     if (!ok) { atomicOr(status, GPE_STATUS_TIMEOUT); }
     mlp_fwd_teardown(S);
@@ -789,7 +821,8 @@ struct gpe_pbf {
     CollectK col{};
     bool pending_accinit = false; // stage API: the next DELTA_P starts the running sum
     bool mem_valid    = false;    // the multiplier memory holds a previous step's sums (else it is 0)
-    int32_t lam_grid  = 0;        // persistent grid of k_lambda_mlp
+    int32_t lam_grid  = 0;        // persistent grid of k_mlp_apply
+    uint16_t* feat    = nullptr;  // network operand tiles (GPE_WARM_MLP), allocated on demand
 
     // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
     int X = 0, SX = -1, XS = -1, XO = -1;
@@ -998,18 +1031,17 @@ const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, fa
                            {{dp_launch<true, false, false>, dp_launch<true, false, true>},
                             {dp_launch<true, true, false>, dp_launch<true, true, true>}}};
 
-using WarmFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                        const float2*, const float2*, const float*, float*, const uint32_t*, const MlpDev*,
-                        uint32_t*);
+using FeatFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+                        const float2*, const float2*, const float*, const uint32_t*, const MlpDev*, uint16_t*);
 template <bool M, bool S>
-void mlp_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                const uint32_t* start, const float2* xs, const float2* xo, const float* prev, float* lam,
-                const uint32_t* pid, const MlpDev* mlp, uint32_t* status)
+void feat_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+                 const uint32_t* start, const float2* xs, const float2* xo, const float* prev, const uint32_t* pid,
+                 const MlpDev* mlp, uint16_t* feat)
 {
-    k_lambda_mlp<M, S><<<g, MLP_TILE, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, mlp, status);
+    k_lambda_feat<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
 }
-const WarmFn kMlp[2][2] = {{mlp_launch<false, false>, mlp_launch<false, true>},
-                           {mlp_launch<true, false>, mlp_launch<true, true>}};
+const FeatFn kFeat[2][2] = {{feat_launch<false, false>, feat_launch<false, true>},
+                            {feat_launch<true, false>, feat_launch<true, true>}};
 
 using ColFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                        const float2*, const float2*, const float*, float*, const uint32_t*, const CollectK&);
@@ -1037,7 +1069,9 @@ const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
 // accumulation mode of the lambda passes after the first in the engine's current mode
 int acc_mode(const gpe_pbf* s)
 {
-    if (s->collecting || s->warm == GPE_WARM_MLP) { return ACC_SUM; }
+    // a network step keeps its own Lambda as the memory; only the step that starts the memory (a plain
+    // step with the training solve's iterations) and collection sum their iterations
+    if (s->collecting || (s->warm == GPE_WARM_MLP && !s->mem_valid)) { return ACC_SUM; }
     return s->warm == GPE_WARM_PREV ? ACC_PROJ : ACC_NONE;
 }
 
@@ -1064,11 +1098,15 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
     const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
     if (s->warm == GPE_WARM_MLP && s->mem_valid && !s->collecting) {
+        const gpe::MlpDev* md = gpe::mlp_device(s->mlp);
+        kFeat[mi][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
+                      s->prev, pid, md, s->feat);
+        GPE_CHECK_LAUNCH("k_lambda_feat");
         const int64_t tiles = (lsize(s) + MLP_TILE - 1) / MLP_TILE;
         const unsigned g    = (unsigned)std::min<int64_t>(tiles, s->lam_grid);
-        kMlp[mi][sg](g, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX], s->prev, s->lam, pid,
-                     gpe::mlp_device(s->mlp), s->status);
-        GPE_CHECK_LAUNCH("k_lambda_mlp");
+        k_mlp_apply<<<g, MLP_TILE, 0, st>>>(s->k, s->feat, s->prev, s->lam, md, s->status);
+        GPE_CHECK_LAUNCH("k_mlp_apply");
+        s->launches += 1;
     } else {
         kCol[mi][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
                      s->prev, s->lam, pid, s->col);
@@ -1269,6 +1307,7 @@ int32_t gpe_pbf_destroy(gpe_pbf* s)
     if (!s) { return GPE_ERR_BAD_ARG; }
     s->drop_graphs();
     if (s->base) { cudaFree(s->base); }
+    if (s->feat) { cudaFree(s->feat); }
     delete s;
     return GPE_OK;
 }
@@ -1644,8 +1683,10 @@ int32_t gpe_pbf_status(gpe_pbf* s, uint32_t* status, void* stream)
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
 {
     if (!s || !launches) { return GPE_ERR_BAD_ARG; }
-    const bool skip_first = s->warm == GPE_WARM_PREV && s->prm.iters > 0; // lambda_prev is placed by the sort
-    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0) - (skip_first ? 1 : 0);
+    const bool warm = s->prm.iters > 0;
+    // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network
+    const int32_t first = (warm && s->warm == GPE_WARM_PREV) ? -1 : ((warm && s->warm == GPE_WARM_MLP) ? 1 : 0);
+    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0) + first;
     return GPE_OK;
 }
 
@@ -1748,19 +1789,18 @@ extern "C" int32_t gpe_pbf_set_warm_start(gpe_pbf* s, int32_t mode, const gpe_ml
     }
     if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
     if (mode == GPE_WARM_MLP) {
-        // persistent grid: every CTA resident at once (each holds 64 TMEM columns of the SM's 512)
-        // the kernel's tiles live in shared memory: prefer the largest carveout so that 7 CTAs fit per SM
-        const void* fns[4] = {reinterpret_cast<const void*>(k_lambda_mlp<false, false>),
-                              reinterpret_cast<const void*>(k_lambda_mlp<false, true>),
-                              reinterpret_cast<const void*>(k_lambda_mlp<true, false>),
-                              reinterpret_cast<const void*>(k_lambda_mlp<true, true>)};
-        for (const void* f : fns) {
-            GPE_TRY_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                              (int)cudaSharedmemCarveoutMaxShared));
-        }
-        // grid: as many CTAs per SM as TMEM holds (512 columns / 64); CTAs beyond those resident queue,
-        // and no CTA can wait for TMEM
+        // the network kernel's tiles live in shared memory: prefer the largest carveout so that 6 CTAs fit
+        GPE_TRY_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k_mlp_apply),
+                                          cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared));
+        // persistent grid: as many CTAs per SM as TMEM holds (512 columns / 64); CTAs beyond those resident
+        // queue, and no CTA can wait for TMEM
         s->lam_grid = (int32_t)(512 / MLP_FWD_TMEM_COLS) * gpe::sm_count();
+        if (!s->feat) {
+            // layer-1 operand tiles of the network, 32 B per particle, whole tiles
+            const size_t tiles = (size_t)((s->cap + MLP_TILE - 1) / MLP_TILE);
+            GPE_TRY_CUDA(cudaMalloc(&s->feat, (tiles > 0 ? tiles : 1) * MLP_A1_TILE_BYTES));
+        }
     }
     s->warm = mode;
     s->mlp  = mode == GPE_WARM_MLP ? mlp : nullptr;

@@ -980,7 +980,9 @@ void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t 
                 lambda_proj_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, sum, lam);
             } else {
                 lambda_pass(p, di, pb, n, xsa, dsort, cs, pid_sorted, lam, NULL);
-                for (int64_t i = 0; i < n; ++i) { sum[i] += lam[i]; }
+                if (mode == GPE_WARM_NONE) {
+                    for (int64_t i = 0; i < n; ++i) { sum[i] += lam[i]; }
+                }
             }
             delta_p_pass(p, di, n, xsa, dsort, cs, lam, xsb);
             double* t = xsa;

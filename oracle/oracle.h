@@ -68,7 +68,7 @@ void orc_mlp_gradient(const float* blob, int64_t n, const float* X, const float*
  *   GPE_WARM_PREV  first delta-p pass with lambda_prev, later iterations update the sum by the unclamped
  *                  lambda projected to <= 0 and apply the change; acc <- that sum
  *   GPE_WARM_MLP   first delta-p pass with L = min(lambda_prev + r, 0), r from the network blob, later
- *                  iterations plain; acc <- L plus the later iterations' lambdas
+ *                  iterations plain; acc <- L
  * Other arguments as orc_pbf_step. */
 void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd, int64_t n, float* x, float* v,
                        int32_t* dom, uint32_t* pair_id, float* acc, int32_t mode, const float* blob,
