@@ -46,6 +46,12 @@ ALG_BYTES = {  # algorithmic bytes per particle per launch (FP32 SoA, each field
 }
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the 1M-particle step's neighbour
+# kernels from one ncu capture (profiles/pbf_k_lambda_k_delta_p_1m.md); below the algorithmic bytes because
+# the outputs stay in L2 for the next kernel
+NCU_TRAFFIC = {"lambda": 9.532416e6, "delta_p": 13.72416e6}
+
+
 def peaks():
     try:
         d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -288,6 +294,54 @@ def reference_cuda_leg(args, stream, flush_l2):
                    "same scene and constants, L2 flushed before each timed substep"}
 
 
+def mpm_leg(args, stream, flush_l2):
+    """MLS-MPM, timed like the headline (graph-launched steps, L2 flushed before each):
+    mixed: 4,194,304 particles (a third each of water, snow and jelly in seeded discs) on a 1024^2 grid,
+           dt = 5e-5, spatial re-sort every 16 steps; algorithmic bytes 136 per particle (x, v, C, F, J,
+           material and plastic state read and written once) plus 64 per grid node;
+    elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid, dt = 1e-4 (launch-bound)."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+
+    sh = stream.cuda_stream
+    peak, _ = peaks()
+
+    def timed(p, pos, vel, mat, alg_bytes):
+        n = len(pos)
+        e = gpe.Mpm(p, capacity=n)
+        e.set_state(pos, vel, material=mat, stream=sh)
+        for _ in range(args.warmup):
+            e.step(1, stream=sh)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            flush_l2()
+            a.record(stream)
+            e.step(1, stream=sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+        s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        st = e.status()
+        launches = e.launches_per_step()
+        e.close()
+        gbs = alg_bytes * args.steps / s / 1e9
+        return {"particles": n, "value": n * args.steps / s, "unit": "particle-steps/s",
+                "ms_per_step": 1e3 * s / args.steps, "alg_bytes_per_step": alg_bytes, "effective_gbs": gbs,
+                "hbm_frac": gbs / peak, "launches_per_step": launches, "status": st}
+
+    out = {}
+    n = 4194304
+    p = scenes.mixed_params(n)
+    pos, mat = scenes.mixed_discs(n)
+    out["mixed_4m"] = timed(p, pos, np.zeros_like(pos), mat, 136.0 * n + 64.0 * p.nx * p.ny)
+    pe = scenes.elastic_params()
+    pos, vel = scenes.two_squares()
+    out["elastic_65k"] = timed(pe, pos, vel, None, 120.0 * len(pos) + 64.0 * pe.nx * pe.ny)
+    return out
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return
@@ -393,7 +447,7 @@ def run_gpe(args, rank, ws):
     roofline = {"bound": "hbm", "kernel": {"lambda": "k_lambda", "delta_p": "k_delta_p", "xsph": "k_xsph",
                                            "predict_sort": "sort group"}[dom_name],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind, "traffic": None,
+                "peak_source": peak_kind, "traffic": NCU_TRAFFIC.get(dom_name),
                 "alg_bytes_per_launch": ALG_BYTES[dom_name] * n, "launch_ms": per_launch_ms,
                 "share": {k: v / tot for k, v in share.items()},
                 "stage_ms_per_step": {k: statistics.mean(v) for k, v in stage_ms.items()}}
@@ -430,6 +484,12 @@ def run_gpe(args, rank, ws):
                                  "speedup_ge_2x": learned["speedup_vs_plain_k4"] >= 2.0}
         except Exception as exc:  # reported, never fatal to the headline number
             learned = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
+    mpm = None
+    if ws == 1 and not args.no_mpm:
+        try:
+            mpm = mpm_leg(args, stream, flush_l2)
+        except Exception as exc:  # reported, never fatal to the headline number
+            mpm = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
     ref_cuda = None
     if ws == 1 and not args.no_reference_cuda:
         try:
@@ -444,7 +504,7 @@ def run_gpe(args, rank, ws):
             "gpu_launches": launches * args.steps, "launches_per_step": launches,
             "hbm_effective_gbs": 212.0 * value / ws / 1e9,
             "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary(),
-            "learned": learned, "reference_cuda": ref_cuda}
+            "learned": learned, "mpm": mpm, "reference_cuda": ref_cuda}
     print(json.dumps(line), flush=True)
 
 
@@ -457,6 +517,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-mpm", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -598,6 +598,7 @@ struct MpmGraph {
     cudaGraphExec_t exec = nullptr;
     int ga_end;
     int cur_end;
+    int32_t launches = 0; // kernel launches per step of the captured sequence (rounded up)
 };
 
 struct gpe_mpm {
@@ -1055,6 +1056,7 @@ int32_t gpe_mpm_step(gpe_mpm* s, int32_t n_steps, void* stream)
         cudaGraph_t graph    = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(cap_st, &graph);
         MpmGraph g;
+        g.launches = (s->launches + n_steps - 1) / n_steps;
         g.ga_end  = s->ga;
         g.cur_end = s->cur;
         s->ga     = ga0;
@@ -1076,8 +1078,9 @@ int32_t gpe_mpm_step(gpe_mpm* s, int32_t n_steps, void* stream)
         it = s->graphs.emplace(key, g).first;
     }
     GPE_TRY_CUDA(cudaGraphLaunch(it->second.exec, st));
-    s->ga  = it->second.ga_end;
-    s->cur = it->second.cur_end;
+    s->ga       = it->second.ga_end;
+    s->cur      = it->second.cur_end;
+    s->launches = it->second.launches;
     s->steps_since_sort = do_sort ? n_steps : s->steps_since_sort + n_steps;
     return GPE_OK;
 }
@@ -1128,7 +1131,7 @@ int32_t gpe_mpm_status(gpe_mpm* s, uint32_t* status, void* stream)
 int32_t gpe_mpm_launches_per_step(const gpe_mpm* s, int32_t* launches)
 {
     if (!s || !launches) { return GPE_ERR_BAD_ARG; }
-    *launches = 1;
+    *launches = s->launches; // of the last gpe_mpm_step, per step
     return GPE_OK;
 }
 

@@ -513,6 +513,11 @@ class Mpm:
     def enqueue(self, n_steps: int, stream=None) -> None:
         check(lib().gpe_mpm_enqueue(self.h, int(n_steps), stream), "gpe_mpm_enqueue")
 
+    def launches_per_step(self) -> int:
+        v = C.c_int32()
+        check(lib().gpe_mpm_launches_per_step(self.h, C.byref(v)), "gpe_mpm_launches_per_step")
+        return v.value
+
     def buffers(self) -> dict:
         ptrs = [C.c_void_p() for _ in range(6)]
         check(lib().gpe_mpm_buffers(self.h, *[C.byref(p) for p in ptrs]), "gpe_mpm_buffers")

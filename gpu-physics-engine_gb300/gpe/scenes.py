@@ -295,8 +295,10 @@ def mixed_params(n: int, grid: int = 1024) -> MpmParams:
     p.p_min = -1e30
     p.p_max = 1e30
     p.flags = MPM_FLAG_PER_PARTICLE_MATERIAL
-    p.mass = 1.0 / n
+    # density 1000: the jelly's wave speed sqrt(E / rho) is then 2.2 m/s and dt c / dx = 0.12 on the 1024^2
+    # grid (at density 3.3, 1 / n per particle, it is 2.0 and the step diverges)
     p.vol0 = 0.3 / n
+    p.mass = 1000.0 * p.vol0
     p.sort_interval = 16
     return p
 
