@@ -319,16 +319,26 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
         }
         __syncthreads();
         if (valid) {
+            // Particles of one cell (a dozen or more, consecutive after the spatial sort) share their 9 nodes;
+            // visiting the nodes in the same order would make their shared-memory atomics collide on one
+            // address at a time. Each lane starts at node (lane mod 9), so concurrent lanes of a cell mostly
+            // hit different nodes.
+            const int rot = (int)(threadIdx.x % 9u);
 #pragma unroll
-            for (int i = 0; i < 3; ++i) {
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const float4 c = node_contrib(k, s, v, Q, i, j);
-                    const int t    = (s.by + j - ty0) * tw + (s.bx + i - tx0);
-                    atomicAdd(&s_x[t], c.x);
-                    atomicAdd(&s_y[t], c.y);
-                    atomicAdd(&s_m[t], c.z);
-                }
+            for (int q = 0; q < 9; ++q) {
+                const int nd   = (q + rot) >= 9 ? q + rot - 9 : q + rot;
+                const int i    = nd % 3, j = nd / 3;
+                const float wx = i == 0 ? s.wx[0] : (i == 1 ? s.wx[1] : s.wx[2]);
+                const float wy = j == 0 ? s.wy[0] : (j == 1 ? s.wy[1] : s.wy[2]);
+                const float w   = wx * wy;
+                const float dpx = ((float)i - s.fx) * k.dx;
+                const float dpy = ((float)j - s.fy) * k.dx;
+                const float ax  = dpx * Q.x + dpy * Q.y;
+                const float ay  = dpx * Q.z + dpy * Q.w;
+                const int t     = (s.by + j - ty0) * tw + (s.bx + i - tx0);
+                atomicAdd(&s_x[t], w * (v.x * k.mass + ax));
+                atomicAdd(&s_y[t], w * (v.y * k.mass + ay));
+                atomicAdd(&s_m[t], w * k.mass);
             }
         }
         __syncthreads();
