@@ -294,6 +294,50 @@ def reference_cuda_leg(args, stream, flush_l2):
                    "same scene and constants, L2 flushed before each timed substep"}
 
 
+def batched_leg(args, stream, flush_l2):
+    """Batched PBF: 256 independent dam-break scenes, particle counts log-uniform in [2048, 65536] (seed 3),
+    box aspect U(0.5, 2), C0 physics at dt = 1/480, 4 iterations, all scenes in one engine; timed with the
+    default tuning and with the autotuner's choice (cell size, block size, persistent solve)."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+
+    sh = stream.cuda_stream
+    p = scenes.dam_params(iters=4)
+    p.dt = 1.0 / 480.0
+    pos, vel, dom, boxes = scenes.batched_scenes(n_scenes=256, seed=3, lo=2048, hi=65536)
+    n = len(pos)
+    e = gpe.Pbf(p, boxes, capacity=n)
+
+    def timed():
+        e.set_state(pos, vel, dom, stream=sh)
+        for _ in range(args.warmup):
+            e.step(1, stream=sh)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            flush_l2()
+            a.record(stream)
+            e.step(1, stream=sh)
+            b.record(stream)
+        torch.cuda.synchronize()
+        s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        return {"value": n * args.steps / s, "ms_per_step": 1e3 * s / args.steps, "status": e.status()}
+
+    default = timed()
+    e.set_state(pos, vel, dom, stream=sh)
+    t0 = time.perf_counter()
+    best, trial_ms = e.autotune(trial_steps=4, stream=sh)
+    tune_s = time.perf_counter() - t0
+    tuned = timed()
+    e.close()
+    return {"workload": "pbf_batched_256_scenes", "scenes": 256, "particles": n, "unit": "particle-steps/s",
+            "default": default, "tuned": tuned,
+            "tuning": {"cell_over_h": best.cell / p.h, "block": best.block, "persistent": bool(best.persistent),
+                       "trial_ms_per_step": trial_ms, "autotune_s": tune_s}}
+
+
 def mpm_leg(args, stream, flush_l2):
     """MLS-MPM, timed like the headline (graph-launched steps, L2 flushed before each):
     mixed: 4,194,304 particles (a third each of water, snow and jelly in seeded discs) on a 1024^2 grid,
@@ -484,6 +528,12 @@ def run_gpe(args, rank, ws):
                                  "speedup_ge_2x": learned["speedup_vs_plain_k4"] >= 2.0}
         except Exception as exc:  # reported, never fatal to the headline number
             learned = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
+    batched = None
+    if ws == 1 and not args.no_batched:
+        try:
+            batched = batched_leg(args, stream, flush_l2)
+        except Exception as exc:  # reported, never fatal to the headline number
+            batched = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
     mpm = None
     if ws == 1 and not args.no_mpm:
         try:
@@ -504,7 +554,7 @@ def run_gpe(args, rank, ws):
             "gpu_launches": launches * args.steps, "launches_per_step": launches,
             "hbm_effective_gbs": 212.0 * value / ws / 1e9,
             "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary(),
-            "learned": learned, "mpm": mpm, "reference_cuda": ref_cuda}
+            "learned": learned, "batched": batched, "mpm": mpm, "reference_cuda": ref_cuda}
     print(json.dumps(line), flush=True)
 
 
@@ -518,6 +568,7 @@ def main():
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-mpm", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -56,6 +56,7 @@ struct PbfK {
 namespace {
 
 constexpr int T_PART = 256; // threads per block for the per-particle kernels
+constexpr int T_MAX  = 512; // the largest block the neighbour kernels are launched with (a tuning choice)
 
 // particle count of a launch: the device counter when there is one (the reference keeps num_atoms on the
 // device too, cuda-engine.h:133), else the value passed by the host
@@ -102,6 +103,18 @@ __device__ __forceinline__ void for_neighbours(const DomDev& d, const PbfK& k, c
     }
 }
 
+
+// A neighbour's value. Separate launches read through the read-only cache; inside the persistent solve
+// (CG) another block may have rewritten the value since this SM last cached it, so it is read from L2.
+template <bool CG, class T>
+__device__ __forceinline__ T ldn(const T* p)
+{
+    if constexpr (CG) {
+        return __ldcg(p);
+    } else {
+        return __ldg(p);
+    }
+}
 
 // integer mixer of the reference (hash, cuda-internal.cuh:19-27)
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
@@ -203,14 +216,12 @@ __global__ void __launch_bounds__(T_PART)
 //           unclamped, and the pass moves the particles by the change of L; a sum that overshot is relaxed
 //           again and L never turns into a pull (accumulated-multiplier clamping).
 enum { ACC_NONE = 0, ACC_SUM = 1, ACC_PROJ = 2 };
-template <bool MULTI, bool SELFG, int ACC>
-__global__ void __launch_bounds__(T_PART)
-    k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
-             const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
+template <bool MULTI, bool SELFG, int ACC, bool CG = false>
+__device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                           const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
+                                           const float2* __restrict__ xs, float* __restrict__ lam,
+                                           const uint32_t* __restrict__ pair_id, float* __restrict__ acc, int32_t i)
 {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     const float2 p       = xs[i];
@@ -224,9 +235,9 @@ __global__ void __launch_bounds__(T_PART)
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q  = __ldg(&xs[j]);
+        const float2 q  = ldn<CG>(&xs[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = rx * rx + ry * ry;
+        const float r2  = fmaf(rx, rx, ry * ry);
         const bool self = j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
@@ -284,16 +295,24 @@ __global__ void __launch_bounds__(T_PART)
     }
 }
 
-// ----- delta p with artificial pressure and over-relaxation, then walls (PBF.cu:398-447, 471-499) -------
-// ACCINIT: this pass applies the warm start; its multiplier starts the step's running sum.
-template <bool MULTI, bool SCORR, bool ACCINIT>
-__global__ void __launch_bounds__(T_PART)
-    k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-              const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
-              float2* __restrict__ xs_out, float* __restrict__ acc)
+template <bool MULTI, bool SELFG, int ACC>
+__global__ void __launch_bounds__(T_MAX)
+    k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
+             const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
+    if (i < count_of(k)) { lambda_one<MULTI, SELFG, ACC>(k, doms, dom, start, xs, lam, pair_id, acc, i); }
+}
+
+// ----- delta p with artificial pressure and over-relaxation, then walls (PBF.cu:398-447, 471-499) -------
+// ACCINIT: this pass applies the warm start; its multiplier starts the step's running sum.
+template <bool MULTI, bool SCORR, bool ACCINIT, bool CG = false>
+__device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                            const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
+                                            const float2* __restrict__ xs, const float* __restrict__ lam,
+                                            float2* __restrict__ xs_out, float* __restrict__ acc, int32_t i)
+{
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float2 p  = xs[i];
     const float li  = lam[i];
@@ -304,10 +323,10 @@ __global__ void __launch_bounds__(T_PART)
     const float c6w = k.c6 * k.inv_w_dq;
     float sx = 0.f, sy = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q  = __ldg(&xs[j]);
-        const float lj  = __ldg(&lam[j]);
+        const float2 q  = ldn<CG>(&xs[j]);
+        const float lj  = ldn<CG>(&lam[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = rx * rx + ry * ry;
+        const float r2  = fmaf(rx, rx, ry * ry);
         const bool ok   = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
         const float inv = rsqrtf(ok ? r2 : 1.f);
         float l         = fmaf(lj, k.mass, mli);
@@ -330,6 +349,16 @@ __global__ void __launch_bounds__(T_PART)
     xs_out[i] = make_float2(ox, oy);
 }
 
+template <bool MULTI, bool SCORR, bool ACCINIT>
+__global__ void __launch_bounds__(T_MAX)
+    k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+              const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
+              float2* __restrict__ xs_out, float* __restrict__ acc)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count_of(k)) { delta_p_one<MULTI, SCORR, ACCINIT>(k, doms, dom, start, xs, lam, xs_out, acc, i); }
+}
+
 // ----- warm start: features of the first lambda pass ------------------------------------------------------
 // The lambda sums of k_lambda plus the neighbour count and the poly6-weighted sum of the neighbours'
 // lambda_prev; returns the cold first-iteration lambda and fills the network's 12 features (the order is
@@ -348,7 +377,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
         const float2 q  = __ldg(&xs[j]);
         const float lp  = __ldg(&prev[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = rx * rx + ry * ry;
+        const float r2  = fmaf(rx, rx, ry * ry);
         const bool self = j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
@@ -539,7 +568,7 @@ __global__ void k_collect_advance(int32_t* __restrict__ cnt, int32_t cap)
 // velocityClamp, PBF.cu:629-638
 __device__ __forceinline__ void velocity_clamp(const PbfK& k, float& vx, float& vy)
 {
-    const float v2  = vx * vx + vy * vy;
+    const float v2  = fmaf(vx, vx, vy * vy);
     // v2 == 0 can only pass the first test when v_min == 0 (never in the reference); avoid 0 * inf there
     const float inv = (v2 < k.v_min2 || v2 == 0.f) ? 0.f : rsqrtf(v2);
     const float nx = vx * inv, ny = vy * inv;
@@ -550,14 +579,13 @@ __device__ __forceinline__ void velocity_clamp(const PbfK& k, float& vx, float& 
 }
 
 // ----- velocity + XSPH (+ vorticity omega) (PBF.cu:538, 585-627) ---------------------------------------
-template <bool MULTI, bool VORT>
-__global__ void __launch_bounds__(T_PART)
-    k_xsph(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-           const uint32_t* __restrict__ start, const float2* __restrict__ x, const float2* __restrict__ xs,
-           float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
+template <bool MULTI, bool VORT, bool CG = false>
+__device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                         const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
+                                         const float2* __restrict__ x, const float2* __restrict__ xs,
+                                         float2* __restrict__ v_out, float* __restrict__ omega,
+                                         uint32_t* __restrict__ status, int32_t i)
 {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float2 p  = xs[i];
     const float2 po = x[i];
@@ -566,12 +594,14 @@ __global__ void __launch_bounds__(T_PART)
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float dvx = 0.f, dvy = 0.f, w = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q  = __ldg(&xs[j]);
-        const float2 qo = __ldg(&x[j]);
+        const float2 q  = ldn<CG>(&xs[j]);
+        const float2 qo = ldn<CG>(&x[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = rx * rx + ry * ry;
+        // explicit fused forms: the result must not depend on how the compiler contracts this body in the
+        // kernel it is inlined into (separate launches and the persistent solve are compared bit for bit)
+        const float r2  = fmaf(rx, rx, ry * ry);
         const bool in   = r2 <= k.h2; // masked, branch-free (see k_lambda)
-        const float dx = (q.x - qo.x) * k.inv_dt - vax, dy = (q.y - qo.y) * k.inv_dt - vay;
+        const float dx = fmaf(q.x - qo.x, k.inv_dt, -vax), dy = fmaf(q.y - qo.y, k.inv_dt, -vay);
         const float qq  = in ? k.h2 - r2 : 0.f;
         const float p6  = qq * qq * qq;
         dvx             = fmaf(dx, p6, dvx);
@@ -581,7 +611,7 @@ __global__ void __launch_bounds__(T_PART)
             const float inv  = rsqrtf(dir ? r2 : 1.f);
             const float diff = k.h - r2 * inv;
             const float gm   = dir ? diff * diff * inv : 0.f;
-            w                = fmaf(gm, dx * ry - dy * rx, w);
+            w                = fmaf(gm, fmaf(dx, ry, -(dy * rx)), w);
         }
     });
     w *= k.cs;
@@ -596,25 +626,33 @@ __global__ void __launch_bounds__(T_PART)
     if (VORT) { omega[i] = w; }
 }
 
-// ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
-template <bool MULTI>
-__global__ void __launch_bounds__(T_PART)
-    k_vorticity(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                const uint32_t* __restrict__ start, const float2* __restrict__ xs,
-                const float* __restrict__ omega, float2* __restrict__ v)
+template <bool MULTI, bool VORT>
+__global__ void __launch_bounds__(T_MAX)
+    k_xsph(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+           const uint32_t* __restrict__ start, const float2* __restrict__ x, const float2* __restrict__ xs,
+           float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
+    if (i < count_of(k)) { xsph_one<MULTI, VORT>(k, doms, dom, start, x, xs, v_out, omega, status, i); }
+}
+
+// ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
+template <bool MULTI, bool CG = false>
+__device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                              const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
+                                              const float2* __restrict__ xs, const float* __restrict__ omega,
+                                              float2* __restrict__ v, int32_t i)
+{
     const DomDev d = load_dom<MULTI>(k, doms, dom, i);
     const float2 p = xs[i];
     const float wi = omega[i];
     const float aw = fabsf(wi);
     float ex = 0.f, ey = 0.f;
     for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
-        const float2 q   = __ldg(&xs[j]);
-        const float wj   = __ldg(&omega[j]);
+        const float2 q   = ldn<CG>(&xs[j]);
+        const float wj   = ldn<CG>(&omega[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2   = rx * rx + ry * ry;
+        const float r2   = fmaf(rx, rx, ry * ry); // explicit fused forms, as in xsph_one
         const bool ok    = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
         const float inv  = rsqrtf(ok ? r2 : 1.f);
         const float diff = k.h - r2 * inv;
@@ -626,14 +664,104 @@ __global__ void __launch_bounds__(T_PART)
     ex             = -ex;
     ey             = -ey;
     float2 vv      = v[i];
-    const float e2 = ex * ex + ey * ey;
+    const float e2 = fmaf(ex, ex, ey * ey);
     if (e2 > 1e-40f) {
         const float il = rsqrtf(e2);
-        vv.x += k.vort_dt * (ey * il * wi);
-        vv.y += k.vort_dt * (-ex * il * wi);
+        vv.x           = fmaf(k.vort_dt, ey * il * wi, vv.x);
+        vv.y           = fmaf(k.vort_dt, -ex * il * wi, vv.y);
     }
     if (k.flags & GPE_PBF_VEL_CLAMP) { velocity_clamp(k, vv.x, vv.y); }
     v[i] = vv;
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(T_MAX)
+    k_vorticity(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                const uint32_t* __restrict__ start, const float2* __restrict__ xs,
+                const float* __restrict__ omega, float2* __restrict__ v)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count_of(k)) { vorticity_one<MULTI>(k, doms, dom, start, xs, omega, v, i); }
+}
+
+// ----- the persistent solve: every Jacobi pass (and XSPH) of a step in one launch -----------------------
+// For many small scenes (or one small one) a step is a chain of short passes whose launch gaps cost as much
+// as the work; here the passes run back to back in one cooperative launch, separated by a grid barrier in
+// global memory. Each thread handles the same particles in every pass (grid-stride loop), so its own
+// values are read back from where it wrote them; other particles' values are read from L2 (ldn<true>).
+struct GridSync {
+    unsigned int count;
+    unsigned int gen;
+};
+constexpr uint64_t GRID_WAIT_NS = 100ull * 1000ull * 1000ull; // a barrier wait gives up after 100 ms
+
+// All threads of every block. False when this block gave up waiting (GPE_STATUS_TIMEOUT is set); the
+// caller then returns, and the other blocks time out at their next barrier in turn.
+__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uint32_t* status)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned int target = gen + 1u;
+        __threadfence(); // this block's writes are visible device-wide before it arrives
+        if (atomicAdd(&g->count, 1u) == gridDim.x - 1u) {
+            atomicExch(&g->count, 0u);
+            __threadfence();
+            atomicExch(&g->gen, target);
+        } else {
+            const uint64_t t0 = tc::globaltimer();
+            while (atomicAdd(&g->gen, 0u) != target) {
+                if (tc::globaltimer() - t0 > GRID_WAIT_NS) {
+                    ok = 0;
+                    atomicOr(status, GPE_STATUS_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    gen += 1u;
+    return s_ok != 0;
+}
+
+// XSPH: the velocity pass runs here too; with vorticity confinement it runs as its usual launch after the
+// kernel instead (the omega-carrying pass inlined here differs from its own kernel in the last bit).
+template <bool MULTI, bool SELFG, bool SCORR, bool XSPH>
+__global__ void __launch_bounds__(T_MAX)
+    k_solve_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                       const uint32_t* __restrict__ start, float2* __restrict__ xs_a, float2* __restrict__ xs_b,
+                       const float2* __restrict__ x, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
+                       float2* __restrict__ v, float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
+                       uint32_t* __restrict__ status)
+{
+    const int32_t n      = count_of(k);
+    const int32_t stride = (int32_t)(gridDim.x * blockDim.x);
+    const int32_t i0     = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+    unsigned int gen     = 0u; // the barrier word is zeroed before every launch
+    float2* cur          = xs_a;
+    float2* nxt          = xs_b;
+    for (int32_t it = 0; it < iters; ++it) {
+        for (int32_t i = i0; i < n; i += stride) {
+            lambda_one<MULTI, SELFG, ACC_NONE, true>(k, doms, dom, start, cur, lam, pair_id, nullptr, i);
+        }
+        if (!grid_barrier(gs, gen, status)) { return; }
+        for (int32_t i = i0; i < n; i += stride) {
+            delta_p_one<MULTI, SCORR, false, true>(k, doms, dom, start, cur, lam, nxt, nullptr, i);
+        }
+        if (!grid_barrier(gs, gen, status)) { return; }
+        float2* t = cur;
+        cur       = nxt;
+        nxt       = t;
+    }
+    if (XSPH) {
+        for (int32_t i = i0; i < n; i += stride) {
+            xsph_one<MULTI, false, true>(k, doms, dom, start, x, cur, v, omega, status, i);
+        }
+    }
 }
 
 // ----- density for the density-error metric --------------------------------------------------------------
@@ -652,7 +780,7 @@ __global__ void __launch_bounds__(T_PART)
         for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
             const float2 q = __ldg(&xs[j]);
             const float rx = p.x - q.x, ry = p.y - q.y;
-            const float r2 = rx * rx + ry * ry;
+            const float r2 = fmaf(rx, rx, ry * ry);
             const float qq = (r2 <= k.h2) ? k.h2 - r2 : 0.f;
             s6             = fmaf(qq * qq, qq, s6);
         });
@@ -710,7 +838,7 @@ __global__ void k_pbf_emit(const PbfK k, const HoseK h, float2* __restrict__ x, 
     float vx = h.vx, vy = h.vy;
     if (k.flags & GPE_PBF_VEL_CLAMP) {
         // velocityClamp, as emitterKernel applies to the stream velocity (PBF.cu:990-991)
-        const float v2  = vx * vx + vy * vy;
+        const float v2  = fmaf(vx, vx, vy * vy);
         const float inv = (v2 < k.v_min2 || v2 == 0.f) ? 0.f : rsqrtf(v2);
         const float sp  = fminf(v2 * inv, k.v_max);
         vx *= inv * sp;
@@ -791,6 +919,7 @@ struct gpe_pbf {
     std::vector<DomDev> domdev;
     int64_t cap = 0, n = 0;
     uint32_t ncells = 0;
+    uint64_t cells_cap = 0; // cell arrays are sized for this many cells
 
     void* base        = nullptr;
     DomDev* d_doms    = nullptr;
@@ -822,6 +951,10 @@ struct gpe_pbf {
     bool pending_accinit = false; // stage API: the next DELTA_P starts the running sum
     bool mem_valid    = false;    // the multiplier memory holds a previous step's sums (else it is 0)
     int32_t lam_grid  = 0;        // persistent grid of k_mlp_apply
+    int32_t block     = 256;      // threads per block of the neighbour kernels (tuning)
+    bool persistent   = false;    // plain steps run their passes in one persistent launch (tuning)
+    int32_t coop_grid = 0;        // blocks of the persistent launch (all resident)
+    GridSync* gsync   = nullptr;  // its barrier word
     uint16_t* feat    = nullptr;  // network operand tiles (GPE_WARM_MLP), allocated on demand
 
     // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
@@ -958,6 +1091,8 @@ uint64_t count_cells(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd
 }
 
 unsigned blocks_for(int64_t n) { return (unsigned)((n + T_PART - 1) / T_PART); }
+// blocks of a neighbour-kernel launch at the tuned block size
+unsigned nblk(const gpe_pbf* s) { return (unsigned)((lsize(s) + s->block - 1) / s->block); }
 
 // ----- stage launchers ----------------------------------------------------------------------------------
 
@@ -1005,63 +1140,63 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 }
 
 // Template dispatch tables: [multi scene][flag][accumulation mode]
-using LamFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using LamFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                        const float2*, float*, const uint32_t*, float*);
 template <bool M, bool S, int A>
-void lam_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+void lam_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                 const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc)
 {
-    k_lambda<M, S, A><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    k_lambda<M, S, A><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
 }
 #define GPE_LAM3(M, S) {lam_launch<M, S, ACC_NONE>, lam_launch<M, S, ACC_SUM>, lam_launch<M, S, ACC_PROJ>}
 const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
                              {GPE_LAM3(true, false), GPE_LAM3(true, true)}};
 #undef GPE_LAM3
 
-using DpFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using DpFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                       const float2*, const float*, float2*, float*);
 template <bool M, bool S, bool A>
-void dp_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+void dp_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc)
 {
-    k_delta_p<M, S, A><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+    k_delta_p<M, S, A><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
 }
 const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, false, true>},
                             {dp_launch<false, true, false>, dp_launch<false, true, true>}},
                            {{dp_launch<true, false, false>, dp_launch<true, false, true>},
                             {dp_launch<true, true, false>, dp_launch<true, true, true>}}};
 
-using FeatFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using FeatFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                         const float2*, const float2*, const float*, const uint32_t*, const MlpDev*, uint16_t*);
 template <bool M, bool S>
-void feat_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+void feat_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                  const uint32_t* start, const float2* xs, const float2* xo, const float* prev, const uint32_t* pid,
                  const MlpDev* mlp, uint16_t* feat)
 {
-    k_lambda_feat<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+    k_lambda_feat<M, S><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
 }
 const FeatFn kFeat[2][2] = {{feat_launch<false, false>, feat_launch<false, true>},
                             {feat_launch<true, false>, feat_launch<true, true>}};
 
-using ColFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using ColFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                        const float2*, const float2*, const float*, float*, const uint32_t*, const CollectK&);
 template <bool M, bool S>
-void col_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+void col_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                 const uint32_t* start, const float2* xs, const float2* xo, const float* prev, float* lam,
                 const uint32_t* pid, const CollectK& col)
 {
-    k_lambda_collect<M, S><<<g, T_PART, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, col);
+    k_lambda_collect<M, S><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, col);
 }
 const ColFn kCol[2][2] = {{col_launch<false, false>, col_launch<false, true>},
                           {col_launch<true, false>, col_launch<true, true>}};
 
-using XsFn = void (*)(unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using XsFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                       const float2*, const float2*, float2*, float*, uint32_t*);
 template <bool M, bool V>
-void xs_launch(unsigned g, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+void xs_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status)
 {
-    k_xsph<M, V><<<g, T_PART, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+    k_xsph<M, V><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
 }
 const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
                         {xs_launch<true, false>, xs_launch<true, true>}};
@@ -1080,7 +1215,7 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st, int acc)
     if (lsize(s) == 0) { return GPE_OK; }
     const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
-    kLam[multi(s) ? 1 : 0][sg][acc](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
+    kLam[multi(s) ? 1 : 0][sg][acc](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
                                     s->lam, pid, s->acc);
     GPE_CHECK_LAUNCH("k_lambda");
     s->launches += 1;
@@ -1099,7 +1234,7 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
     if (s->warm == GPE_WARM_MLP && s->mem_valid && !s->collecting) {
         const gpe::MlpDev* md = gpe::mlp_device(s->mlp);
-        kFeat[mi][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
+        kFeat[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
                       s->prev, pid, md, s->feat);
         GPE_CHECK_LAUNCH("k_lambda_feat");
         const int64_t tiles = (lsize(s) + MLP_TILE - 1) / MLP_TILE;
@@ -1108,7 +1243,7 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
         GPE_CHECK_LAUNCH("k_mlp_apply");
         s->launches += 1;
     } else {
-        kCol[mi][sg](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
+        kCol[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
                      s->prev, s->lam, pid, s->col);
         GPE_CHECK_LAUNCH("k_lambda_collect");
     }
@@ -1120,7 +1255,7 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
 {
     if (lsize(s) > 0) {
         const int sc = s->prm.scorr_k != 0.f ? 1 : 0;
-        kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start,
+        kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
                                                    s->pos[s->XS], s->lam, s->pos[s->XO], s->acc);
         GPE_CHECK_LAUNCH("k_delta_p");
         s->launches += 1;
@@ -1133,7 +1268,7 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
-    kXs[multi(s) ? 1 : 0][vort](blocks_for(lsize(s)), st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
+    kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
                                 s->pos[s->XS], s->vel, s->omega, s->status);
     GPE_CHECK_LAUNCH("k_xsph");
     s->launches += 1;
@@ -1143,11 +1278,11 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) == 0 || s->prm.vort_eps == 0.f) { return GPE_OK; }
-    const unsigned g = blocks_for(lsize(s));
+    const unsigned g = nblk(s);
     if (multi(s)) {
-        k_vorticity<true><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega, s->vel);
+        k_vorticity<true><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega, s->vel);
     } else {
-        k_vorticity<false><<<g, T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega,
+        k_vorticity<false><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega,
                                                  s->vel);
     }
     GPE_CHECK_LAUNCH("k_vorticity");
@@ -1162,10 +1297,67 @@ int32_t stage_finish(gpe_pbf* s)
     return GPE_OK;
 }
 
+// The Jacobi passes and XSPH of a plain step in one cooperative launch (k_solve_persistent).
+template <bool M, bool S, bool C, bool V>
+const void* solve_fn()
+{
+    return reinterpret_cast<const void*>(k_solve_persistent<M, S, C, V>);
+}
+const void* solve_kernel(const gpe_pbf* s)
+{
+    const bool m = multi(s), sg = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0, sc = s->prm.scorr_k != 0.f,
+               v = s->prm.vort_eps == 0.f; // XSPH inside the kernel
+    const void* tab[16] = {
+        solve_fn<false, false, false, false>(), solve_fn<false, false, false, true>(),
+        solve_fn<false, false, true, false>(),  solve_fn<false, false, true, true>(),
+        solve_fn<false, true, false, false>(),  solve_fn<false, true, false, true>(),
+        solve_fn<false, true, true, false>(),   solve_fn<false, true, true, true>(),
+        solve_fn<true, false, false, false>(),  solve_fn<true, false, false, true>(),
+        solve_fn<true, false, true, false>(),   solve_fn<true, false, true, true>(),
+        solve_fn<true, true, false, false>(),   solve_fn<true, true, false, true>(),
+        solve_fn<true, true, true, false>(),    solve_fn<true, true, true, true>()};
+    return tab[(m ? 8 : 0) + (sg ? 4 : 0) + (sc ? 2 : 0) + (v ? 1 : 0)];
+}
+
+int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
+{
+    if (lsize(s) > 0) {
+        const void* fn = solve_kernel(s);
+        if (s->coop_grid <= 0) {
+            int per_sm = 0;
+            GPE_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, s->block, 0));
+            s->coop_grid = std::max(1, per_sm) * gpe::sm_count();
+        }
+        const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
+        PbfK k              = s->k;
+        float2* xa          = s->pos[s->XS];
+        float2* xb          = s->pos[s->XO];
+        const float2* xsort = s->pos[s->SX];
+        int32_t iters       = s->prm.iters;
+        void* args[]        = {&k,  &s->d_doms, &s->dom, &s->start, &xa,   &xb,        &xsort,
+                               &s->lam, &pid, &s->vel, &s->omega, &iters, &s->gsync, &s->status};
+        GPE_TRY_CUDA(cudaMemsetAsync(s->gsync, 0, sizeof(GridSync), st));
+        GPE_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)s->coop_grid), dim3((unsigned)s->block), args, 0,
+                                                 st));
+        s->launches += 1;
+    }
+    if (s->prm.iters & 1) { std::swap(s->XS, s->XO); } // the kernel's final x* is in the other buffer
+    return GPE_OK;
+}
+
 int32_t run_step(gpe_pbf* s, cudaStream_t st)
 {
     const bool acc = accumulating(s);
     int32_t rc     = stage_predict_sort(s, st);
+    if (rc == GPE_OK && s->persistent && !acc) {
+        rc = stage_solve_persistent(s, st);
+        if (rc == GPE_OK && s->prm.vort_eps != 0.f) {
+            rc = stage_xsph(s, st);
+            if (rc == GPE_OK) { rc = stage_vorticity(s, st); }
+        }
+        if (rc == GPE_OK) { rc = stage_finish(s); }
+        return rc;
+    }
     for (int32_t it = 0; it < s->prm.iters && rc == GPE_OK; ++it) {
         if (it == 0 && acc) {
             rc = stage_lambda_warm(s, st);
@@ -1192,7 +1384,7 @@ int32_t run_step(gpe_pbf* s, cudaStream_t st)
 int32_t alloc_buffers(gpe_pbf* s)
 {
     const size_t N = (size_t)s->cap;
-    const size_t M = (size_t)s->ncells;
+    const size_t M = (size_t)s->cells_cap; // room for the finest sort grid the tuning may select
     Carver c;
     const size_t o_doms = c.take<DomDev>((size_t)s->nd);
     size_t o_pos[4];
@@ -1217,6 +1409,7 @@ int32_t alloc_buffers(gpe_pbf* s)
     const size_t o_cnt1  = c.take<int32_t>(1);
     const size_t o_acc   = c.take<float>(N);
     const size_t o_prev  = c.take<float>(N);
+    const size_t o_gs    = c.take<GridSync>(1);
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -1242,6 +1435,7 @@ int32_t alloc_buffers(gpe_pbf* s)
     s->d_count = reinterpret_cast<int32_t*>(b + o_cnt1);
     s->acc     = reinterpret_cast<float*>(b + o_acc);
     s->prev    = reinterpret_cast<float*>(b + o_prev);
+    s->gsync   = reinterpret_cast<GridSync*>(b + o_gs);
     s->k.n_dev = s->d_count;
     GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
     return GPE_OK;
@@ -1292,6 +1486,13 @@ int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, 
     s->dynamic = (params->flags & GPE_PBF_DYNAMIC_COUNT) != 0;
     s->cap = capacity;
     build_domains(s);
+    {
+        // the cell arrays also hold the h/2 grid, so that the tuning can select it later
+        gpe_pbf_params half = *params;
+        half.cell           = 0.5f * params->h;
+        const uint64_t ch   = count_cells(&half, domains, n_domains);
+        s->cells_cap        = std::max<uint64_t>(cells, ch <= ((uint64_t)1 << 30) ? ch : 0);
+    }
     rc = alloc_buffers(s);
     if (rc) {
         if (s->base) { cudaFree(s->base); }
@@ -1774,6 +1975,190 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
     s->X         = X0;
     s->id_cur    = id0;
     s->have_sort = true;
+    return GPE_OK;
+}
+
+// =====================================================================================================
+// Tuning (cell size, block size, persistent solve) and the autotuner
+// =====================================================================================================
+
+namespace {
+
+int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
+{
+    if (!(t.cell >= 0.f) || (t.block != 128 && t.block != 256 && t.block != 512) ||
+        (t.persistent != 0 && t.persistent != 1)) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0 or 1");
+        return GPE_ERR_BAD_ARG;
+    }
+    const float c_old = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
+    const float c_new = t.cell > 0.f ? t.cell : s->prm.h;
+    if (c_new != c_old) {
+        if (c_new < 0.2f * s->prm.h) {
+            gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_tuning: cell size below h/5");
+            return GPE_ERR_BAD_ARG;
+        }
+        gpe_pbf_params np = s->prm;
+        np.cell           = c_new;
+        const uint64_t nc = count_cells(&np, s->doms.data(), s->nd);
+        if (nc > s->cells_cap) {
+            gpe::set_error(GPE_ERR_CAPACITY, "gpe_pbf_set_tuning: %llu cells exceed the %llu the engine holds",
+                           (unsigned long long)nc, (unsigned long long)s->cells_cap);
+            return GPE_ERR_CAPACITY;
+        }
+        s->prm.cell = c_new;
+        build_domains(s);
+        GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
+        s->have_sort = false;
+    }
+    if (t.block != s->block) { s->coop_grid = 0; }
+    s->block      = t.block;
+    s->persistent = t.persistent != 0;
+    s->drop_graphs();
+    return GPE_OK;
+}
+
+struct TuneKey {
+    int32_t nd, log_n, log_aspect, iters;
+    uint32_t flags;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(nd, log_n, log_aspect, iters, flags) < std::tie(o.nd, o.log_n, o.log_aspect, o.iters, o.flags);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, gpe_pbf_tuning> g_tune_cache;
+
+} // namespace
+
+extern "C" int32_t gpe_pbf_get_tuning(const gpe_pbf* s, gpe_pbf_tuning* t)
+{
+    if (!s || !t) { return GPE_ERR_BAD_ARG; }
+    t->cell       = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
+    t->block      = s->block;
+    t->persistent = s->persistent ? 1 : 0;
+    return GPE_OK;
+}
+
+extern "C" int32_t gpe_pbf_set_tuning(gpe_pbf* s, const gpe_pbf_tuning* t)
+{
+    gpe::clear_error();
+    if (!s || !t) { return GPE_ERR_BAD_ARG; }
+    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    return apply_tuning(s, *t);
+}
+
+extern "C" int32_t gpe_pbf_autotune(gpe_pbf* s, int32_t trial_steps, gpe_pbf_tuning* best, float* ms_per_step,
+                                    void* stream)
+{
+    gpe::clear_error();
+    if (!s || trial_steps < 1) { return GPE_ERR_BAD_ARG; }
+    if (!s->have_state || s->SX >= 0 || s->warm != GPE_WARM_NONE || s->dynamic) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_autotune: needs a state, GPE_WARM_NONE and a host particle count");
+        return GPE_ERR_NOT_READY;
+    }
+    cudaStream_t st = as_stream(stream);
+    // the cache key: scenes, particle count and mean aspect to the nearest power of two, iterations, flags
+    double aspect = 0.0;
+    for (const gpe_domain& d : s->doms) { aspect += std::log2((double)d.extent[0] / (double)d.extent[1]); }
+    const TuneKey key{s->nd, (int32_t)std::lround(std::log2((double)std::max<int64_t>(s->n, 1))),
+                      (int32_t)std::lround(aspect / (double)s->nd), s->prm.iters,
+                      s->prm.flags & (GPE_PBF_SELF_GRAD | GPE_PBF_PAIR_IDS)};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const int32_t rc = apply_tuning(s, it->second);
+            if (rc == GPE_OK && best) { *best = it->second; }
+            if (ms_per_step) { *ms_per_step = -1.f; } // not timed: taken from the cache
+            return rc;
+        }
+    }
+    // save the state (positions, velocities, scenes, ids), restored before every trial and at the end
+    const int64_t n   = s->n;
+    const bool ids    = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
+    void* save        = nullptr;
+    const size_t nb   = (size_t)std::max<int64_t>(n, 1);
+    GPE_TRY_CUDA(cudaMalloc(&save, nb * (2 * sizeof(float2) + 2 * sizeof(int32_t))));
+    float2* sx        = static_cast<float2*>(save);
+    float2* sv        = sx + nb;
+    int32_t* sd       = reinterpret_cast<int32_t*>(sv + nb);
+    uint32_t* sid     = reinterpret_cast<uint32_t*>(sd + nb);
+    auto restore      = [&]() -> int32_t {
+        int32_t rc = gpe_pbf_set_state(s, reinterpret_cast<float*>(sx), reinterpret_cast<float*>(sv),
+                                       s->nd > 1 ? sd : nullptr, n, GPE_MEM_DEVICE, stream);
+        if (rc == GPE_OK && ids && n > 0) {
+            GPE_TRY_CUDA(cudaMemcpyAsync(s->ids[s->id_cur], sid, sizeof(uint32_t) * (size_t)n,
+                                         cudaMemcpyDeviceToDevice, st));
+        }
+        return rc;
+    };
+    int32_t rc = gpe_pbf_get_state(s, reinterpret_cast<float*>(sx), reinterpret_cast<float*>(sv),
+                                   s->nd > 1 ? sd : nullptr, n, GPE_MEM_DEVICE, stream);
+    if (rc == GPE_OK && ids && n > 0) {
+        const cudaError_t e = cudaMemcpyAsync(sid, s->ids[s->id_cur], sizeof(uint32_t) * (size_t)n,
+                                              cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            gpe::set_cuda_error(e, "gpe_pbf_autotune");
+            rc = GPE_ERR_CUDA;
+        }
+    }
+    gpe_pbf_tuning start{};
+    gpe_pbf_get_tuning(s, &start);
+    gpe_pbf_tuning win = start;
+    float win_ms       = -1.f;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == GPE_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) {
+        rc = GPE_ERR_CUDA;
+    }
+    const float cells[2] = {s->prm.h, 0.5f * s->prm.h};
+    const int32_t blocks[3] = {128, 256, 512};
+    for (int ci = 0; ci < 2 && rc == GPE_OK; ++ci) {
+        for (int bi = 0; bi < 3 && rc == GPE_OK; ++bi) {
+            for (int pi = 0; pi < 2 && rc == GPE_OK; ++pi) {
+                const gpe_pbf_tuning cand{cells[ci], blocks[bi], pi};
+                if (apply_tuning(s, cand) != GPE_OK) { continue; } // e.g. the h/2 grid does not fit
+                rc = restore();
+                if (rc) { break; }
+                // two untimed steps capture the candidate's graph; a candidate that cannot run is skipped
+                if (gpe_pbf_step(s, 2, stream) != GPE_OK || cudaStreamSynchronize(st) != cudaSuccess) {
+                    cudaGetLastError();
+                    continue;
+                }
+                cudaEventRecord(e0, st);
+                const int32_t src = gpe_pbf_step(s, trial_steps, stream);
+                cudaEventRecord(e1, st);
+                if (src != GPE_OK || cudaEventSynchronize(e1) != cudaSuccess) {
+                    cudaGetLastError();
+                    continue;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= (float)trial_steps;
+                uint32_t stt = 0;
+                gpe_pbf_status(s, &stt, stream);
+                if (stt != 0) { continue; } // a trial whose state went bad does not count
+                if (win_ms < 0.f || ms < win_ms) {
+                    win_ms = ms;
+                    win    = cand;
+                }
+            }
+        }
+    }
+    if (e0) { cudaEventDestroy(e0); }
+    if (e1) { cudaEventDestroy(e1); }
+    int32_t rc2 = apply_tuning(s, win_ms >= 0.f ? win : start);
+    if (rc2 == GPE_OK) { rc2 = restore(); }
+    cudaStreamSynchronize(st);
+    cudaFree(save);
+    if (rc) { return rc; }
+    if (rc2) { return rc2; }
+    if (win_ms >= 0.f) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = win;
+    }
+    if (best) { *best = win_ms >= 0.f ? win : start; }
+    if (ms_per_step) { *ms_per_step = win_ms; }
     return GPE_OK;
 }
 

@@ -78,6 +78,10 @@ class View(C.Structure):
                 ("chunks_y", C.c_int32), ("chunk_dim", C.c_float), ("chunk_capacity", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("cell", C.c_float), ("block", C.c_int32), ("persistent", C.c_int32)]
+
+
 class TrainParams(C.Structure):
     _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("weight_decay", C.c_float),
                 ("beta1", C.c_float), ("beta2", C.c_float), ("adam_eps", C.c_float), ("val_fraction", C.c_float),
@@ -157,6 +161,9 @@ def lib() -> C.CDLL:
             "gpe_mpm_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_mpm_launches_per_step": [vp, C.POINTER(i32)],
             "gpe_pbf_set_warm_start": [vp, i32, vp],
+            "gpe_pbf_get_tuning": [vp, C.POINTER(Tuning)],
+            "gpe_pbf_set_tuning": [vp, C.POINTER(Tuning)],
+            "gpe_pbf_autotune": [vp, i32, C.POINTER(Tuning), C.POINTER(C.c_float), vp],
             "gpe_mlp_create": [i64, C.c_uint64, C.POINTER(vp)],
             "gpe_mlp_destroy": [vp],
             "gpe_mlp_get_blob": [vp, vp, i64],
@@ -342,6 +349,20 @@ class Pbf:
 
     def enqueue(self, n_steps: int, stream=None) -> None:
         check(lib().gpe_pbf_enqueue(self.h, int(n_steps), stream), "gpe_pbf_enqueue")
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        check(lib().gpe_pbf_get_tuning(self.h, C.byref(t)), "gpe_pbf_get_tuning")
+        return t
+
+    def set_tuning(self, cell: float = 0.0, block: int = 256, persistent: bool = False) -> None:
+        t = Tuning(cell, block, 1 if persistent else 0)
+        check(lib().gpe_pbf_set_tuning(self.h, C.byref(t)), "gpe_pbf_set_tuning")
+
+    def autotune(self, trial_steps: int = 4, stream=None) -> tuple[Tuning, float]:
+        t, ms = Tuning(), C.c_float()
+        check(lib().gpe_pbf_autotune(self.h, int(trial_steps), C.byref(t), C.byref(ms), stream), "gpe_pbf_autotune")
+        return t, ms.value
 
     def set_warm_start(self, mode: int, mlp: "Mlp | None" = None) -> None:
         check(lib().gpe_pbf_set_warm_start(self.h, int(mode), None if mlp is None else mlp.h),

@@ -284,6 +284,33 @@ int32_t gpe_mlp_gradient(gpe_mlp* mlp, const float* features, const float* targe
  * Resets lambda_prev to 0. */
 int32_t gpe_pbf_set_warm_start(gpe_pbf* pbf, int32_t mode, const gpe_mlp* mlp);
 
+/* ======================================================================================================
+ * Tuning of the PBF step and the autotuner
+ * ======================================================================================================
+ * A tuning changes how a step runs, not what it computes: for a given cell size every choice gives the same
+ * result bit for bit. */
+typedef struct gpe_pbf_tuning {
+    float cell;         /* sort-cell edge; 0 selects h. h/2 scans 5 x 5 cells of a quarter of the area,
+                           testing fewer candidates per particle, over more and shorter cell rows          */
+    int32_t block;      /* threads per block of the neighbour kernels: 128, 256 or 512                 */
+    int32_t persistent; /* 1: the Jacobi passes and XSPH of a plain step run in one cooperative launch
+                           with grid barriers between them (for many small scenes, whose steps are
+                           otherwise launch-bound; vorticity keeps its own launches); 0: one launch
+                           per pass                                                                     */
+} gpe_pbf_tuning;
+
+int32_t gpe_pbf_get_tuning(const gpe_pbf* pbf, gpe_pbf_tuning* tuning);
+/* A new cell size rebuilds the scenes' sort grids (the engine holds cell arrays for h/2 and for the cell
+ * size it was created with). */
+int32_t gpe_pbf_set_tuning(gpe_pbf* pbf, const gpe_pbf_tuning* tuning);
+/* Times trial_steps steps of every candidate (cell h or h/2, block 128, 256 or 512, persistent or not) on
+ * the current state, which is restored after every trial and at the end, and applies the fastest;
+ * *best and *ms_per_step receive it and its time (-1 when the choice came from the cache). Choices are
+ * cached for the process per (scenes, particle count and mean scene aspect to the nearest power of two,
+ * iterations, pair-direction flags). Needs GPE_WARM_NONE and a host particle count. */
+int32_t gpe_pbf_autotune(gpe_pbf* pbf, int32_t trial_steps, gpe_pbf_tuning* best, float* ms_per_step,
+                         void* stream);
+
 /* Allocation-free predict + cell sort for one scene. It has no counterpart in the reference (whose arenas
  * are all allocated up front, cuda-engine.cpp:102-139); it exists for callers that cannot call cudaMalloc,
  * such as a host whose device memory is owned by another framework, or a real-time loop that must not
