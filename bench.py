@@ -294,6 +294,51 @@ def reference_cuda_leg(args, stream, flush_l2):
                    "same scene and constants, L2 flushed before each timed substep"}
 
 
+def render_leg(args, stream, flush_l2, eng):
+    """The headless splat rasteriser on the 1M-particle state: published into a 4 x 4-chunk view and drawn
+    into a 2048 x 2048 RGBA8 image (100 pixels per metre), timed per frame (publish + draw) like the
+    headline. Bytes per frame: particles read by the publish (16 B) and written to the view (16 B) and read
+    by the splat pass (8 B), coverage zeroed, counted (21 splat updates of 4 B) and read (4 B per pixel),
+    image written (4 B per pixel)."""
+    import torch
+
+    import gpe
+
+    sh = stream.cuda_stream
+    n = eng.n
+    cx = cy = 4
+    dim, cap = 5.12, 1 << 18  # a chunk of 5.12 m holds 512 x 512 atoms at 0.01 m spacing
+    vp = torch.empty((cx * cy * cap, 2), dtype=torch.float32, device="cuda")
+    vv = torch.empty_like(vp)
+    vc = torch.zeros(cx * cy, dtype=torch.int32, device="cuda")
+    view = gpe.View(vp.data_ptr(), vv.data_ptr(), vc.data_ptr(), cx, cy, dim, cap)
+    W = H = 2048
+    img = torch.empty((H, 4 * W), dtype=torch.uint8, device="cuda")
+    cov = torch.empty((H, W), dtype=torch.int32, device="cuda")
+    r = gpe.Raster(img.data_ptr(), 4 * W, W, H, 100.0, dim, cov.data_ptr())
+
+    def frame():
+        eng.publish(view, stream=sh)
+        gpe.render_frame(r, view, stream=sh)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in ev:
+        flush_l2()
+        a.record(stream)
+        frame()
+        b.record(stream)
+    torch.cuda.synchronize()
+    s = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
+    bytes_frame = 40.0 * n + 21 * 4.0 * n + (4 + 4 + 4 + 4) * W * H
+    peak, _ = peaks()
+    return {"workload": "render_1m_2048x2048", "particles": n, "pixels": W * H, "ms_per_frame": 1e3 * s,
+            "pixels_per_s": W * H / s, "particles_per_s": n / s, "alg_bytes_per_frame": bytes_frame,
+            "effective_gbs": bytes_frame / s / 1e9, "hbm_frac": bytes_frame / s / 1e9 / peak}
+
+
 def batched_leg(args, stream, flush_l2):
     """Batched PBF: 256 independent dam-break scenes, particle counts log-uniform in [2048, 65536] (seed 3),
     box aspect U(0.5, 2), C0 physics at dt = 1/480, 4 iterations, all scenes in one engine; timed with the
@@ -518,6 +563,12 @@ def run_gpe(args, rank, ws):
     base = None
     if ws == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(p, pos, vel, boxes)
+    render = None
+    if ws == 1 and not args.no_render:
+        try:
+            render = render_leg(args, stream, flush_l2, eng)
+        except Exception as exc:  # reported, never fatal to the headline number
+            render = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
     eng.close()
     learned = None
     if ws == 1 and not args.no_learned:
@@ -554,7 +605,7 @@ def run_gpe(args, rank, ws):
             "gpu_launches": launches * args.steps, "launches_per_step": launches,
             "hbm_effective_gbs": 212.0 * value / ws / 1e9,
             "density_error": {"max": dmax, "mean": dmean}, "clocks": clk.summary(),
-            "learned": learned, "batched": batched, "mpm": mpm, "reference_cuda": ref_cuda}
+            "learned": learned, "batched": batched, "mpm": mpm, "render": render, "reference_cuda": ref_cuda}
     print(json.dumps(line), flush=True)
 
 
@@ -569,6 +620,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-mpm", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-render", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

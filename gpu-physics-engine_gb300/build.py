@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libgpe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "sort.cu", "pbf.cu", "mpm.cu", "mlp.cu"]
+SOURCES = ["capi.cu", "sort.cu", "pbf.cu", "mpm.cu", "mlp.cu", "render.cu"]
 
 
 def nvcc() -> str:

@@ -78,6 +78,17 @@ class View(C.Structure):
                 ("chunks_y", C.c_int32), ("chunk_dim", C.c_float), ("chunk_capacity", C.c_int32)]
 
 
+class Raster(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("pitch", C.c_int64), ("width", C.c_int32), ("height", C.c_int32),
+                ("scale", C.c_float), ("chunk_dim", C.c_float), ("coverage", C.c_void_p)]
+
+
+def render_frame(raster: "Raster", view, view_mem: int = MEM_HOST, stream=None) -> None:
+    """Draws a published view into the raster's RGBA8 device image (gpe_render_frame)."""
+    ptr = C.addressof(view) if view_mem == MEM_HOST else int(view)
+    check(lib().gpe_render_frame(C.byref(raster), ptr, view_mem, stream), "gpe_render_frame")
+
+
 class Tuning(C.Structure):
     _fields_ = [("cell", C.c_float), ("block", C.c_int32), ("persistent", C.c_int32)]
 
@@ -161,6 +172,7 @@ def lib() -> C.CDLL:
             "gpe_mpm_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_mpm_launches_per_step": [vp, C.POINTER(i32)],
             "gpe_pbf_set_warm_start": [vp, i32, vp],
+            "gpe_render_frame": [C.POINTER(Raster), vp, i32, vp],
             "gpe_pbf_get_tuning": [vp, C.POINTER(Tuning)],
             "gpe_pbf_set_tuning": [vp, C.POINTER(Tuning)],
             "gpe_pbf_autotune": [vp, i32, C.POINTER(Tuning), C.POINTER(C.c_float), vp],

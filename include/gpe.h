@@ -285,6 +285,27 @@ int32_t gpe_mlp_gradient(gpe_mlp* mlp, const float* features, const float* targe
 int32_t gpe_pbf_set_warm_start(gpe_pbf* pbf, int32_t mode, const gpe_mlp* mlp);
 
 /* ======================================================================================================
+ * Headless particle splat rasteriser
+ * ======================================================================================================
+ * The reference's render path without D3D12 (backgroundKernel and drawKernel launched by launchFill,
+ * libs/render/source/cuda-render.cu:189-310) into a pitched RGBA8 device image: the background (black chunk
+ * grid lines every chunk_dim * scale pixels, else a vertical gradient), then every particle of a published
+ * view as a 5 x 5 splat without corners blended with the reference's alpha() (:244-258), at pixel
+ * ((int)(x * scale), (int)(y * scale)). The reference's unsynchronised blend makes overlapping splats race;
+ * here each pixel gets the sequential result (the blend applied once per covering splat), independent of
+ * scheduling. */
+typedef struct gpe_raster {
+    uint8_t* rgba;     /* device image, `pitch` bytes per row                                            */
+    int64_t pitch;     /* >= 4 * width                                                                   */
+    int32_t width, height;
+    float scale;       /* pixels per scene unit (kSimScale, constants.h:59)                              */
+    float chunk_dim;   /* chunk edge in scene units (kChunkDim, constants.h:48)                          */
+    int32_t* coverage; /* device scratch of width * height int32 (splats covering each pixel)           */
+} gpe_raster;
+/* view_mem: where the gpe_view struct lives (its arrays are device memory either way). */
+int32_t gpe_render_frame(const gpe_raster* raster, const gpe_view* view, int32_t view_mem, void* stream);
+
+/* ======================================================================================================
  * Tuning of the PBF step and the autotuner
  * ======================================================================================================
  * A tuning changes how a step runs, not what it computes: for a given cell size every choice gives the same

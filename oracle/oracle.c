@@ -1022,6 +1022,59 @@ void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t 
 }
 
 /* ===================================================================================================== */
+/* Splat rasteriser: backgroundKernel, alpha and drawKernel of libs/render/source/cuda-render.cu:214-310,     */
+/* run sequentially (chunk by chunk, atom by atom) into a tightly packed RGBA8 image                        */
+/* ===================================================================================================== */
+
+static uint8_t blend_ch(uint8_t over, uint8_t under, float a, float ia)
+{
+    return (uint8_t)((float)over * a + (float)under * ia + 0.5f); /* alpha(), cuda-render.cu:244-258 */
+}
+
+void orc_render_frame(int32_t width, int32_t height, float scale, float chunk_dim, int32_t chunks, int32_t capacity,
+                      const float* pos, const int32_t* counts, uint8_t* rgba)
+{
+    const int32_t every = (int32_t)(chunk_dim * scale);
+    for (int32_t y = 0; y < height; ++y) {
+        for (int32_t x = 0; x < width; ++x) {
+            uint8_t* px = &rgba[((size_t)y * width + x) * 4];
+            if (x % every == 0 || y % every == 0) {
+                px[0] = px[1] = px[2] = 0;
+            } else {
+                const float t = 100.f * ((float)y / (float)height);
+                px[0]         = (uint8_t)(255u - (uint8_t)t);
+                px[1]         = (uint8_t)(160u - (uint8_t)t);
+                px[2]         = 80;
+            }
+            px[3] = 255;
+        }
+    }
+    const float c  = 1.f / 255.f;
+    const float a  = (float)100 * c;
+    const float ia = 1.f - a;
+    for (int32_t ch = 0; ch < chunks; ++ch) {
+        const int32_t n = counts[ch] < capacity ? counts[ch] : capacity;
+        for (int32_t k = 0; k < n; ++k) {
+            const float* p   = &pos[((size_t)ch * capacity + k) * 2];
+            const int32_t px = (int32_t)(p[0] * scale);
+            const int32_t py = (int32_t)(p[1] * scale);
+            if (px < 0 || py < 0 || px >= width || py >= height) { continue; }
+            for (int32_t i = -2; i <= 2; ++i) {
+                if (py + i < 0 || py + i >= height) { continue; }
+                for (int32_t j = -2; j <= 2; ++j) {
+                    if (px + j < 0 || px + j >= width || ((i == 2 || i == -2) && (j == 2 || j == -2))) { continue; }
+                    uint8_t* q = &rgba[((size_t)(py + i) * width + (px + j)) * 4];
+                    q[0]       = blend_ch(140, q[0], a, ia);
+                    q[1]       = blend_ch(210, q[1], a, ia);
+                    q[2]       = blend_ch(255, q[2], a, ia);
+                    q[3]       = 255;
+                }
+            }
+        }
+    }
+}
+
+/* ===================================================================================================== */
 /* MLS-MPM                                                                                                */
 /* ===================================================================================================== */
 

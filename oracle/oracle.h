@@ -74,6 +74,13 @@ void orc_pbf_step_warm(const gpe_pbf_params* p, const gpe_domain* doms, int32_t 
                        int32_t* dom, uint32_t* pair_id, float* acc, int32_t mode, const float* blob,
                        int32_t n_steps);
 
+/* ---------- splat rasteriser ---------- */
+/* The reference's background and splat blend, sequentially (chunk by chunk, atom by atom): pos holds
+ * chunks * capacity float2 (chunk-major, as a published view), counts the atoms per chunk; rgba receives
+ * width * height * 4 bytes. */
+void orc_render_frame(int32_t width, int32_t height, float scale, float chunk_dim, int32_t chunks, int32_t capacity,
+                      const float* pos, const int32_t* counts, uint8_t* rgba);
+
 /* ---------- MLS-MPM ---------- */
 /* grid: nx*ny*3 doubles (momentum x, momentum y, mass) */
 void orc_mpm_p2g(const gpe_mpm_params* p, int64_t n, const float* x, const float* v, const float* C,

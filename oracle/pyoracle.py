@@ -40,6 +40,7 @@ def lib() -> C.CDLL:
         L.orc_mlp_forward.argtypes = [vp, i64, vp, vp, i32]
         L.orc_mlp_gradient.argtypes = [vp, i64, vp, vp, vp, vp, i32]
         L.orc_pbf_step_warm.argtypes = [pp, dp, i32, i64, vp, vp, vp, vp, vp, i32, vp, i32]
+        L.orc_render_frame.argtypes = [i32, i32, C.c_float, C.c_float, i32, i32, vp, vp, vp]
         L.orc_mpm_p2g.argtypes = [mp, i64, vp, vp, vp, vp, vp, vp, vp]
         L.orc_mpm_grid_update.argtypes = [mp, vp]
         L.orc_mpm_g2p.argtypes = [mp, i64, vp, vp, vp, vp, vp, vp, vp]
@@ -209,6 +210,17 @@ def mlp_gradient(blob, X, T, bf16=True):
     lib().orc_mlp_gradient(_p(_c(blob, np.float32)), X.shape[0], _p(X), _p(T), _p(g), C.byref(loss),
                            int(bool(bf16)))
     return g, loss.value
+
+
+def render_frame(width, height, scale, chunk_dim, pos, counts):
+    """pos: (chunks, capacity, 2) float32 chunk-major view arrays; counts: (chunks,) int32."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    counts = np.ascontiguousarray(counts, np.int32)
+    chunks, capacity = pos.shape[0], pos.shape[1]
+    out = np.empty((height, width, 4), np.uint8)
+    lib().orc_render_frame(int(width), int(height), float(scale), float(chunk_dim), chunks, capacity, _p(pos),
+                           _p(counts), _p(out))
+    return out
 
 
 def num_threads() -> int:
