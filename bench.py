@@ -297,9 +297,9 @@ def reference_cuda_leg(args, stream, flush_l2):
 def render_leg(args, stream, flush_l2, eng):
     """The headless splat rasteriser on the 1M-particle state: published into a 4 x 4-chunk view and drawn
     into a 2048 x 2048 RGBA8 image (100 pixels per metre), timed per frame (publish + draw) like the
-    headline. Bytes per frame: particles read by the publish (16 B) and written to the view (16 B) and read
-    by the splat pass (8 B), coverage zeroed, counted (21 splat updates of 4 B) and read (4 B per pixel),
-    image written (4 B per pixel)."""
+    headline. Algorithmic bytes per frame: particles read by the publish (16 B) and written to the view
+    (16 B), view positions read by the splat pass (8 B); per pixel the centre counts zeroed and read (4 + 4 B)
+    and the image written (4 B). The one atomic per particle lands on the 16 MB count image in L2."""
     import torch
 
     import gpe
@@ -332,7 +332,7 @@ def render_leg(args, stream, flush_l2, eng):
         b.record(stream)
     torch.cuda.synchronize()
     s = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
-    bytes_frame = 40.0 * n + 21 * 4.0 * n + (4 + 4 + 4 + 4) * W * H
+    bytes_frame = 40.0 * n + (4 + 4 + 4) * W * H
     peak, _ = peaks()
     return {"workload": "render_1m_2048x2048", "particles": n, "pixels": W * H, "ms_per_frame": 1e3 * s,
             "pixels_per_s": W * H / s, "particles_per_s": n / s, "alg_bytes_per_frame": bytes_frame,

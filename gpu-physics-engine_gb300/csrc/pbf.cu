@@ -867,26 +867,90 @@ __global__ void k_view_zero(const gpe_view* __restrict__ vp)
     }
 }
 
-__global__ void k_pbf_publish(const PbfK k, const gpe_view vv, const gpe_view* __restrict__ vp,
-                              const float2* __restrict__ x, const float2* __restrict__ v, uint32_t* __restrict__ status)
+// One block publishes PUB_PER_BLOCK consecutive particles. The chunk counters of a view sit side by side in
+// one cache line, so one returning atomic per particle (or per warp) queues at one L2 slice. Here the lanes
+// of a warp bound for the same chunk form a group (match_any); the group's first lane ranks the group in a
+// shared-memory table of the block's chunks (open addressing over PUB_SLOTS slots), the block takes one
+// global atomic per chunk it touches, and each particle is written at that base plus its rank. Particles
+// past chunk_capacity give their slots back, so a full chunk ends at chunk_capacity as with one atomic per
+// particle; slot order within a chunk depends on scheduling either way. A group that finds the table full
+// (more than PUB_SLOTS chunks in one block) takes its own global atomic.
+constexpr int32_t PUB_PER_THREAD = 4, PUB_PER_BLOCK = PUB_PER_THREAD * T_PART, PUB_SLOTS = 64;
+
+__global__ void __launch_bounds__(T_PART)
+    k_pbf_publish(const PbfK k, const gpe_view vv, const gpe_view* __restrict__ vp, const float2* __restrict__ x,
+                  const float2* __restrict__ v, uint32_t* __restrict__ status)
 {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
+    __shared__ int32_t key[PUB_SLOTS], cnt[PUB_SLOTS], base[PUB_SLOTS];
     const gpe_view view = vp ? *vp : vv;
-    const float2 p   = x[i];
-    const float inv  = 1.f / view.chunk_dim;
-    const int32_t cx = min(max((int32_t)floorf((p.x - k.d0.ox) * inv), 0), view.chunks_x - 1);
-    const int32_t cy = min(max((int32_t)floorf((p.y - k.d0.oy) * inv), 0), view.chunks_y - 1);
-    const int32_t c  = cx + cy * view.chunks_x;
-    const int32_t s  = atomicAdd(&view.counts[c], 1);
-    if (s >= view.chunk_capacity) {
-        atomicOr(status, GPE_STATUS_CAPACITY);
-        atomicSub(&view.counts[c], 1);
-        return;
+    const int32_t n     = count_of(k);
+    const int32_t i0    = blockIdx.x * PUB_PER_BLOCK + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (int32_t t = threadIdx.x; t < PUB_SLOTS; t += blockDim.x) {
+        key[t] = -1;
+        cnt[t] = 0;
     }
-    const size_t o                            = (size_t)c * (size_t)view.chunk_capacity + (size_t)s;
-    reinterpret_cast<float2*>(view.pos)[o] = p;
-    reinterpret_cast<float2*>(view.vel)[o] = v[i];
+    __syncthreads();
+    const float inv = 1.f / view.chunk_dim;
+    int32_t c[PUB_PER_THREAD], slot[PUB_PER_THREAD], rank[PUB_PER_THREAD];
+    float2 p[PUB_PER_THREAD];
+#pragma unroll
+    for (int32_t j = 0; j < PUB_PER_THREAD; ++j) {
+        const int32_t i = i0 + j * T_PART;
+        c[j]            = -1;
+        if (i < n) {
+            p[j]             = x[i];
+            const int32_t cx = min(max((int32_t)floorf((p[j].x - k.d0.ox) * inv), 0), view.chunks_x - 1);
+            const int32_t cy = min(max((int32_t)floorf((p[j].y - k.d0.oy) * inv), 0), view.chunks_y - 1);
+            c[j]             = cx + cy * view.chunks_x;
+        }
+        const uint32_t group = __match_any_sync(0xffffffffu, c[j]);
+        const int32_t leader = __ffs(group) - 1;
+        const int32_t size   = __popc(group);
+        int32_t h = -1, r = 0;
+        if ((int32_t)lane == leader && c[j] >= 0) {
+            int32_t probe = 0;
+            for (h = (int32_t)(((uint32_t)c[j] * 2654435761u) >> 26); probe < PUB_SLOTS;
+                 ++probe, h = (h + 1) & (PUB_SLOTS - 1)) {
+                const int32_t old = atomicCAS(&key[h], -1, c[j]);
+                if (old == -1 || old == c[j]) { break; }
+            }
+            if (probe < PUB_SLOTS) {
+                r = atomicAdd(&cnt[h], size);
+            } else { // table full: the group's own global slots
+                h                  = -1;
+                r                  = atomicAdd(&view.counts[c[j]], size);
+                const int32_t over = min(r + size - view.chunk_capacity, size);
+                if (over > 0) {
+                    atomicOr(status, GPE_STATUS_CAPACITY);
+                    atomicSub(&view.counts[c[j]], over);
+                }
+            }
+        }
+        slot[j] = __shfl_sync(0xffffffffu, h, leader);
+        rank[j] = __shfl_sync(0xffffffffu, r, leader) + __popc(group & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    for (int32_t t = threadIdx.x; t < PUB_SLOTS; t += blockDim.x) {
+        if (key[t] < 0) { continue; }
+        const int32_t b    = atomicAdd(&view.counts[key[t]], cnt[t]);
+        const int32_t over = min(b + cnt[t] - view.chunk_capacity, cnt[t]);
+        if (over > 0) {
+            atomicOr(status, GPE_STATUS_CAPACITY);
+            atomicSub(&view.counts[key[t]], over);
+        }
+        base[t] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int32_t j = 0; j < PUB_PER_THREAD; ++j) {
+        if (c[j] < 0) { continue; }
+        const int32_t sl = slot[j] >= 0 ? base[slot[j]] + rank[j] : rank[j];
+        if (sl >= view.chunk_capacity) { continue; }
+        const size_t o                         = (size_t)c[j] * (size_t)view.chunk_capacity + (size_t)sl;
+        reinterpret_cast<float2*>(view.pos)[o] = p[j];
+        reinterpret_cast<float2*>(view.vel)[o] = v[i0 + j * T_PART];
+    }
 }
 
 __global__ void k_iota(uint32_t* __restrict__ a, int32_t n)
@@ -1941,7 +2005,8 @@ extern "C" int32_t gpe_pbf_publish(gpe_pbf* s, const gpe_view* view, int32_t vie
         GPE_CHECK_LAUNCH("k_view_zero");
     }
     if (lsize(s) > 0) {
-        k_pbf_publish<<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, vv, vp, s->pos[s->X], s->vel, s->status);
+        k_pbf_publish<<<(unsigned)((lsize(s) + PUB_PER_BLOCK - 1) / PUB_PER_BLOCK), T_PART, 0, st>>>(
+            s->k, vv, vp, s->pos[s->X], s->vel, s->status);
         GPE_CHECK_LAUNCH("k_pbf_publish");
     }
     return GPE_OK;

@@ -300,7 +300,7 @@ typedef struct gpe_raster {
     int32_t width, height;
     float scale;       /* pixels per scene unit (kSimScale, constants.h:59)                              */
     float chunk_dim;   /* chunk edge in scene units (kChunkDim, constants.h:48)                          */
-    int32_t* coverage; /* device scratch of width * height int32 (splats covering each pixel)           */
+    int32_t* coverage; /* device scratch of width * height int32 (splats centred on each pixel)        */
 } gpe_raster;
 /* view_mem: where the gpe_view struct lives (its arrays are device memory either way). */
 int32_t gpe_render_frame(const gpe_raster* raster, const gpe_view* view, int32_t view_mem, void* stream);

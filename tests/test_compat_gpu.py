@@ -178,6 +178,33 @@ def test_pbf_publish_host_and_device_view(gpe_mod, cuda_ok):
     _check_pbf_publish(bufs2, x, v, 12, 6, 32.0, 1536)
 
 
+def test_pbf_publish_overflowing_chunks(gpe_mod, cuda_ok):
+    """Chunks with more particles than chunk_capacity keep exactly chunk_capacity of them (PBFOutputKernel's
+    give-back of slots past the capacity), all distinct particles of that chunk, and raise the capacity
+    status bit."""
+    torch = pytest.importorskip("torch")
+    e, p, pos, vel, _ = _pbf(gpe_mod)
+    e.step(2)
+    x, v, _ = e.get_state()
+    cx, cy, dim, cap = 12, 6, 32.0, 64
+    view, bufs = _view(gpe_mod, torch, cx, cy, dim, cap)
+    e.publish(view)
+    torch.cuda.synchronize()
+    vpos, vvel, counts = (t.cpu().numpy() for t in bufs)
+    inv = np.float32(1.0 / dim)  # exact for dim = 32, as the kernel's x * (1 / chunk_dim)
+    kx = np.clip(np.floor(x[:, 0].astype(np.float32) * inv).astype(np.int64), 0, cx - 1)
+    ky = np.clip(np.floor(x[:, 1].astype(np.float32) * inv).astype(np.int64), 0, cy - 1)
+    true = np.bincount(kx + ky * cx, minlength=cx * cy)
+    assert true.max() > cap  # the block overflows some chunks
+    np.testing.assert_array_equal(counts, np.minimum(true, cap))
+    allrows = {tuple(r) for r in np.concatenate([x, v], 1).tolist()}
+    for c in range(cx * cy):
+        rows = np.concatenate([vpos[c * cap:c * cap + counts[c]], vvel[c * cap:c * cap + counts[c]]], 1)
+        got = [tuple(r) for r in rows.tolist()]
+        assert len(set(got)) == len(got) and all(r in allrows for r in got)
+    assert e.status() & gpe_mod.STATUS_CAPACITY
+
+
 def test_pbf_enqueue_captured_with_publish_replays(gpe_mod, cuda_ok):
     """enqueue + publish recorded into the caller's CUDA graph (instantiatePBFGraph's pattern), replayed with
     the device-resident view retargeted between replays (the reference's triple-buffered output), equals

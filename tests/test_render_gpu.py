@@ -70,3 +70,41 @@ def test_render_published_pbf_frame(gpe_mod, cuda_ok, oracle):
     np.testing.assert_array_equal(got, want)
     # the splats changed the picture where the fluid is
     assert (got[..., 2] != 80).sum() > len(pos)
+
+
+def test_render_device_view_captured_with_step_and_publish(gpe_mod, cuda_ok, oracle):
+    """enqueue + publish + render_frame recorded into one CUDA graph with the view struct in device memory
+    (read only by the kernels), replayed twice: each replay's image equals the oracle's drawing of the view
+    that replay published."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from gpe import scenes
+
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_pbf_block()
+    e = gpe_mod.Pbf(p, boxes, capacity=len(pos))
+    e.set_state(pos, vel)
+    cx, cy, dim, cap = 12, 6, 32.0, 1536
+    vp = torch.zeros((cx * cy * cap, 2), dtype=torch.float32, device="cuda")
+    vv = torch.zeros_like(vp)
+    vc = torch.zeros(cx * cy, dtype=torch.int32, device="cuda")
+    view = gpe_mod.View(vp.data_ptr(), vv.data_ptr(), vc.data_ptr(), cx, cy, dim, cap)
+    raw = bytes(C.string_at(C.addressof(view), C.sizeof(view)))
+    dview = torch.frombuffer(bytearray(raw), dtype=torch.uint8).cuda()
+    W, H = int(cx * dim * 5), int(cy * dim * 5)
+    r, img, _ = _raster(gpe_mod, torch, W, H, 5.0, dim, pad=0)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        st = torch.cuda.current_stream().cuda_stream
+        e.enqueue(3, stream=st)
+        e.publish(dview.data_ptr(), view_mem=gpe_mod.MEM_DEVICE, stream=st)
+        gpe_mod.render_frame(r, dview.data_ptr(), view_mem=gpe_mod.MEM_DEVICE, stream=st)
+    for _ in range(2):
+        g.replay()
+        torch.cuda.synchronize()
+        got = img.cpu().numpy().reshape(H, W, 4)
+        want = oracle.render_frame(W, H, 5.0, dim, vp.cpu().numpy().reshape(cx * cy, cap, 2), vc.cpu().numpy())
+        np.testing.assert_array_equal(got, want)
