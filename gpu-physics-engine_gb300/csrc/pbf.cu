@@ -50,6 +50,13 @@ struct PbfK {
     int32_t n;                // particle count when n_dev is null
     const int32_t* n_dev;     // device-resident particle count (emitters append on the device)
     DomDev d0; // the scene when there is only one
+    // candidate masks (cell h only): per particle the candidates within h + skin, per cell a mark that a
+    // particle of the 3 x 3 cells around it moved too far for them
+    const uint32_t* keys;     // sort cell of each slot
+    uint4* nmask;
+    uint8_t* mflag;
+    float skin2;              // (h + skin)^2
+    float move2;              // (skin / (2 iters))^2, shrunk by 1%
 };
 
 
@@ -83,6 +90,18 @@ __device__ __forceinline__ DomDev load_dom(const PbfK& k, const DomDev* __restri
     }
 }
 
+// A neighbour's value. Separate launches read through the read-only cache; inside the persistent solve
+// (CG) another block may have rewritten the value since this SM last cached it, so it is read from L2.
+template <bool CG, class T>
+__device__ __forceinline__ T ldn(const T* p)
+{
+    if constexpr (CG) {
+        return __ldcg(p);
+    } else {
+        return __ldg(p);
+    }
+}
+
 // Visits every particle index in the cells within R of the base cell of (px, py) (the reference scans the
 // 3x3 cells around clamp(floorf(x)/kCellDim), PBF.cu:252-263). Each row of cells is one contiguous range.
 template <class F>
@@ -103,18 +122,128 @@ __device__ __forceinline__ void for_neighbours(const DomDev& d, const PbfK& k, c
     }
 }
 
-
-// A neighbour's value. Separate launches read through the read-only cache; inside the persistent solve
-// (CG) another block may have rewritten the value since this SM last cached it, so it is read from L2.
-template <bool CG, class T>
-__device__ __forceinline__ T ldn(const T* p)
+// for_neighbours from a given base cell
+template <class F>
+__device__ __forceinline__ void for_neighbours_at(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
+                                                  int32_t bx, int32_t by, F&& f)
 {
-    if constexpr (CG) {
-        return __ldcg(p);
-    } else {
-        return __ldg(p);
+    const int32_t x0 = max(bx - k.R, 0);
+    const int32_t x1 = min(bx + k.R, d.ncx - 1);
+    const int32_t y0 = max(by - k.R, 0);
+    const int32_t y1 = min(by + k.R, d.ncy - 1);
+    for (int32_t y = y0; y <= y1; ++y) {
+        const uint32_t row = d.coff + (uint32_t)y * (uint32_t)d.ncx;
+        const uint32_t b   = __ldg(&start[row + x0]);
+        const uint32_t e   = __ldg(&start[row + x1 + 1]);
+        for (uint32_t j = b; j < e; ++j) { f(j); }
     }
 }
+
+// ----- candidate masks -----------------------------------------------------------------------------------
+// With sort cells of edge h a particle scans three rows of three cells, each row one contiguous range of
+// slots. The first plain lambda pass of a step records which candidates of each row lie within h + skin
+// (word r, bit t: the candidate at slot start[row r, first cell] + t), and the later passes of the step
+// visit only those. Every pair within h is still visited, in the scan order, as long as
+//   - the particle's base cell is still its sort cell (so its rows are the recorded ones), and
+//   - no particle of the 3 x 3 cells around it has moved by skin / 2 or more since the masks were made:
+//     a delta p pass that moves a particle by skin / (2 iters) or more marks the 9 cells around that
+//     particle's sort cell for the rest of the step, and a particle whose own cell is marked scans in full.
+// The terms of pairs beyond h are exact zeros in every sum (the sums start at +0, and adding a masked
+// +-0 leaves any value bit for bit), so masked and full scans give the same result.
+enum { MASK_OFF = 0, MASK_BUILD = 1, MASK_USE = 2 };
+constexpr uint32_t MASK_BAD = 0x80000000u; // in word 0: this particle's masks are not usable
+
+// The full scan of a particle whose base cell is (bx, by) (cell h, R = 1), recording its masks. f(j)
+// returns whether candidate j lies within h + skin.
+template <class F>
+__device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
+                                            int32_t by, F&& f)
+{
+    const int32_t x0 = max(bx - 1, 0);
+    const int32_t x1 = min(bx + 1, d.ncx - 1);
+    uint32_t w[3]    = {0u, 0u, 0u};
+    bool bad         = false;
+#pragma unroll
+    for (int32_t r = 0; r < 3; ++r) {
+        const int32_t y = by - 1 + r;
+        if (y < 0 || y >= d.ncy) { continue; }
+        const uint32_t row = d.coff + (uint32_t)y * (uint32_t)d.ncx;
+        const uint32_t b   = __ldg(&start[row + x0]);
+        const uint32_t e   = __ldg(&start[row + x1 + 1]);
+        bad                = bad || (e - b > 31u);
+        uint32_t wr        = 0u;
+        for (uint32_t j = b; j < e; ++j) {
+            const bool near = f(j);
+            const uint32_t t = j - b;
+            wr |= (near && t < 31u) ? (1u << t) : 0u;
+        }
+        w[r] = wr;
+    }
+    return make_uint4(w[0] | (bad ? MASK_BAD : 0u), w[1], w[2], 0u);
+}
+
+// Visits the candidates of the masks m around base cell (bx, by), in scan order.
+template <class F>
+__device__ __forceinline__ void scan_masked(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
+                                            int32_t by, const uint4 m, F&& f)
+{
+    const int32_t x0    = max(bx - 1, 0);
+    const uint32_t w[3] = {m.x, m.y, m.z};
+#pragma unroll
+    for (int32_t r = 0; r < 3; ++r) {
+        const int32_t y = by - 1 + r;
+        uint32_t bits   = w[r];
+        if (y < 0 || y >= d.ncy || bits == 0u) { continue; }
+        const uint32_t b = __ldg(&start[d.coff + (uint32_t)y * (uint32_t)d.ncx + x0]);
+        while (bits) {
+            const uint32_t t = (uint32_t)__ffs(bits) - 1u;
+            bits &= bits - 1u;
+            f(b + t);
+        }
+    }
+}
+
+// The neighbour scan of particle i at (px, py) in mask mode MASK. f(j) returns whether j lies within
+// h + skin (used by MASK_BUILD only).
+template <int MASK, bool CG, class F>
+__device__ __forceinline__ void scan(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start, float px,
+                                     float py, int32_t i, F&& f)
+{
+    if constexpr (MASK == MASK_OFF) {
+        for_neighbours(d, k, start, px, py, f);
+    } else {
+        const int32_t bx   = cell_coord(px, d.ox, k.inv_cell, d.ncx);
+        const int32_t by   = cell_coord(py, d.oy, k.inv_cell, d.ncy);
+        const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
+        if constexpr (MASK == MASK_BUILD) {
+            uint4 m = scan_build(d, start, bx, by, f);
+            if (key != __ldg(&k.keys[i])) { m.x |= MASK_BAD; } // built around another cell than the sort cell
+            k.nmask[i] = m;
+        } else {
+            const uint4 m = ldn<CG>(&k.nmask[i]);
+            if (!(m.x & MASK_BAD) && key == __ldg(&k.keys[i]) && ldn<CG>(&k.mflag[key]) == 0) {
+                scan_masked(d, start, bx, by, m, f);
+            } else {
+                for_neighbours_at(d, k, start, bx, by, f);
+            }
+        }
+    }
+}
+
+// A delta p pass moved particle i (sort cell key) by at least skin / (2 iters): the particles of the 3 x 3
+// cells around its sort cell scan in full for the rest of the step.
+__device__ __noinline__ void mark_mover(const DomDev& d, const PbfK& k, uint32_t key)
+{
+    const uint32_t local = key - d.coff;
+    const int32_t cy     = (int32_t)(local / (uint32_t)d.ncx);
+    const int32_t cx     = (int32_t)(local - (uint32_t)cy * (uint32_t)d.ncx);
+    for (int32_t y = max(cy - 1, 0); y <= min(cy + 1, d.ncy - 1); ++y) {
+        for (int32_t x = max(cx - 1, 0); x <= min(cx + 1, d.ncx - 1); ++x) {
+            k.mflag[d.coff + (uint32_t)y * (uint32_t)d.ncx + (uint32_t)x] = 1u;
+        }
+    }
+}
+
 
 // integer mixer of the reference (hash, cuda-internal.cuh:19-27)
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
@@ -216,7 +345,7 @@ __global__ void __launch_bounds__(T_PART)
 //           unclamped, and the pass moves the particles by the change of L; a sum that overshot is relaxed
 //           again and L never turns into a pull (accumulated-multiplier clamping).
 enum { ACC_NONE = 0, ACC_SUM = 1, ACC_PROJ = 2 };
-template <bool MULTI, bool SELFG, int ACC, bool CG = false>
+template <bool MULTI, bool SELFG, int ACC, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restrict__ doms,
                                            const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
                                            const float2* __restrict__ xs, float* __restrict__ lam,
@@ -234,7 +363,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     // Branch-free body: every lane of a warp runs the same instructions for every candidate and the terms of
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
-    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q  = ldn<CG>(&xs[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
         const float r2  = fmaf(rx, rx, ry * ry);
@@ -263,6 +392,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
             sy = fmaf(k.h2, ny, sy);
             s4 = fmaf(k.h2, k.h2, s4);
         }
+        return r2 < k.skin2;
     });
     if (self_seen) {
         s6 = fmaf(k.h2 * k.h2, k.h2, s6);
@@ -295,19 +425,21 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     }
 }
 
-template <bool MULTI, bool SELFG, int ACC>
-__global__ void __launch_bounds__(T_MAX)
+template <bool MULTI, bool SELFG, int ACC, int MASK>
+__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : 1) // the mask pass in 32 registers
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
              const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
              const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { lambda_one<MULTI, SELFG, ACC>(k, doms, dom, start, xs, lam, pair_id, acc, i); }
+    if (i < count_of(k)) {
+        lambda_one<MULTI, SELFG, ACC, false, MASK>(k, doms, dom, start, xs, lam, pair_id, acc, i);
+    }
 }
 
 // ----- delta p with artificial pressure and over-relaxation, then walls (PBF.cu:398-447, 471-499) -------
 // ACCINIT: this pass applies the warm start; its multiplier starts the step's running sum.
-template <bool MULTI, bool SCORR, bool ACCINIT, bool CG = false>
+template <bool MULTI, bool SCORR, bool ACCINIT, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restrict__ doms,
                                             const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
                                             const float2* __restrict__ xs, const float* __restrict__ lam,
@@ -322,7 +454,7 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     // closer than 1e-6 (the self pair included) have a zero direction there and are skipped here.
     const float c6w = k.c6 * k.inv_w_dq;
     float sx = 0.f, sy = 0.f;
-    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q  = ldn<CG>(&xs[j]);
         const float lj  = ldn<CG>(&lam[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
@@ -340,6 +472,7 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
         const float w    = ok ? diff * diff * inv * l : 0.f;
         sx               = fmaf(w, rx, sx);
         sy               = fmaf(w, ry, sy);
+        return false;
     });
     const float s = -k.cs * k.dp_scale;
     float ox = fmaf(s, sx, p.x), oy = fmaf(s, sy, p.y);
@@ -347,23 +480,29 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
     ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
     xs_out[i] = make_float2(ox, oy);
+    if constexpr (MASK == MASK_USE) {
+        const float mx = ox - p.x, my = oy - p.y;
+        if (!(fmaf(mx, mx, my * my) < k.move2)) { mark_mover(d, k, __ldg(&k.keys[i])); }
+    }
 }
 
-template <bool MULTI, bool SCORR, bool ACCINIT>
+template <bool MULTI, bool SCORR, bool ACCINIT, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
               const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
               float2* __restrict__ xs_out, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { delta_p_one<MULTI, SCORR, ACCINIT>(k, doms, dom, start, xs, lam, xs_out, acc, i); }
+    if (i < count_of(k)) {
+        delta_p_one<MULTI, SCORR, ACCINIT, false, MASK>(k, doms, dom, start, xs, lam, xs_out, acc, i);
+    }
 }
 
 // ----- warm start: features of the first lambda pass ------------------------------------------------------
 // The lambda sums of k_lambda plus the neighbour count and the poly6-weighted sum of the neighbours'
 // lambda_prev; returns the cold first-iteration lambda and fills the network's 12 features (the order is
 // the one documented with gpe_pbf_set_warm_start).
-template <bool MULTI, bool SELFG>
+template <bool MULTI, bool SELFG, int MASK = MASK_OFF>
 __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, const uint32_t* __restrict__ start,
                                                const float2* __restrict__ xs, const float2* __restrict__ xsorted,
                                                const float* __restrict__ prev, const uint32_t* __restrict__ pair_id,
@@ -373,7 +512,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
     float sx = 0.f, sy = 0.f, s4 = 0.f, s6 = 0.f, swl = 0.f;
     int32_t nn     = 0;
     bool self_seen = false;
-    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+    scan<MASK, false>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q  = __ldg(&xs[j]);
         const float lp  = __ldg(&prev[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
@@ -404,6 +543,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
             sy = fmaf(k.h2, ny, sy);
             s4 = fmaf(k.h2, k.h2, s4);
         }
+        return r2 < k.skin2;
     });
     const float lpi = prev[i];
     if (self_seen) {
@@ -451,7 +591,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
 // memory with one bulk copy. (Computing the features inside the tensor-core kernel caps the neighbour loop
 // at the 7 CTAs of 4 warps that fit an SM beside their TMEM and operand tiles: 126 us against about 50 us
 // here at 1M particles.)
-template <bool MULTI, bool SELFG>
+template <bool MULTI, bool SELFG, int MASK>
 __global__ void __launch_bounds__(T_PART)
     k_lambda_feat(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
                   const uint32_t* __restrict__ start, const float2* __restrict__ xs,
@@ -463,7 +603,7 @@ __global__ void __launch_bounds__(T_PART)
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     float f[MLP_F];
-    (void)warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    (void)warm_features<MULTI, SELFG, MASK>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
     float mu[MLP_FP], isd[MLP_FP];
 #pragma unroll
     for (int q = 0; q < MLP_FP; ++q) {
@@ -579,7 +719,7 @@ __device__ __forceinline__ void velocity_clamp(const PbfK& k, float& vx, float& 
 }
 
 // ----- velocity + XSPH (+ vorticity omega) (PBF.cu:538, 585-627) ---------------------------------------
-template <bool MULTI, bool VORT, bool CG = false>
+template <bool MULTI, bool VORT, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict__ doms,
                                          const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
                                          const float2* __restrict__ x, const float2* __restrict__ xs,
@@ -593,7 +733,7 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     // dv = c sum (v_j - v_i) W6 (PBF.cu:602-615) with the poly6 coefficient hoisted; the self pair adds 0.
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float dvx = 0.f, dvy = 0.f, w = 0.f;
-    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q  = ldn<CG>(&xs[j]);
         const float2 qo = ldn<CG>(&x[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
@@ -613,6 +753,7 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
             const float gm   = dir ? diff * diff * inv : 0.f;
             w                = fmaf(gm, fmaf(dx, ry, -(dy * rx)), w);
         }
+        return false;
     });
     w *= k.cs;
     const float cx = k.xsph_c * k.c6;
@@ -626,18 +767,18 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     if (VORT) { omega[i] = w; }
 }
 
-template <bool MULTI, bool VORT>
+template <bool MULTI, bool VORT, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_xsph(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
            const uint32_t* __restrict__ start, const float2* __restrict__ x, const float2* __restrict__ xs,
            float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { xsph_one<MULTI, VORT>(k, doms, dom, start, x, xs, v_out, omega, status, i); }
+    if (i < count_of(k)) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, x, xs, v_out, omega, status, i); }
 }
 
 // ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
-template <bool MULTI, bool CG = false>
+template <bool MULTI, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __restrict__ doms,
                                               const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
                                               const float2* __restrict__ xs, const float* __restrict__ omega,
@@ -648,7 +789,7 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
     const float wi = omega[i];
     const float aw = fabsf(wi);
     float ex = 0.f, ey = 0.f;
-    for_neighbours(d, k, start, p.x, p.y, [&](uint32_t j) {
+    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q   = ldn<CG>(&xs[j]);
         const float wj   = ldn<CG>(&omega[j]);
         const float rx = p.x - q.x, ry = p.y - q.y;
@@ -659,6 +800,7 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
         const float dwg  = ok ? (fabsf(wj) - aw) * (diff * diff * inv) : 0.f; // grad_i W = -cs (...)
         ex               = fmaf(dwg, rx, ex);
         ey               = fmaf(dwg, ry, ey);
+        return false;
     });
     // only the direction of eta = grad|omega| is used, so the positive factor cs drops out; the sign stays
     ex             = -ex;
@@ -674,14 +816,14 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
     v[i] = vv;
 }
 
-template <bool MULTI>
+template <bool MULTI, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_vorticity(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
                 const uint32_t* __restrict__ start, const float2* __restrict__ xs,
                 const float* __restrict__ omega, float2* __restrict__ v)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { vorticity_one<MULTI>(k, doms, dom, start, xs, omega, v, i); }
+    if (i < count_of(k)) { vorticity_one<MULTI, false, MASK>(k, doms, dom, start, xs, omega, v, i); }
 }
 
 // ----- the persistent solve: every Jacobi pass (and XSPH) of a step in one launch -----------------------
@@ -730,7 +872,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
 
 // XSPH: the velocity pass runs here too; with vorticity confinement it runs as its usual launch after the
 // kernel instead (the omega-carrying pass inlined here differs from its own kernel in the last bit).
-template <bool MULTI, bool SELFG, bool SCORR, bool XSPH>
+template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
 __global__ void __launch_bounds__(T_MAX)
     k_solve_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
                        const uint32_t* __restrict__ start, float2* __restrict__ xs_a, float2* __restrict__ xs_b,
@@ -744,13 +886,20 @@ __global__ void __launch_bounds__(T_MAX)
     unsigned int gen     = 0u; // the barrier word is zeroed before every launch
     float2* cur          = xs_a;
     float2* nxt          = xs_b;
+    constexpr int MU = MASKS ? MASK_USE : MASK_OFF;
     for (int32_t it = 0; it < iters; ++it) {
-        for (int32_t i = i0; i < n; i += stride) {
-            lambda_one<MULTI, SELFG, ACC_NONE, true>(k, doms, dom, start, cur, lam, pair_id, nullptr, i);
+        if (MASKS && it == 0) {
+            for (int32_t i = i0; i < n; i += stride) {
+                lambda_one<MULTI, SELFG, ACC_NONE, true, MASK_BUILD>(k, doms, dom, start, cur, lam, pair_id, nullptr, i);
+            }
+        } else {
+            for (int32_t i = i0; i < n; i += stride) {
+                lambda_one<MULTI, SELFG, ACC_NONE, true, MU>(k, doms, dom, start, cur, lam, pair_id, nullptr, i);
+            }
         }
         if (!grid_barrier(gs, gen, status)) { return; }
         for (int32_t i = i0; i < n; i += stride) {
-            delta_p_one<MULTI, SCORR, false, true>(k, doms, dom, start, cur, lam, nxt, nullptr, i);
+            delta_p_one<MULTI, SCORR, false, true, MU>(k, doms, dom, start, cur, lam, nxt, nullptr, i);
         }
         if (!grid_barrier(gs, gen, status)) { return; }
         float2* t = cur;
@@ -759,7 +908,7 @@ __global__ void __launch_bounds__(T_MAX)
     }
     if (XSPH) {
         for (int32_t i = i0; i < n; i += stride) {
-            xsph_one<MULTI, false, true>(k, doms, dom, start, x, cur, v, omega, status, i);
+            xsph_one<MULTI, false, true, MU>(k, doms, dom, start, x, cur, v, omega, status, i);
         }
     }
 }
@@ -1018,8 +1167,15 @@ struct gpe_pbf {
     int32_t block     = 256;      // threads per block of the neighbour kernels (tuning)
     bool persistent   = false;    // plain steps run their passes in one persistent launch (tuning)
     int32_t coop_grid = 0;        // blocks of the persistent launch (all resident)
+    const void* coop_fn = nullptr; // the kernel coop_grid was sized for
     GridSync* gsync   = nullptr;  // its barrier word
     uint16_t* feat    = nullptr;  // network operand tiles (GPE_WARM_MLP), allocated on demand
+    float skin        = 0.1f;     // candidate-mask skin in units of h (tuning; 0: full scans only)
+    uint4* nmask      = nullptr;  // candidate masks of the current step
+    uint8_t* mflag    = nullptr;  // per cell: a particle of its 3 x 3 cells moved too far for the masks
+    bool masks_valid  = false;    // the masks were made in this step
+    int32_t dp_since_build = 0;   // delta p passes since they were made
+    int32_t mask_passes = 1;      // delta p passes the move threshold k.move2 allows for
 
     // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
     int X = 0, SX = -1, XS = -1, XO = -1;
@@ -1098,6 +1254,25 @@ PbfK make_k(const gpe_pbf_params& p)
     return k;
 }
 
+// the engine's buffers and mask thresholds in the kernel constants
+void bind_k(gpe_pbf* s)
+{
+    s->k.n_dev       = s->d_count;
+    s->k.keys        = s->keys;
+    s->k.nmask       = s->nmask;
+    s->k.mflag       = s->mflag;
+    const float skin = s->skin * s->prm.h;
+    s->k.skin2       = (s->prm.h + skin) * (s->prm.h + skin);
+    // each of the step's delta p passes may move a particle by less than this, so all of them together
+    // by less than skin / 2 (with 5% to spare for rounding)
+    s->mask_passes   = std::max(s->prm.iters, 1);
+    const float mv   = 0.95f * skin / (2.f * (float)s->mask_passes);
+    s->k.move2       = mv * mv;
+}
+
+// masks in this engine's configuration: cell h (3 x 3 scan), a skin, at least one iteration
+bool masks_on(const gpe_pbf* s) { return s->skin > 0.f && s->k.R == 1 && s->prm.iters > 0; }
+
 int32_t cells_along(float extent, float cell)
 {
     const int32_t c = (int32_t)std::ceil(extent / cell);
@@ -1126,7 +1301,7 @@ void build_domains(gpe_pbf* s)
     s->ncells  = (uint32_t)off;
     s->k       = make_k(s->prm);
     s->k.d0    = s->domdev[0];
-    s->k.n_dev = s->d_count;
+    bind_k(s);
 }
 
 // Launch size: with a device-resident count that emitters can grow inside a captured graph, every launch
@@ -1162,6 +1337,7 @@ unsigned nblk(const gpe_pbf* s) { return (unsigned)((lsize(s) + s->block - 1) / 
 
 int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 {
+    s->masks_valid  = false;
     const int32_t n = (int32_t)lsize(s);
     // roles for this step: the three buffers other than X, in order
     int fr[3], c = 0;
@@ -1205,12 +1381,20 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 
 // Template dispatch tables: [multi scene][flag][accumulation mode]
 using LamFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                       const float2*, float*, const uint32_t*, float*);
+                       const float2*, float*, const uint32_t*, float*, int);
 template <bool M, bool S, int A>
 void lam_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc)
+                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc, int mask)
 {
-    k_lambda<M, S, A><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    if constexpr (A == ACC_PROJ) { // the projected-increment ablation keeps full scans
+        k_lambda<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    } else if (mask == MASK_BUILD) {
+        k_lambda<M, S, A, MASK_BUILD><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    } else if (mask == MASK_USE) {
+        k_lambda<M, S, A, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    } else {
+        k_lambda<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+    }
 }
 #define GPE_LAM3(M, S) {lam_launch<M, S, ACC_NONE>, lam_launch<M, S, ACC_SUM>, lam_launch<M, S, ACC_PROJ>}
 const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
@@ -1218,12 +1402,16 @@ const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
 #undef GPE_LAM3
 
 using DpFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                      const float2*, const float*, float2*, float*);
+                      const float2*, const float*, float2*, float*, int);
 template <bool M, bool S, bool A>
 void dp_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-               const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc)
+               const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc, int mask)
 {
-    k_delta_p<M, S, A><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+    if (mask == MASK_USE) {
+        k_delta_p<M, S, A, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+    } else {
+        k_delta_p<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+    }
 }
 const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, false, true>},
                             {dp_launch<false, true, false>, dp_launch<false, true, true>}},
@@ -1231,13 +1419,17 @@ const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, fa
                             {dp_launch<true, true, false>, dp_launch<true, true, true>}}};
 
 using FeatFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                        const float2*, const float2*, const float*, const uint32_t*, const MlpDev*, uint16_t*);
+                        const float2*, const float2*, const float*, const uint32_t*, const MlpDev*, uint16_t*, int);
 template <bool M, bool S>
 void feat_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                  const uint32_t* start, const float2* xs, const float2* xo, const float* prev, const uint32_t* pid,
-                 const MlpDev* mlp, uint16_t* feat)
+                 const MlpDev* mlp, uint16_t* feat, int mask)
 {
-    k_lambda_feat<M, S><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+    if (mask == MASK_BUILD) {
+        k_lambda_feat<M, S, MASK_BUILD><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+    } else {
+        k_lambda_feat<M, S, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+    }
 }
 const FeatFn kFeat[2][2] = {{feat_launch<false, false>, feat_launch<false, true>},
                             {feat_launch<true, false>, feat_launch<true, true>}};
@@ -1255,12 +1447,17 @@ const ColFn kCol[2][2] = {{col_launch<false, false>, col_launch<false, true>},
                           {col_launch<true, false>, col_launch<true, true>}};
 
 using XsFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                      const float2*, const float2*, float2*, float*, uint32_t*);
+                      const float2*, const float2*, float2*, float*, uint32_t*, int);
 template <bool M, bool V>
 void xs_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-               const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status)
+               const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status,
+               int mask)
 {
-    k_xsph<M, V><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+    if (mask == MASK_USE) {
+        k_xsph<M, V, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+    } else {
+        k_xsph<M, V, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+    }
 }
 const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
                         {xs_launch<true, false>, xs_launch<true, true>}};
@@ -1279,9 +1476,18 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st, int acc)
     if (lsize(s) == 0) { return GPE_OK; }
     const int sg        = (s->prm.flags & GPE_PBF_SELF_GRAD) ? 1 : 0;
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
+    int mask = MASK_OFF;
+    if (masks_on(s) && acc != ACC_PROJ) {
+        mask = s->masks_valid ? MASK_USE : MASK_BUILD;
+        if (mask == MASK_BUILD) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
+    }
     kLam[multi(s) ? 1 : 0][sg][acc](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
-                                    s->lam, pid, s->acc);
+                                    s->lam, pid, s->acc, mask);
     GPE_CHECK_LAUNCH("k_lambda");
+    if (mask == MASK_BUILD) {
+        s->masks_valid    = true;
+        s->dp_since_build = 0;
+    }
     s->launches += 1;
     return GPE_OK;
 }
@@ -1298,9 +1504,16 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
     if (s->warm == GPE_WARM_MLP && s->mem_valid && !s->collecting) {
         const gpe::MlpDev* md = gpe::mlp_device(s->mlp);
+        // the feature pass scans every neighbour on the sorted positions: it makes the step's masks
+        const int mask = masks_on(s) ? MASK_BUILD : MASK_OFF;
+        if (mask == MASK_BUILD) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
         kFeat[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
-                      s->prev, pid, md, s->feat);
+                      s->prev, pid, md, s->feat, mask);
         GPE_CHECK_LAUNCH("k_lambda_feat");
+        if (mask == MASK_BUILD) {
+            s->masks_valid    = true;
+            s->dp_since_build = 0;
+        }
         const int64_t tiles = (lsize(s) + MLP_TILE - 1) / MLP_TILE;
         const unsigned g    = (unsigned)std::min<int64_t>(tiles, s->lam_grid);
         k_mlp_apply<<<g, MLP_TILE, 0, st>>>(s->k, s->feat, s->prev, s->lam, md, s->status);
@@ -1319,8 +1532,13 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
 {
     if (lsize(s) > 0) {
         const int sc = s->prm.scorr_k != 0.f ? 1 : 0;
+        // the move threshold covers mask_passes passes after the masks were made (a step with more
+        // iterations, such as the one that starts the network's memory, scans in full after those)
+        if (s->masks_valid && s->dp_since_build >= s->mask_passes) { s->masks_valid = false; }
+        const int mask = s->masks_valid ? MASK_USE : MASK_OFF;
+        s->dp_since_build += 1;
         kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
-                                                   s->pos[s->XS], s->lam, s->pos[s->XO], s->acc);
+                                                   s->pos[s->XS], s->lam, s->pos[s->XO], s->acc, mask);
         GPE_CHECK_LAUNCH("k_delta_p");
         s->launches += 1;
     }
@@ -1333,7 +1551,7 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
     if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
     kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                s->pos[s->XS], s->vel, s->omega, s->status);
+                                s->pos[s->XS], s->vel, s->omega, s->status, s->masks_valid ? MASK_USE : MASK_OFF);
     GPE_CHECK_LAUNCH("k_xsph");
     s->launches += 1;
     return GPE_OK;
@@ -1343,11 +1561,23 @@ int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) == 0 || s->prm.vort_eps == 0.f) { return GPE_OK; }
     const unsigned g = nblk(s);
+    const bool mu = s->masks_valid;
     if (multi(s)) {
-        k_vorticity<true><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega, s->vel);
+        if (mu) {
+            k_vorticity<true, MASK_USE><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                         s->pos[s->XS], s->omega, s->vel);
+        } else {
+            k_vorticity<true, MASK_OFF><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                         s->pos[s->XS], s->omega, s->vel);
+        }
     } else {
-        k_vorticity<false><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->omega,
-                                                 s->vel);
+        if (mu) {
+            k_vorticity<false, MASK_USE><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                          s->pos[s->XS], s->omega, s->vel);
+        } else {
+            k_vorticity<false, MASK_OFF><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
+                                                                          s->pos[s->XS], s->omega, s->vel);
+        }
     }
     GPE_CHECK_LAUNCH("k_vorticity");
     s->launches += 1;
@@ -1356,38 +1586,45 @@ int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 
 int32_t stage_finish(gpe_pbf* s)
 {
+    s->masks_valid = false;
     s->X  = s->XS;
     s->SX = s->XS = s->XO = -1;
     return GPE_OK;
 }
 
 // The Jacobi passes and XSPH of a plain step in one cooperative launch (k_solve_persistent).
-template <bool M, bool S, bool C, bool V>
+template <bool M, bool S, bool C, bool V, bool K>
 const void* solve_fn()
 {
-    return reinterpret_cast<const void*>(k_solve_persistent<M, S, C, V>);
+    return reinterpret_cast<const void*>(k_solve_persistent<M, S, C, V, K>);
+}
+template <bool K>
+const void* solve_kernel_k(bool m, bool sg, bool sc, bool v)
+{
+    const void* tab[16] = {
+        solve_fn<false, false, false, false, K>(), solve_fn<false, false, false, true, K>(),
+        solve_fn<false, false, true, false, K>(),  solve_fn<false, false, true, true, K>(),
+        solve_fn<false, true, false, false, K>(),  solve_fn<false, true, false, true, K>(),
+        solve_fn<false, true, true, false, K>(),   solve_fn<false, true, true, true, K>(),
+        solve_fn<true, false, false, false, K>(),  solve_fn<true, false, false, true, K>(),
+        solve_fn<true, false, true, false, K>(),   solve_fn<true, false, true, true, K>(),
+        solve_fn<true, true, false, false, K>(),   solve_fn<true, true, false, true, K>(),
+        solve_fn<true, true, true, false, K>(),    solve_fn<true, true, true, true, K>()};
+    return tab[(m ? 8 : 0) + (sg ? 4 : 0) + (sc ? 2 : 0) + (v ? 1 : 0)];
 }
 const void* solve_kernel(const gpe_pbf* s)
 {
     const bool m = multi(s), sg = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0, sc = s->prm.scorr_k != 0.f,
                v = s->prm.vort_eps == 0.f; // XSPH inside the kernel
-    const void* tab[16] = {
-        solve_fn<false, false, false, false>(), solve_fn<false, false, false, true>(),
-        solve_fn<false, false, true, false>(),  solve_fn<false, false, true, true>(),
-        solve_fn<false, true, false, false>(),  solve_fn<false, true, false, true>(),
-        solve_fn<false, true, true, false>(),   solve_fn<false, true, true, true>(),
-        solve_fn<true, false, false, false>(),  solve_fn<true, false, false, true>(),
-        solve_fn<true, false, true, false>(),   solve_fn<true, false, true, true>(),
-        solve_fn<true, true, false, false>(),   solve_fn<true, true, false, true>(),
-        solve_fn<true, true, true, false>(),    solve_fn<true, true, true, true>()};
-    return tab[(m ? 8 : 0) + (sg ? 4 : 0) + (sc ? 2 : 0) + (v ? 1 : 0)];
+    return masks_on(s) ? solve_kernel_k<true>(m, sg, sc, v) : solve_kernel_k<false>(m, sg, sc, v);
 }
 
 int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) > 0) {
         const void* fn = solve_kernel(s);
-        if (s->coop_grid <= 0) {
+        if (s->coop_grid <= 0 || s->coop_fn != fn) {
+            s->coop_fn = fn;
             int per_sm = 0;
             GPE_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, s->block, 0));
             s->coop_grid = std::max(1, per_sm) * gpe::sm_count();
@@ -1401,6 +1638,7 @@ int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
         void* args[]        = {&k,  &s->d_doms, &s->dom, &s->start, &xa,   &xb,        &xsort,
                                &s->lam, &pid, &s->vel, &s->omega, &iters, &s->gsync, &s->status};
         GPE_TRY_CUDA(cudaMemsetAsync(s->gsync, 0, sizeof(GridSync), st));
+        if (masks_on(s)) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
         GPE_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)s->coop_grid), dim3((unsigned)s->block), args, 0,
                                                  st));
         s->launches += 1;
@@ -1474,6 +1712,8 @@ int32_t alloc_buffers(gpe_pbf* s)
     const size_t o_acc   = c.take<float>(N);
     const size_t o_prev  = c.take<float>(N);
     const size_t o_gs    = c.take<GridSync>(1);
+    const size_t o_nm    = c.take<uint4>(N);
+    const size_t o_mf    = c.take<uint8_t>(M);
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -1500,7 +1740,9 @@ int32_t alloc_buffers(gpe_pbf* s)
     s->acc     = reinterpret_cast<float*>(b + o_acc);
     s->prev    = reinterpret_cast<float*>(b + o_prev);
     s->gsync   = reinterpret_cast<GridSync*>(b + o_gs);
-    s->k.n_dev = s->d_count;
+    s->nmask   = reinterpret_cast<uint4*>(b + o_nm);
+    s->mflag   = b + o_mf;
+    bind_k(s);
     GPE_TRY_CUDA(cudaMemcpy(s->d_doms, s->domdev.data(), sizeof(DomDev) * (size_t)s->nd, cudaMemcpyHostToDevice));
     return GPE_OK;
 }
@@ -1922,6 +2164,7 @@ int32_t gpe_pbf_set_field(gpe_pbf* s, int32_t field, const void* src, int64_t n_
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_field: field %d is derived and read-only", field);
         return GPE_ERR_BAD_ARG;
     }
+    s->masks_valid = false; // a written position (or anything else) may move a particle past its masks
     void* p;
     size_t es;
     int64_t cnt;
@@ -2052,8 +2295,9 @@ namespace {
 int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
 {
     if (!(t.cell >= 0.f) || (t.block != 128 && t.block != 256 && t.block != 512) ||
-        (t.persistent != 0 && t.persistent != 1)) {
-        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0 or 1");
+        (t.persistent != 0 && t.persistent != 1) || !(t.skin >= 0.f && t.skin <= 1.f)) {
+        gpe::set_error(GPE_ERR_BAD_ARG,
+                       "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0 or 1, skin in [0, 1]");
         return GPE_ERR_BAD_ARG;
     }
     const float c_old = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
@@ -2079,6 +2323,8 @@ int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
     if (t.block != s->block) { s->coop_grid = 0; }
     s->block      = t.block;
     s->persistent = t.persistent != 0;
+    s->skin       = t.skin;
+    bind_k(s);
     s->drop_graphs();
     return GPE_OK;
 }
@@ -2102,6 +2348,7 @@ extern "C" int32_t gpe_pbf_get_tuning(const gpe_pbf* s, gpe_pbf_tuning* t)
     t->cell       = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
     t->block      = s->block;
     t->persistent = s->persistent ? 1 : 0;
+    t->skin       = s->skin;
     return GPE_OK;
 }
 
@@ -2176,12 +2423,14 @@ extern "C" int32_t gpe_pbf_autotune(gpe_pbf* s, int32_t trial_steps, gpe_pbf_tun
     if (rc == GPE_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) {
         rc = GPE_ERR_CUDA;
     }
-    const float cells[2] = {s->prm.h, 0.5f * s->prm.h};
+    // cell h with and without candidate masks (skin 0.1 h), and h/2 (no masks: its scan has five rows)
+    const float cells[3] = {s->prm.h, s->prm.h, 0.5f * s->prm.h};
+    const float skins[3] = {0.1f, 0.f, 0.f};
     const int32_t blocks[3] = {128, 256, 512};
-    for (int ci = 0; ci < 2 && rc == GPE_OK; ++ci) {
+    for (int ci = 0; ci < 3 && rc == GPE_OK; ++ci) {
         for (int bi = 0; bi < 3 && rc == GPE_OK; ++bi) {
             for (int pi = 0; pi < 2 && rc == GPE_OK; ++pi) {
-                const gpe_pbf_tuning cand{cells[ci], blocks[bi], pi};
+                const gpe_pbf_tuning cand{cells[ci], blocks[bi], pi, skins[ci]};
                 if (apply_tuning(s, cand) != GPE_OK) { continue; } // e.g. the h/2 grid does not fit
                 rc = restore();
                 if (rc) { break; }

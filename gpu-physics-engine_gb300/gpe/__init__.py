@@ -90,7 +90,7 @@ def render_frame(raster: "Raster", view, view_mem: int = MEM_HOST, stream=None) 
 
 
 class Tuning(C.Structure):
-    _fields_ = [("cell", C.c_float), ("block", C.c_int32), ("persistent", C.c_int32)]
+    _fields_ = [("cell", C.c_float), ("block", C.c_int32), ("persistent", C.c_int32), ("skin", C.c_float)]
 
 
 class TrainParams(C.Structure):
@@ -367,8 +367,8 @@ class Pbf:
         check(lib().gpe_pbf_get_tuning(self.h, C.byref(t)), "gpe_pbf_get_tuning")
         return t
 
-    def set_tuning(self, cell: float = 0.0, block: int = 256, persistent: bool = False) -> None:
-        t = Tuning(cell, block, 1 if persistent else 0)
+    def set_tuning(self, cell: float = 0.0, block: int = 256, persistent: bool = False, skin: float = 0.1) -> None:
+        t = Tuning(cell, block, 1 if persistent else 0, skin)
         check(lib().gpe_pbf_set_tuning(self.h, C.byref(t)), "gpe_pbf_set_tuning")
 
     def autotune(self, trial_steps: int = 4, stream=None) -> tuple[Tuning, float]:

@@ -318,13 +318,20 @@ typedef struct gpe_pbf_tuning {
                            with grid barriers between them (for many small scenes, whose steps are
                            otherwise launch-bound; vorticity keeps its own launches); 0: one launch
                            per pass                                                                     */
+    float skin;         /* candidate masks, in units of h, in [0, 1] (cell h only; default 0.1): the
+                           first lambda pass of a step records per particle which candidates of its
+                           3 x 3 cells lie within h + skin * h, and the later passes of the step visit
+                           only those while no particle nearby has moved by skin * h / 2 (else that
+                           particle's neighbourhood scans in full). Same result bit for bit; 0 turns
+                           the masks off                                                                */
 } gpe_pbf_tuning;
 
 int32_t gpe_pbf_get_tuning(const gpe_pbf* pbf, gpe_pbf_tuning* tuning);
 /* A new cell size rebuilds the scenes' sort grids (the engine holds cell arrays for h/2 and for the cell
  * size it was created with). */
 int32_t gpe_pbf_set_tuning(gpe_pbf* pbf, const gpe_pbf_tuning* tuning);
-/* Times trial_steps steps of every candidate (cell h or h/2, block 128, 256 or 512, persistent or not) on
+/* Times trial_steps steps of every candidate (cell h with skin 0.1 or without masks, or h/2; block 128,
+ * 256 or 512; persistent or not) on
  * the current state, which is restored after every trial and at the end, and applies the fastest;
  * *best and *ms_per_step receive it and its time (-1 when the choice came from the cache). Choices are
  * cached for the process per (scenes, particle count and mean scene aspect to the nearest power of two,

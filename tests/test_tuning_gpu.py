@@ -87,7 +87,7 @@ def test_autotune_restores_state_and_caches(gpe_mod, cuda_ok):
     e.step(2)
     got = e.get_state()
     ref = _run(gpe_mod, p, pos, vel, dom, boxes, steps=2,
-               tuning=dict(cell=best.cell, block=best.block, persistent=bool(best.persistent)))
+               tuning=dict(cell=best.cell, block=best.block, persistent=bool(best.persistent), skin=best.skin))
     for a, b in zip(ref, got):
         np.testing.assert_array_equal(a, b)
     # a second engine with the same scenes takes the choice from the cache
