@@ -395,6 +395,8 @@ def mpm_leg(args, stream, flush_l2):
     mixed: 4,194,304 particles (a third each of water, snow and jelly in seeded discs) on a 1024^2 grid,
            dt = 5e-5, spatial re-sort every 16 steps; algorithmic bytes 136 per particle (x, v, C, F, J,
            material and plastic state read and written once) plus 64 per grid node;
+    library: the same grid and particle count with a fifth each of water, jelly, snow, Neo-Hookean and
+           Drucker-Prager sand (two discs each);
     elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid, dt = 1e-4 (launch-bound)."""
     import torch
 
@@ -432,6 +434,10 @@ def mpm_leg(args, stream, flush_l2):
     p = scenes.mixed_params(n)
     pos, mat = scenes.mixed_discs(n)
     out["mixed_4m"] = timed(p, pos, np.zeros_like(pos), mat, 136.0 * n + 64.0 * p.nx * p.ny)
+    # the whole constitutive library in one scene: water, jelly (corotated), snow, Neo-Hookean and sand
+    lib = (gpe.MPM_MAT_FLUID, gpe.MPM_MAT_COROTATED, gpe.MPM_MAT_SNOW, gpe.MPM_MAT_NEOHOOKEAN, gpe.MPM_MAT_SAND)
+    pos, mat = scenes.mixed_discs(n, seed=5, discs_per_material=2, materials=lib)
+    out["library_4m"] = timed(p, pos, np.zeros_like(pos), mat, 136.0 * n + 64.0 * p.nx * p.ny)
     pe = scenes.elastic_params()
     pos, vel = scenes.two_squares()
     out["elastic_65k"] = timed(pe, pos, vel, None, 120.0 * len(pos) + 64.0 * pe.nx * pe.ny)

@@ -38,6 +38,8 @@ struct MpmK {
     uint32_t flags;
     float k_bulk, gamma, p_min, p_max, J_min, J_max;
     float mu0, la0, theta_c, theta_s, hardening;
+    float sh0, sh1, sh2, sh3; // sand friction-angle hardening, degrees
+    float sand_cf;            // (d la + 2 mu) / (2 mu), d = 2
     float apic_s; // 4 / dx^2
     int32_t n;            // particle count when n_dev is null
     const int32_t* n_dev; // device-resident count (the reference's num_points[0], MPM.cu:64)
@@ -48,7 +50,13 @@ namespace {
 constexpr int T_MPM     = 256;
 constexpr int TILE_CAP  = 2048; // nodes of the shared-memory accumulation tile (24 KB)
 
-enum MatMode { MODE_FLUID = 0, MODE_COROT = 1, MODE_SNOW = 2, MODE_MIXED = 3 };
+// single-material modes are the material ids; MODE_MIXED reads an id per particle
+enum MatMode { MODE_FLUID = 0, MODE_COROT = 1, MODE_SNOW = 2, MODE_NEOHOOKEAN = 3, MODE_SAND = 4, MODE_MIXED = 8 };
+
+// materials whose particles carry F / J between steps (corotated and Neo-Hookean need no J: their volume
+// is det F; the fluid keeps F only when asked to, as the reference does)
+__device__ __forceinline__ bool keeps_f(int m, bool track_f) { return m != MODE_FLUID || track_f; }
+__device__ __forceinline__ bool keeps_j(int m) { return m == MODE_FLUID || m == MODE_SNOW || m == MODE_SAND; }
 
 __device__ __forceinline__ int32_t count_of(const MpmK& k) { return k.n_dev ? __ldg(k.n_dev) : k.n; }
 
@@ -101,8 +109,24 @@ __device__ __forceinline__ float4 polar_rotation(float4 F)
     return make_float4(c * in, -s * in, s * in, c * in);
 }
 
+// 2x2 SVD through the polar decomposition: F = U diag(s) V^T with U, V rotations
+__device__ __forceinline__ void svd2(float4 F, float4& U, float2& s, float4& V)
+{
+    const float4 R = polar_rotation(F);
+    const float a  = R.x * F.x + R.z * F.z;
+    const float b  = R.x * F.y + R.z * F.w;
+    const float d  = R.y * F.y + R.w * F.w;
+    float c = 1.f, sn = 0.f;
+    if (fabsf(b) > 1e-30f) { sincosf(0.5f * atan2f(2.f * b, a - d), &sn, &c); }
+    V   = make_float4(c, -sn, sn, c);
+    s.x = c * c * a + 2.f * c * sn * b + sn * sn * d;
+    s.y = sn * sn * a - 2.f * c * sn * b + c * c * d;
+    U   = make_float4(R.x * V.x + R.y * V.z, R.x * V.y + R.y * V.w, R.z * V.x + R.w * V.z, R.z * V.y + R.w * V.w);
+}
+
 // Affine momentum Q = m C + coeff * Kirchhoff stress. Fluid: P2GKernel MPM.cu:68-80; elastic: fixed
-// corotated tau = 2 mu (F - R) F^T + la (J - 1) J I (Stomakhin et al. 2012), snow hardening exp(xi(1-Jp)).
+// corotated tau = 2 mu (F - R) F^T + la (J - 1) J I (Stomakhin et al. 2012), snow hardening exp(xi(1-Jp));
+// Neo-Hookean; sand (Klar et al. 2016).
 __device__ __forceinline__ float4 affine(const MpmK& k, int m, float4 Cp, float4 F, float J)
 {
     if (m == MODE_FLUID) {
@@ -113,20 +137,42 @@ __device__ __forceinline__ float4 affine(const MpmK& k, int m, float4 Cp, float4
         return make_float4(k.mass * Cp.x + coeff * -pressure, k.mass * Cp.y + coeff * 0.f,
                            k.mass * Cp.z + coeff * 0.f, k.mass * Cp.w + coeff * -pressure);
     }
-    float mu = k.mu0, la = k.la0;
-    if (m == MODE_SNOW) {
-        const float hf = __expf(k.hardening * (1.f - J));
-        mu *= hf;
-        la *= hf;
+    float t0, t1, t2, t3; // Kirchhoff stress
+    if (m == MODE_NEOHOOKEAN) {
+        // tau = mu (F F^T - I) + la ln(J) I
+        const float lj = k.la0 * logf(fmaxf(F.x * F.w - F.y * F.z, 1e-6f));
+        t0             = k.mu0 * (F.x * F.x + F.y * F.y - 1.f) + lj;
+        t1             = k.mu0 * (F.x * F.z + F.y * F.w);
+        t2             = t1;
+        t3             = k.mu0 * (F.z * F.z + F.w * F.w - 1.f) + lj;
+    } else if (m == MODE_SAND) {
+        // St. Venant-Kirchhoff on the Hencky strain: tau = U (2 mu eps + la tr(eps) I) U^T, eps = ln(sigma)
+        float4 U, V;
+        float2 sg;
+        svd2(F, U, sg, V);
+        const float e0 = logf(fmaxf(sg.x, 1e-6f)), e1 = logf(fmaxf(sg.y, 1e-6f));
+        const float lt = k.la0 * (e0 + e1);
+        const float a0 = 2.f * k.mu0 * e0 + lt, a1 = 2.f * k.mu0 * e1 + lt;
+        t0             = U.x * U.x * a0 + U.y * U.y * a1;
+        t1             = U.x * U.z * a0 + U.y * U.w * a1;
+        t2             = t1;
+        t3             = U.z * U.z * a0 + U.w * U.w * a1;
+    } else {
+        float mu = k.mu0, la = k.la0;
+        if (m == MODE_SNOW) {
+            const float hf = __expf(k.hardening * (1.f - J));
+            mu *= hf;
+            la *= hf;
+        }
+        const float4 R  = polar_rotation(F);
+        const float Je  = F.x * F.w - F.y * F.z;
+        const float a0 = F.x - R.x, a1 = F.y - R.y, a2 = F.z - R.z, a3 = F.w - R.w;
+        const float vol = la * (Je - 1.f) * Je;
+        t0              = 2.f * mu * (a0 * F.x + a1 * F.y) + vol;
+        t1              = 2.f * mu * (a0 * F.z + a1 * F.w);
+        t2              = 2.f * mu * (a2 * F.x + a3 * F.y);
+        t3              = 2.f * mu * (a2 * F.z + a3 * F.w) + vol;
     }
-    const float4 R  = polar_rotation(F);
-    const float Je  = F.x * F.w - F.y * F.z;
-    const float a0 = F.x - R.x, a1 = F.y - R.y, a2 = F.z - R.z, a3 = F.w - R.w;
-    const float vol = la * (Je - 1.f) * Je;
-    const float t0  = 2.f * mu * (a0 * F.x + a1 * F.y) + vol;
-    const float t1  = 2.f * mu * (a0 * F.z + a1 * F.w);
-    const float t2  = 2.f * mu * (a2 * F.x + a3 * F.y);
-    const float t3  = 2.f * mu * (a2 * F.z + a3 * F.w) + vol;
     const float coeff = -k.dt * k.vol0 * 4.f * k.inv_dx * k.inv_dx;
     return make_float4(k.mass * Cp.x + coeff * t0, k.mass * Cp.y + coeff * t1, k.mass * Cp.z + coeff * t2,
                        k.mass * Cp.w + coeff * t3);
@@ -163,21 +209,6 @@ struct PState {
     float4 C, F;
     float J;
 };
-
-// 2x2 SVD through the polar decomposition: F = U diag(s) V^T with U, V rotations
-__device__ __forceinline__ void svd2(float4 F, float4& U, float2& s, float4& V)
-{
-    const float4 R = polar_rotation(F);
-    const float a  = R.x * F.x + R.z * F.z;
-    const float b  = R.x * F.y + R.z * F.w;
-    const float d  = R.y * F.y + R.w * F.w;
-    float c = 1.f, sn = 0.f;
-    if (fabsf(b) > 1e-30f) { sincosf(0.5f * atan2f(2.f * b, a - d), &sn, &c); }
-    V   = make_float4(c, -sn, sn, c);
-    s.x = c * c * a + 2.f * c * sn * b + sn * sn * d;
-    s.y = sn * sn * a - 2.f * c * sn * b + c * c * d;
-    U   = make_float4(R.x * V.x + R.y * V.z, R.x * V.y + R.y * V.w, R.z * V.x + R.w * V.z, R.z * V.y + R.w * V.w);
-}
 
 // G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301). RAW: the grid holds accumulated
 // momentum/mass and the node update is applied on the fly; otherwise it holds velocities.
@@ -245,7 +276,7 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
     ps.v = vel;
     // F <- (I + dt C) F; J <- J det(I + dt C), clamped (MPM.cu:258-265)
     const float4 A = make_float4(1 + ps.C.x * k.dt, ps.C.y * k.dt, ps.C.z * k.dt, 1 + ps.C.w * k.dt);
-    if (m != MODE_FLUID || track_f) {
+    if (keeps_f(m, track_f)) {
         const float4 F = ps.F;
         ps.F           = make_float4(A.x * F.x + A.y * F.z, A.x * F.y + A.y * F.w, A.z * F.x + A.w * F.z,
                                      A.z * F.y + A.w * F.w);
@@ -262,6 +293,40 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
         ps.J *= (sg.x * sg.y) / (c0 * c1);
         ps.F = make_float4(U.x * c0 * V.x + U.y * c1 * V.y, U.x * c0 * V.z + U.y * c1 * V.w,
                            U.z * c0 * V.x + U.w * c1 * V.y, U.z * c0 * V.z + U.w * c1 * V.w);
+    } else if (m == MODE_SAND) {
+        // Drucker-Prager return mapping of the Hencky strain (Klar et al. 2016, d = 2): expansion projects to
+        // the cone's tip (F = U V^T), a state outside the cone onto its surface; J holds 1 + q
+        float4 U, V;
+        float2 sg;
+        svd2(ps.F, U, sg, V);
+        const float e0 = logf(fmaxf(sg.x, 1e-6f)), e1 = logf(fmaxf(sg.y, 1e-6f));
+        const float tr = e0 + e1;
+        const float d0 = e0 - 0.5f * tr, d1 = e1 - 0.5f * tr;
+        const float dn = sqrtf(d0 * d0 + d1 * d1);
+        const float q  = ps.J - 1.f;
+        const float phi = k.sh0 + (k.sh1 * q - k.sh3) * expf(-k.sh2 * q);
+        const float sp  = sinf(phi * 0.017453292519943295f);
+        const float alpha = 1.632993161855452f * sp / (3.f - sp); // sqrt(2/3) * 2 sin(phi) / (3 - sin(phi))
+        float c0 = 1.f, c1 = 1.f, dq = 0.f;
+        bool proj = true;
+        if (tr >= 0.f) {
+            dq = sqrtf(e0 * e0 + e1 * e1);
+        } else {
+            const float dg = dn + k.sand_cf * tr * alpha;
+            if (dg <= 0.f) {
+                proj = false;
+            } else {
+                const float f = dg / dn;
+                c0            = expf(e0 - f * d0);
+                c1            = expf(e1 - f * d1);
+                dq            = dg;
+            }
+        }
+        if (proj) {
+            ps.J += dq;
+            ps.F = make_float4(U.x * c0 * V.x + U.y * c1 * V.y, U.x * c0 * V.z + U.y * c1 * V.w,
+                               U.z * c0 * V.x + U.w * c1 * V.y, U.z * c0 * V.z + U.w * c1 * V.w);
+        }
     }
 }
 
@@ -385,7 +450,7 @@ __global__ void __launch_bounds__(T_MPM)
     if (valid) {
         const int m     = mat_of(k, MODE, mat, i);
         const float4 Fp = (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : F[i];
-        const float Jp  = (m == MODE_COROT) ? 1.f : J[i];
+        const float Jp  = keeps_j(m) ? J[i] : 1.f;
         Q               = affine(k, m, C[i], Fp, Jp);
         vv              = v[i];
         s               = stencil(k, x[i], status);
@@ -424,14 +489,14 @@ __global__ void __launch_bounds__(T_MPM)
     const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
     PState ps;
     ps.x = x[i];
-    ps.F = (m != MODE_FLUID || track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
-    ps.J = (m != MODE_COROT) ? J[i] : 1.f;
+    ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+    ps.J = keeps_j(m) ? J[i] : 1.f;
     g2p_body<RAW>(k, m, track_f, grid, ps, status);
     x[i] = ps.x;
     v[i] = ps.v;
     C[i] = ps.C;
-    if (m != MODE_FLUID || track_f) { F[i] = ps.F; }
-    if (m != MODE_COROT) { J[i] = ps.J; }
+    if (keeps_f(m, track_f)) { F[i] = ps.F; }
+    if (keeps_j(m)) { J[i] = ps.J; }
 }
 
 // G2P of one step fused with P2G of the next; zeroes the grid used two steps later
@@ -455,12 +520,12 @@ __global__ void __launch_bounds__(T_MPM)
         const int m = mat_of(k, MODE, mat, i);
         PState ps;
         ps.x = x[i];
-        ps.F = (m != MODE_FLUID || track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
-        ps.J = (m != MODE_COROT) ? J[i] : 1.f;
+        ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+        ps.J = keeps_j(m) ? J[i] : 1.f;
         g2p_body<true>(k, m, track_f, grid_in, ps, status);
         x[i] = ps.x;
-        if (m != MODE_FLUID || track_f) { F[i] = ps.F; }
-        if (m != MODE_COROT) { J[i] = ps.J; }
+        if (keeps_f(m, track_f)) { F[i] = ps.F; }
+        if (keeps_j(m)) { J[i] = ps.J; }
         Q  = affine(k, m, ps.C, (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : ps.F, ps.J);
         vv = ps.v;
         s  = stencil(k, ps.x, status);
@@ -656,7 +721,7 @@ namespace {
 int32_t mpm_validate(const gpe_mpm_params* p)
 {
     if (!p || !(p->dx > 0.f) || p->nx < 3 || p->ny < 3 || !(p->dt > 0.f) || !(p->mass > 0.f) || p->bc_width < 0 ||
-        p->material < 0 || p->material > 2 || (int64_t)p->nx * p->ny > ((int64_t)1 << 30)) {
+        p->material < 0 || p->material > GPE_MPM_MAT_SAND || (int64_t)p->nx * p->ny > ((int64_t)1 << 30)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "invalid MPM parameters");
         return GPE_ERR_BAD_ARG;
     }
@@ -697,6 +762,12 @@ MpmK mpm_make_k(const gpe_mpm_params& p)
     k.theta_c   = p.theta_c;
     k.theta_s   = p.theta_s;
     k.hardening = p.hardening;
+    const bool dflt = p.sand_h[0] == 0.f && p.sand_h[1] == 0.f && p.sand_h[2] == 0.f && p.sand_h[3] == 0.f;
+    k.sh0       = dflt ? 35.f : p.sand_h[0]; // Klar et al. 2016
+    k.sh1       = dflt ? 9.f : p.sand_h[1];
+    k.sh2       = dflt ? 0.2f : p.sand_h[2];
+    k.sh3       = dflt ? 10.f : p.sand_h[3];
+    k.sand_cf   = (2.f * k.la0 + 2.f * k.mu0) / (2.f * k.mu0);
     k.apic_s    = 4.f * k.inv_dx * k.inv_dx;
     return k;
 }
@@ -747,6 +818,8 @@ int32_t launch_p2g(gpe_mpm* s, float4* grid, cudaStream_t st)
         case MODE_FLUID: return launch_p2g_t<MODE_FLUID>(s, grid, st);
         case MODE_COROT: return launch_p2g_t<MODE_COROT>(s, grid, st);
         case MODE_SNOW: return launch_p2g_t<MODE_SNOW>(s, grid, st);
+        case MODE_NEOHOOKEAN: return launch_p2g_t<MODE_NEOHOOKEAN>(s, grid, st);
+        case MODE_SAND: return launch_p2g_t<MODE_SAND>(s, grid, st);
         default: return launch_p2g_t<MODE_MIXED>(s, grid, st);
     }
 }
@@ -771,6 +844,8 @@ int32_t launch_g2p(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st
         case MODE_FLUID: return launch_g2p_t<MODE_FLUID, RAW>(s, grid, zero, st);
         case MODE_COROT: return launch_g2p_t<MODE_COROT, RAW>(s, grid, zero, st);
         case MODE_SNOW: return launch_g2p_t<MODE_SNOW, RAW>(s, grid, zero, st);
+        case MODE_NEOHOOKEAN: return launch_g2p_t<MODE_NEOHOOKEAN, RAW>(s, grid, zero, st);
+        case MODE_SAND: return launch_g2p_t<MODE_SAND, RAW>(s, grid, zero, st);
         default: return launch_g2p_t<MODE_MIXED, RAW>(s, grid, zero, st);
     }
 }
@@ -793,6 +868,8 @@ int32_t launch_fused(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero,
         case MODE_FLUID: return launch_fused_t<MODE_FLUID>(s, gin, gout, gzero, st);
         case MODE_COROT: return launch_fused_t<MODE_COROT>(s, gin, gout, gzero, st);
         case MODE_SNOW: return launch_fused_t<MODE_SNOW>(s, gin, gout, gzero, st);
+        case MODE_NEOHOOKEAN: return launch_fused_t<MODE_NEOHOOKEAN>(s, gin, gout, gzero, st);
+        case MODE_SAND: return launch_fused_t<MODE_SAND>(s, gin, gout, gzero, st);
         default: return launch_fused_t<MODE_MIXED>(s, gin, gout, gzero, st);
     }
 }
@@ -966,8 +1043,8 @@ int32_t gpe_mpm_set_state(gpe_mpm* s, const float* pos, const float* vel, const 
     }
     if (mem == GPE_MEM_HOST && material) {
         for (int64_t i = 0; i < n; ++i) {
-            if (material[i] < 0 || material[i] > 2) {
-                gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_state: material ids must be in [0, 2]");
+            if (material[i] < 0 || material[i] > GPE_MPM_MAT_SAND) {
+                gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_state: material ids must be in [0, 4]");
                 return GPE_ERR_BAD_ARG;
             }
         }

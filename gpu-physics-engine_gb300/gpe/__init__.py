@@ -28,7 +28,7 @@ PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS, PBF_DYNAMIC_COUNT = 0
 WARM_NONE, WARM_PREV, WARM_MLP = 0, 1, 2
 MLP_FEATURES, MLP_HIDDEN, MLP_NUM_WEIGHTS, MLP_BLOB_FLOATS = 12, 64, 5057, 5083
 
-MPM_MAT_FLUID, MPM_MAT_COROTATED, MPM_MAT_SNOW = 0, 1, 2
+MPM_MAT_FLUID, MPM_MAT_COROTATED, MPM_MAT_SNOW, MPM_MAT_NEOHOOKEAN, MPM_MAT_SAND = 0, 1, 2, 3, 4
 MPM_BC_SLIP, MPM_BC_STICKY = 0, 1
 MPM_FLAG_PER_PARTICLE_MATERIAL, MPM_FLAG_FLUID_F, MPM_FLAG_DYNAMIC_COUNT = 0x1, 0x2, 0x4
 MPM_STAGE_CLEAR, MPM_STAGE_P2G, MPM_STAGE_GRID, MPM_STAGE_G2P, MPM_STAGE_SORT = range(5)
@@ -60,7 +60,7 @@ class MpmParams(C.Structure):
                 ("gamma", C.c_float), ("p_min", C.c_float), ("p_max", C.c_float), ("J_min", C.c_float),
                 ("J_max", C.c_float), ("E", C.c_float), ("nu", C.c_float), ("theta_c", C.c_float),
                 ("theta_s", C.c_float), ("hardening", C.c_float), ("sort_interval", C.c_int32),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("sand_h", C.c_float * 4)]
 
     def copy(self) -> "MpmParams":
         o = MpmParams()

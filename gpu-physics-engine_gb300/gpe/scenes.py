@@ -303,14 +303,17 @@ def mixed_params(n: int, grid: int = 1024) -> MpmParams:
     return p
 
 
-def mixed_discs(n: int = 4194304, seed: int = 4, discs_per_material: int = 3, area: float = 0.3):
-    """n particles, a third each of water, snow and jelly, in seeded random discs of equal radius."""
+def mixed_discs(n: int = 4194304, seed: int = 4, discs_per_material: int = 3, area: float = 0.3,
+                materials=(MPM_MAT_FLUID, MPM_MAT_SNOW, MPM_MAT_COROTATED)):
+    """n particles, an equal share of each material (default: water, snow and jelly), in seeded random discs
+    of equal radius."""
     g = rng(seed)
-    nd = 3 * discs_per_material
+    k_m = len(materials)
+    nd = k_m * discs_per_material
     r = math.sqrt(area / (nd * math.pi))
-    per_mat = [n // 3, n // 3, n - 2 * (n // 3)]
+    per_mat = [n // k_m] * (k_m - 1) + [n - (k_m - 1) * (n // k_m)]
     pos_l, mat_l = [], []
-    for m, cnt in zip((MPM_MAT_FLUID, MPM_MAT_SNOW, MPM_MAT_COROTATED), per_mat):
+    for m, cnt in zip(materials, per_mat):
         cs = g.uniform(0.15 + r, 0.85 - r, (discs_per_material, 2))
         split = [cnt // discs_per_material] * discs_per_material
         split[-1] += cnt - sum(split)

@@ -366,6 +366,12 @@ int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, const gpe_dom
 #define GPE_MPM_MAT_FLUID 0      /* J-based equation of state (reference P2GKernel, MPM.cu:68-80)          */
 #define GPE_MPM_MAT_COROTATED 1  /* fixed-corotated elasticity (Stomakhin et al. 2012)                     */
 #define GPE_MPM_MAT_SNOW 2       /* fixed-corotated with plasticity clamp and hardening (Stomakhin 2013)  */
+#define GPE_MPM_MAT_NEOHOOKEAN 3 /* compressible Neo-Hookean: tau = mu (F F^T - I) + la ln(J) I (J = det F,
+                                    floored at 1e-6)                                                        */
+#define GPE_MPM_MAT_SAND 4       /* Drucker-Prager elastoplastic sand (Klar et al. 2016): St. Venant-Kirchhoff
+                                    stress on the Hencky strain, return mapping of the log singular values
+                                    onto the friction cone, friction-angle hardening; the particle's J holds
+                                    1 + q, q the accumulated plastic strain (J = 1: q = 0)                   */
 
 #define GPE_MPM_BC_SLIP 0        /* zero the velocity component into the wall (MPM.cu:159-168)             */
 #define GPE_MPM_BC_STICKY 1      /* zero the whole node velocity inside the wall band                      */
@@ -398,6 +404,8 @@ typedef struct gpe_mpm_params {
     float theta_c, theta_s, hardening; /* snow plasticity (Stomakhin 2013)                       */
     int32_t sort_interval; /* re-sort particles by cell every this many steps; 0 = never          */
     uint32_t flags;    /* GPE_MPM_FLAG_*                                                         */
+    float sand_h[4];   /* sand friction angle in degrees, phi = h0 + (h1 q - h3) exp(-h2 q) (Klar et al.
+                          2016); all zero selects their (35, 9, 0.2, 10)                          */
 } gpe_mpm_params;
 
 typedef struct gpe_mpm gpe_mpm;

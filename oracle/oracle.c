@@ -19,7 +19,10 @@
  *   G2P, F and J update, handleOOB      MPM.cu:196-301 (gridToParticle, handleOOB); matMul2D/det2D
  *                                       cuda-internal.cuh:44-56
  * The fixed-corotated and snow models (absent in the reference) follow Stomakhin et al. 2012/2013 and the
- * MLS-MPM formulation of Hu et al. 2018.
+ * MLS-MPM formulation of Hu et al. 2018; the Neo-Hookean model is the compressible form of Bonet & Wood
+ * (tau = mu (F F^T - I) + la ln J I); sand follows the Drucker-Prager elastoplasticity of Klar et al. 2016
+ * (Hencky-strain St. Venant-Kirchhoff stress, return mapping onto the friction cone, friction-angle
+ * hardening with the accumulated plastic strain q, kept as J = 1 + q).
  */
 #include "oracle.h"
 
@@ -1151,10 +1154,36 @@ static void mpm_affine(const gpe_mpm_params* p, int mat, const float* C, const f
         tau[3] = -pr;
         const double Vp = (double)p->vol0 * J;
         coeff           = -(double)p->dt * Vp * 4.0 * inv_dx * inv_dx;
+    } else if (mat == GPE_MPM_MAT_NEOHOOKEAN) {
+        const double Fd[4] = {F[0], F[1], F[2], F[3]};
+        const double mu    = (double)p->E / (2.0 * (1.0 + p->nu));
+        const double la    = (double)p->E * p->nu / ((1.0 + p->nu) * (1.0 - 2.0 * p->nu));
+        double Je          = Fd[0] * Fd[3] - Fd[1] * Fd[2];
+        if (Je < 1e-6) { Je = 1e-6; }
+        const double lj = la * log(Je);
+        tau[0] = mu * (Fd[0] * Fd[0] + Fd[1] * Fd[1] - 1.0) + lj;
+        tau[1] = mu * (Fd[0] * Fd[2] + Fd[1] * Fd[3]);
+        tau[2] = tau[1];
+        tau[3] = mu * (Fd[2] * Fd[2] + Fd[3] * Fd[3] - 1.0) + lj;
+        coeff  = -(double)p->dt * p->vol0 * 4.0 * inv_dx * inv_dx;
+    } else if (mat == GPE_MPM_MAT_SAND) {
+        const double Fd[4] = {F[0], F[1], F[2], F[3]};
+        const double mu    = (double)p->E / (2.0 * (1.0 + p->nu));
+        const double la    = (double)p->E * p->nu / ((1.0 + p->nu) * (1.0 - 2.0 * p->nu));
+        double U[4], sg[2], V[4];
+        svd2(Fd, U, sg, V);
+        const double e0 = log(sg[0] > 1e-6 ? sg[0] : 1e-6), e1 = log(sg[1] > 1e-6 ? sg[1] : 1e-6);
+        const double a0 = 2.0 * mu * e0 + la * (e0 + e1), a1 = 2.0 * mu * e1 + la * (e0 + e1);
+        /* tau = U diag(a) U^T */
+        tau[0] = U[0] * U[0] * a0 + U[1] * U[1] * a1;
+        tau[1] = U[0] * U[2] * a0 + U[1] * U[3] * a1;
+        tau[2] = tau[1];
+        tau[3] = U[2] * U[2] * a0 + U[3] * U[3] * a1;
+        coeff  = -(double)p->dt * p->vol0 * 4.0 * inv_dx * inv_dx;
     } else {
         const double Fd[4] = {F[0], F[1], F[2], F[3]};
-        double mu = p->E / (2.0 * (1.0 + p->nu));
-        double la = p->E * p->nu / ((1.0 + p->nu) * (1.0 - 2.0 * p->nu));
+        double mu = (double)p->E / (2.0 * (1.0 + p->nu));
+        double la = (double)p->E * p->nu / ((1.0 + p->nu) * (1.0 - 2.0 * p->nu));
         if (mat == GPE_MPM_MAT_SNOW) {
             const double hf = exp((double)p->hardening * (1.0 - J)); /* J holds the plastic J_p */
             mu *= hf;
@@ -1240,6 +1269,44 @@ void orc_mpm_grid_update(const gpe_mpm_params* p, double* grid)
     }
 }
 
+/* Drucker-Prager return mapping of the Hencky strain (Klar et al. 2016, d = 2). F is projected in place
+ * and *J (= 1 + q) grows by the plastic strain increment; returns whether F changed. */
+static int sand_project(const gpe_mpm_params* p, double F[4], double* J, double sc[2])
+{
+    const int dflt = p->sand_h[0] == 0.f && p->sand_h[1] == 0.f && p->sand_h[2] == 0.f && p->sand_h[3] == 0.f;
+    const double h0 = dflt ? 35.0 : p->sand_h[0], h1 = dflt ? 9.0 : p->sand_h[1];
+    const double h2 = dflt ? 0.2 : p->sand_h[2], h3 = dflt ? 10.0 : p->sand_h[3];
+    const double mu = (double)p->E / (2.0 * (1.0 + p->nu));
+    const double la = (double)p->E * p->nu / ((1.0 + p->nu) * (1.0 - 2.0 * p->nu));
+    double U[4], sg[2], V[4];
+    svd2(F, U, sg, V);
+    const double e0 = log(sg[0] > 1e-6 ? sg[0] : 1e-6), e1 = log(sg[1] > 1e-6 ? sg[1] : 1e-6);
+    const double tr = e0 + e1;
+    const double d0 = e0 - 0.5 * tr, d1 = e1 - 0.5 * tr;
+    const double dn = sqrt(d0 * d0 + d1 * d1);
+    const double q = *J - 1.0;
+    const double phi = h0 + (h1 * q - h3) * exp(-h2 * q); /* degrees */
+    const double sp = sin(phi * M_PI / 180.0);
+    const double alpha = sqrt(2.0 / 3.0) * 2.0 * sp / (3.0 - sp);
+    double dq;
+    if (tr >= 0.0) { /* expansion: the cone's tip */
+        sc[0] = sc[1] = 1.0;
+        dq = sqrt(e0 * e0 + e1 * e1);
+    } else {
+        const double dg = dn + (2.0 * la + 2.0 * mu) / (2.0 * mu) * tr * alpha;
+        if (dg <= 0.0) { return 0; } /* inside the cone: elastic */
+        sc[0] = exp(e0 - dg / dn * d0);
+        sc[1] = exp(e1 - dg / dn * d1);
+        dq    = dg;
+    }
+    *J += dq;
+    F[0] = U[0] * sc[0] * V[0] + U[1] * sc[1] * V[1];
+    F[1] = U[0] * sc[0] * V[2] + U[1] * sc[1] * V[3];
+    F[2] = U[2] * sc[0] * V[0] + U[3] * sc[1] * V[1];
+    F[3] = U[2] * sc[0] * V[2] + U[3] * sc[1] * V[3];
+    return 1;
+}
+
 void orc_mpm_g2p(const gpe_mpm_params* p, int64_t n, const double* grid, float* x, float* v, float* C,
                  float* F, float* J, const int32_t* mat)
 {
@@ -1307,6 +1374,9 @@ void orc_mpm_g2p(const gpe_mpm_params* p, int64_t n, const double* grid, float* 
             Fn[1] = U[0] * sc[0] * V[2] + U[1] * sc[1] * V[3];
             Fn[2] = U[2] * sc[0] * V[0] + U[3] * sc[1] * V[1];
             Fn[3] = U[2] * sc[0] * V[2] + U[3] * sc[1] * V[3];
+        } else if (mt == GPE_MPM_MAT_SAND) {
+            double sc[2];
+            (void)sand_project(p, Fn, &Jn, sc); /* Fn recomposed from the projected singular values sc */
         }
         x[2 * i]     = (float)px;
         x[2 * i + 1] = (float)py;

@@ -36,14 +36,21 @@ def _scene(kind):
     elif kind == "fluid":
         p.material = gpe.MPM_MAT_FLUID
         p.k_bulk, p.gamma = 10.0, 1.0
+    elif kind == "neohookean":
+        p.material = gpe.MPM_MAT_NEOHOOKEAN
+    elif kind == "sand":
+        p.material = gpe.MPM_MAT_SAND
+        p.nu = 0.3
+        J = (1.0 + g.uniform(0.0, 0.5, n)).astype(np.float32)  # J = 1 + q, q the plastic strain so far
     elif kind == "mixed":
+        # every material of the library, in fifths of the particle array
         p.flags = gpe.MPM_FLAG_PER_PARTICLE_MATERIAL
         p.k_bulk, p.gamma = 10.0, 1.0
-        mat = (np.arange(n) * 3 // n).astype(np.int32)
+        mat = (np.arange(n) * 5 // n).astype(np.int32)
     return p, x, v, Cm, F, J, mat
 
 
-KINDS = ["reference", "corotated", "snow", "fluid", "mixed"]
+KINDS = ["reference", "corotated", "snow", "fluid", "neohookean", "sand", "mixed"]
 
 
 def _engine(gpe_mod, p, x, v, Cm, F, J, mat, sort_interval=0):
@@ -114,8 +121,13 @@ def test_fused_steps(gpe_mod, oracle, cuda_ok, kind, steps):
     _close(x1, wx, np.abs(wx), "x", rel=rel, floor=8 * EPS32 * np.abs(wx).max())
     _close(v1, wv, np.abs(wv).max(), "v", rel=10 * rel)
     _close(C1, wC, np.abs(wC).max(), "C", rel=10 * rel)
-    if kind in ("corotated", "snow") or kind == "reference":
+    if kind in ("corotated", "snow", "neohookean", "sand") or kind == "reference":
         _close(F1, wF, np.abs(wF).max(), "F", rel=10 * rel)
+    if kind == "mixed":  # the engine keeps no F for fluid particles
+        sel = mat != gpe_mod.MPM_MAT_FLUID
+        _close(F1[sel], wF[sel], np.abs(wF[sel]).max(), "F", rel=10 * rel)
+    if kind in ("snow", "sand"):
+        _close(J1, wJ, np.abs(wJ).max(), "J", rel=10 * rel)
     assert e.status() == 0
 
 
