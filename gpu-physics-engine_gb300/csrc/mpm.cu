@@ -330,18 +330,7 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
     }
 }
 
-// per-particle contribution for one stencil node (particleToGrid MPM.cu:116-126)
-__device__ __forceinline__ float4 node_contrib(const MpmK& k, const Stencil& s, float2 v, float4 Q, int i, int j)
-{
-    const float w   = s.wx[i] * s.wy[j];
-    const float dpx = ((float)i - s.fx) * k.dx;
-    const float dpy = ((float)j - s.fy) * k.dx;
-    const float ax  = dpx * Q.x + dpy * Q.y;
-    const float ay  = dpx * Q.z + dpy * Q.w;
-    return make_float4(w * (v.x * k.mass + ax), w * (v.y * k.mass + ay), w * k.mass, 0.f);
-}
-
-// Scatter of one block's particles through a shared-memory tile. All threads of the block must call it;
+// Scatter of one block's particles through a shared-memory tile (particleToGrid, MPM.cu:116-126). All threads of the block must call it;
 // `valid` marks threads that carry a particle.
 __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stencil& s, float2 v, float4 Q,
                                           float4* __restrict__ grid)
@@ -383,44 +372,59 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
             s_m[t] = 0.f;
         }
         __syncthreads();
-        if (valid) {
-            // Particles of one cell (a dozen or more, consecutive after the spatial sort) share their 9 nodes;
-            // visiting the nodes in the same order would make their shared-memory atomics collide on one
-            // address at a time. Each lane starts at node (lane mod 9), so concurrent lanes of a cell mostly
-            // hit different nodes.
-            const int rot = (int)(threadIdx.x % 9u);
+    }
+    // Particles are kept spatially sorted, so consecutive lanes mostly share their stencil's base node and
+    // with it all 9 target nodes. For each node the lanes of such a run sum their contributions with a
+    // segmented shuffle reduction, and only the run's first lane updates the tile (or the grid): float
+    // atomics on one shared address serialise, and the lanes of a run would otherwise all hit the same 9.
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t key  = valid ? (uint32_t)s.by * (uint32_t)k.nx + (uint32_t)s.bx : 0xffffffffu;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head     = lane == 0u || prev != key;
+    const uint32_t heads = __ballot_sync(0xffffffffu, head);
+    const uint32_t later = lane == 31u ? 0u : (heads & (0xffffffffu << (lane + 1u)));
+    const uint32_t run_end = later ? (uint32_t)(__ffs(later) - 1) : 32u; // first lane of the next run
 #pragma unroll
-            for (int q = 0; q < 9; ++q) {
-                const int nd   = (q + rot) >= 9 ? q + rot - 9 : q + rot;
-                const int i    = nd % 3, j = nd / 3;
-                const float wx = i == 0 ? s.wx[0] : (i == 1 ? s.wx[1] : s.wx[2]);
-                const float wy = j == 0 ? s.wy[0] : (j == 1 ? s.wy[1] : s.wy[2]);
-                const float w   = wx * wy;
-                const float dpx = ((float)i - s.fx) * k.dx;
-                const float dpy = ((float)j - s.fy) * k.dx;
-                const float ax  = dpx * Q.x + dpy * Q.y;
-                const float ay  = dpx * Q.z + dpy * Q.w;
-                const int t     = (s.by + j - ty0) * tw + (s.bx + i - tx0);
-                atomicAdd(&s_x[t], w * (v.x * k.mass + ax));
-                atomicAdd(&s_y[t], w * (v.y * k.mass + ay));
-                atomicAdd(&s_m[t], w * k.mass);
+    for (int q = 0; q < 9; ++q) {
+        const int i = q % 3, j = q / 3;
+        float cx = 0.f, cy = 0.f, cm = 0.f;
+        if (valid) {
+            const float w   = s.wx[i] * s.wy[j];
+            const float dpx = ((float)i - s.fx) * k.dx;
+            const float dpy = ((float)j - s.fy) * k.dx;
+            cx              = w * (v.x * k.mass + (dpx * Q.x + dpy * Q.y));
+            cy              = w * (v.y * k.mass + (dpx * Q.z + dpy * Q.w));
+            cm              = w * k.mass;
+        }
+#pragma unroll
+        for (uint32_t d = 1u; d < 32u; d <<= 1) {
+            const float ox = __shfl_down_sync(0xffffffffu, cx, d);
+            const float oy = __shfl_down_sync(0xffffffffu, cy, d);
+            const float om = __shfl_down_sync(0xffffffffu, cm, d);
+            if (lane + d < run_end) {
+                cx += ox;
+                cy += oy;
+                cm += om;
             }
         }
+        if (head && valid) {
+            if (tiled) {
+                const int t = (s.by + j - ty0) * tw + (s.bx + i - tx0);
+                atomicAdd(&s_x[t], cx);
+                atomicAdd(&s_y[t], cy);
+                atomicAdd(&s_m[t], cm);
+            } else {
+                atomicAdd(&grid[(size_t)(s.by + j) * (size_t)k.nx + (size_t)(s.bx + i)], make_float4(cx, cy, cm, 0.f));
+            }
+        }
+    }
+    if (tiled) {
         __syncthreads();
         for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
             const float m = s_m[t];
             if (m != 0.f) {
                 const int32_t gx = tx0 + t % tw, gy = ty0 + t / tw;
                 atomicAdd(&grid[(size_t)gy * (size_t)k.nx + (size_t)gx], make_float4(s_x[t], s_y[t], m, 0.f));
-            }
-        }
-    } else if (valid) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const float4 c = node_contrib(k, s, v, Q, i, j);
-                atomicAdd(&grid[(size_t)(s.by + j) * (size_t)k.nx + (size_t)(s.bx + i)], c);
             }
         }
     }
@@ -1071,7 +1075,8 @@ int32_t gpe_mpm_set_state(gpe_mpm* s, const float* pos, const float* vel, const 
     s->k.n              = (int32_t)n;
     s->have_state       = true;
     s->grids_dirty      = true;
-    s->steps_since_sort = 0;
+    // a new state is in the caller's order: the next step sorts it by stencil base node first
+    s->steps_since_sort = s->prm.sort_interval;
     if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
     return GPE_OK;
 }
