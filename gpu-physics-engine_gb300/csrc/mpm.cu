@@ -893,7 +893,7 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
                                                    s->v[o], s->C[o], s->F[o], s->J[o], s->mat[o], s->id[o]);
     GPE_CHECK_LAUNCH("k_mpm_gather");
     s->cur ^= 1;
-    s->launches += 6;
+    s->launches += 3 + scan_launches((uint32_t)s->nn); // key, scan, scatter, gather
     return GPE_OK;
 }
 

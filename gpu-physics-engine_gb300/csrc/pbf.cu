@@ -269,12 +269,18 @@ __device__ __forceinline__ void pair_direction(uint32_t a, uint32_t b, float& nx
 }
 
 // ----- predict + cell key + histogram rank (PBF.cu:786-797) ---------------------------------------------
+// x* = x + dt v + dt^2 g, each operation rounded once as in the oracle (the placement recomputes it)
+__device__ __forceinline__ float2 predict(const PbfK& k, float2 p, float2 w)
+{
+    return make_float2(__fadd_rn(__fmaf_rn(k.dt, w.x, p.x), k.g2x), __fadd_rn(__fmaf_rn(k.dt, w.y, p.y), k.g2y));
+}
+
 // Lanes of a warp that share a cell take consecutive ranks in lane order from one atomicAdd.
 template <bool MULTI>
 __global__ void __launch_bounds__(T_PART)
     k_predict_hist(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                   const float2* __restrict__ x, const float2* __restrict__ v, float2* __restrict__ xs_tmp,
-                   uint2* __restrict__ keyrank, uint32_t* __restrict__ count)
+                   const float2* __restrict__ x, const float2* __restrict__ v, uint2* __restrict__ keyrank,
+                   uint32_t* __restrict__ count)
 {
     const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid   = i < count_of(k);
@@ -283,10 +289,7 @@ __global__ void __launch_bounds__(T_PART)
     float2 ps          = make_float2(0.f, 0.f);
     if (valid) {
         const DomDev d = load_dom<MULTI>(k, doms, dom, i);
-        const float2 p = x[i];
-        const float2 w = v[i];
-        ps.x           = __fadd_rn(__fmaf_rn(k.dt, w.x, p.x), k.g2x);
-        ps.y           = __fadd_rn(__fmaf_rn(k.dt, w.y, p.y), k.g2y);
+        ps             = predict(k, x[i], v[i]);
         const int32_t cx = cell_coord(ps.x, d.ox, k.inv_cell, d.ncx);
         const int32_t cy = cell_coord(ps.y, d.oy, k.inv_cell, d.ncy);
         key              = d.coff + (uint32_t)cy * (uint32_t)d.ncx + (uint32_t)cx;
@@ -298,7 +301,6 @@ __global__ void __launch_bounds__(T_PART)
     base = __shfl_sync(0xffffffffu, base, leader);
     if (valid) {
         const uint32_t rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        xs_tmp[i]           = ps;
         keyrank[i]          = make_uint2(key, rank);
     }
 }
@@ -307,25 +309,24 @@ __global__ void __launch_bounds__(T_PART)
 // The atomic ranks are unique but depend on warp scheduling; the stable slot of particle i is the number of
 // entries of its cell's bucket with a smaller pre-sort index.
 __global__ void __launch_bounds__(T_PART)
-    k_place(int32_t n_host, const int32_t* __restrict__ n_dev, const uint2* __restrict__ keyrank,
-            const uint32_t* __restrict__ start,
+    k_place(const PbfK k, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
             const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
-            const float2* __restrict__ xs_tmp, float2* __restrict__ x_out, float2* __restrict__ xs_out,
+            const float2* __restrict__ v_in, float2* __restrict__ x_out, float2* __restrict__ xs_out,
             uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
             uint32_t* __restrict__ id_out, const float* __restrict__ acc_in, float* __restrict__ prev_out,
             float* __restrict__ lam_out)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int32_t n = n_dev ? __ldg(n_dev) : n_host;
-    if (i >= n) { return; }
+    if (i >= count_of(k)) { return; }
     const uint2 kr   = keyrank[i];
     const uint32_t s = __ldg(&start[kr.x]);
     const uint32_t e = __ldg(&start[kr.x + 1]);
     uint32_t rank    = 0;
     for (uint32_t t = s; t < e; ++t) { rank += (__ldg(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
     const uint32_t dst = s + rank;
-    x_out[dst]         = x_in[i];
-    xs_out[dst]        = xs_tmp[i];
+    const float2 p     = x_in[i];
+    x_out[dst]         = p;
+    xs_out[dst]        = predict(k, p, v_in[i]);
     perm[dst]          = (uint32_t)i;
     key_out[dst]       = kr.x;
     if (id_in) { id_out[dst] = id_in[i]; }
@@ -1138,7 +1139,6 @@ struct gpe_pbf {
     DomDev* d_doms    = nullptr;
     float2* pos[4]    = {};
     float2* vel       = nullptr;
-    float2* xs_tmp    = nullptr;
     float* lam        = nullptr;
     float* omega      = nullptr;
     float* rho        = nullptr;
@@ -1351,10 +1351,10 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     if (n > 0) {
         if (multi(s)) {
             k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X], s->vel,
-                                                                   s->xs_tmp, s->keyrank, s->count);
+                                                                   s->keyrank, s->count);
         } else {
             k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X],
-                                                                    s->vel, s->xs_tmp, s->keyrank, s->count);
+                                                                    s->vel, s->keyrank, s->count);
         }
         GPE_CHECK_LAUNCH("k_predict_hist");
     }
@@ -1364,8 +1364,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     if (rc) { return rc; }
     if (n > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
-        k_place<<<blocks_for(n), T_PART, 0, st>>>(n, s->d_count, s->keyrank, s->start, s->bucket, s->pos[s->X],
-                                                  s->xs_tmp,
+        k_place<<<blocks_for(n), T_PART, 0, st>>>(s->k, s->keyrank, s->start, s->bucket, s->pos[s->X], s->vel,
                                                   s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
                                                   ids ? s->ids[s->id_cur] : nullptr,
                                                   ids ? s->ids[s->id_cur ^ 1] : nullptr,
@@ -1375,7 +1374,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
         if (ids) { s->id_cur ^= 1; }
     }
     s->have_sort = true;
-    s->launches += 6;
+    s->launches += 3 + scan_launches(s->ncells); // predict + histogram, scan, scatter, place
     return GPE_OK;
 }
 
@@ -1692,7 +1691,6 @@ int32_t alloc_buffers(gpe_pbf* s)
     size_t o_pos[4];
     for (int b = 0; b < 4; ++b) { o_pos[b] = c.take<float2>(N); }
     const size_t o_vel   = c.take<float2>(N);
-    const size_t o_xst   = c.take<float2>(N);
     const size_t o_lam   = c.take<float>(N);
     const size_t o_om    = c.take<float>(N);
     const size_t o_rho   = c.take<float>(N);
@@ -1720,7 +1718,6 @@ int32_t alloc_buffers(gpe_pbf* s)
     s->d_doms  = reinterpret_cast<DomDev*>(b + o_doms);
     for (int q = 0; q < 4; ++q) { s->pos[q] = reinterpret_cast<float2*>(b + o_pos[q]); }
     s->vel     = reinterpret_cast<float2*>(b + o_vel);
-    s->xs_tmp  = reinterpret_cast<float2*>(b + o_xst);
     s->lam     = reinterpret_cast<float*>(b + o_lam);
     s->omega   = reinterpret_cast<float*>(b + o_om);
     s->rho     = reinterpret_cast<float*>(b + o_rho);
@@ -2561,8 +2558,7 @@ namespace {
 constexpr size_t NA_MAX_N     = (size_t)GPE_NOALLOC_MAX_PARTICLES;
 constexpr size_t NA_MAX_CELLS = (size_t)GPE_NOALLOC_MAX_CELLS;
 constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
-constexpr size_t NA_OFF_XS    = 0;                                                  // float2[n]
-constexpr size_t NA_OFF_KR    = na_align(NA_OFF_XS + sizeof(float2) * NA_MAX_N);    // uint2[n]
+constexpr size_t NA_OFF_KR    = 0;                                                  // uint2[n]
 constexpr size_t NA_OFF_BK    = na_align(NA_OFF_KR + sizeof(uint2) * NA_MAX_N);     // uint32[n]
 constexpr size_t NA_OFF_CNT   = na_align(NA_OFF_BK + sizeof(uint32_t) * NA_MAX_N);  // uint32[cells]
 constexpr size_t NA_OFF_BS    = na_align(NA_OFF_CNT + sizeof(uint32_t) * NA_MAX_CELLS);
@@ -2637,7 +2633,6 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     uint8_t* scratch = nullptr;
     rc               = noalloc_scratch(&scratch);
     if (rc) { return rc; }
-    float2* xs_tmp   = reinterpret_cast<float2*>(scratch + NA_OFF_XS);
     uint2* keyrank   = reinterpret_cast<uint2*>(scratch + NA_OFF_KR);
     uint32_t* bucket = reinterpret_cast<uint32_t*>(scratch + NA_OFF_BK);
     uint32_t* count  = reinterpret_cast<uint32_t*>(scratch + NA_OFF_CNT);
@@ -2665,8 +2660,8 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     if (n > 0) {
         k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(k, nullptr, nullptr,
                                                                 reinterpret_cast<const float2*>(pos),
-                                                                reinterpret_cast<const float2*>(vel), xs_tmp,
-                                                                keyrank, count);
+                                                                reinterpret_cast<const float2*>(vel), keyrank,
+                                                                count);
         GPE_CHECK_LAUNCH("k_predict_hist (noalloc)");
     }
     rc = launch_exclusive_scan(count, (uint32_t)cells, bsum, cell_start, st);
@@ -2674,8 +2669,9 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     if (n > 0) {
         rc = launch_scatter(keyrank, n, cell_start, bucket, st);
         if (rc) { return rc; }
-        k_place<<<blocks_for(n), T_PART, 0, st>>>((int32_t)n, nullptr, keyrank, cell_start, bucket,
-                                                  reinterpret_cast<const float2*>(pos), xs_tmp,
+        k_place<<<blocks_for(n), T_PART, 0, st>>>(k, keyrank, cell_start, bucket,
+                                                  reinterpret_cast<const float2*>(pos),
+                                                  reinterpret_cast<const float2*>(vel),
                                                   reinterpret_cast<float2*>(pos_sorted),
                                                   reinterpret_cast<float2*>(pred_sorted), perm, key_sorted, nullptr,
                                                   nullptr, nullptr, nullptr, nullptr);

@@ -5,8 +5,9 @@
 // (PBF.cu:786-797), a 256-wide scan incPrefSum256 (PBF.cu:835-860) and a shared-memory scatter
 // (PBF.cu:806-833). Chunks here are not bounded by shared memory (a scene holds up to millions of
 // particles and cells), so the histogram and the scan run device-wide: the histogram is fused into the
-// predict kernel (pbf.cu), the scan below is the usual reduce / scan-of-block-sums / down-sweep over tiles of
-// 2048 cells, and the stable placement is finished by pbf.cu's gather kernel.
+// predict kernel (pbf.cu), the scan below is a reduce / down-sweep over tiles of 2048 cells (with a
+// scan-of-block-sums launch in between for more than 2048 tiles), and the stable placement is finished by
+// pbf.cu's gather kernel.
 #include "gpe_internal.h"
 
 namespace gpe {
@@ -77,12 +78,26 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_bsum(uint32_t* __restrict__ bsu
     }
 }
 
+// SUMS: bsum holds the tiles' totals (not scanned) and each block adds up those before it itself, which
+// saves the single-block scan launch while the tiles are few (FUSED_MAX_TILES); else bsum is already the
+// exclusive scan of the totals.
+constexpr uint32_t FUSED_MAX_TILES = 2048;
+
+template <bool SUMS>
 __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ count, uint32_t M,
                                                       const uint32_t* __restrict__ bsum,
                                                       uint32_t* __restrict__ start)
 {
     __shared__ uint32_t s_tile[SCAN_TILE];
     const uint32_t base = blockIdx.x * SCAN_TILE;
+    uint32_t prefix;
+    if (SUMS) {
+        uint32_t part = 0;
+        for (uint32_t b = threadIdx.x; b < blockIdx.x; b += SCAN_T) { part += bsum[b]; }
+        block_excl_scan(part, &prefix);
+    } else {
+        prefix = bsum[blockIdx.x];
+    }
     // coalesced load, and zero the histogram for the next sort
 #pragma unroll
     for (int t = 0; t < SCAN_I; ++t) {
@@ -106,7 +121,7 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
     }
     uint32_t total;
     const uint32_t ex  = block_excl_scan(s, &total);
-    const uint32_t off = bsum[blockIdx.x] + ex;
+    const uint32_t off = prefix + ex;
 #pragma unroll
     for (int t = 0; t < SCAN_I; ++t) { s_tile[threadIdx.x * SCAN_I + t] = off + loc[t]; }
     __syncthreads();
@@ -116,7 +131,7 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
         const uint32_t idx = base + li;
         if (idx < M) { start[idx] = s_tile[li]; }
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = bsum[blockIdx.x] + total; }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = prefix + total; }
 }
 
 __global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n_host, const int32_t* __restrict__ n_dev,
@@ -140,12 +155,19 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
     if (nb == 0) { return GPE_ERR_BAD_ARG; }
     k_scan_reduce<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
     GPE_CHECK_LAUNCH("k_scan_reduce");
-    k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
-    GPE_CHECK_LAUNCH("k_scan_bsum");
-    k_scan_down<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
-    GPE_CHECK_LAUNCH("k_scan_down");
+    if (nb <= FUSED_MAX_TILES) {
+        k_scan_down<true><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
+        GPE_CHECK_LAUNCH("k_scan_down");
+    } else {
+        k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
+        GPE_CHECK_LAUNCH("k_scan_bsum");
+        k_scan_down<false><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
+        GPE_CHECK_LAUNCH("k_scan_down");
+    }
     return GPE_OK;
 }
+
+int32_t scan_launches(uint32_t n_keys) { return scan_blocks(n_keys) <= FUSED_MAX_TILES ? 2 : 3; }
 
 int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, cudaStream_t st,
                        const int32_t* n_dev)

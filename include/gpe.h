@@ -343,7 +343,7 @@ int32_t gpe_pbf_autotune(gpe_pbf* pbf, int32_t trial_steps, gpe_pbf_tuning* best
  * are all allocated up front, cuda-engine.cpp:102-139); it exists for callers that cannot call cudaMalloc,
  * such as a host whose device memory is owned by another framework, or a real-time loop that must not
  * allocate once it is running. It runs the same kernels as GPE_PBF_STAGE_PREDICT_SORT on caller buffers
- * and keeps its scratch in a fixed static device array (9.0 MiB, sized for the limits below, held by every
+ * and keeps its scratch in a fixed static device array (7.0 MiB, sized for the limits below, held by every
  * GPU that loads the library until the process exits), so it never allocates.
  *   in : pos, vel  n float2 (device pointers), one scene `domain`, `params`
  *   out: pos_sorted, pred_sorted n float2; key_sorted, perm n uint32; cell_start n_cells + 1 uint32
