@@ -2,16 +2,17 @@
 //
 // The reference runs, per substep, resetGrid -> P2GKernel -> gridKernel -> G2PKernel (MPM.cu:353-371) with
 // 27 scalar global atomics per particle (MPM.cu:124-126) and a separate streaming pass over the grid.
-// Here one step is one launch after the first:
-//   k_p2g            P2G of the first step: each block accumulates its particles' 3x3 stencils in a
-//                    shared-memory node tile with shared atomics and flushes every touched node with one
-//                    vector global atomic (red.v4.f32) — particles are kept spatially sorted so a block's
-//                    stencils cover a small tile.
-//   k_g2p_p2g        G2P of step s fused with P2G of step s+1: the grid update (v = p/m + g dt, walls,
-//                    MPM.cu:150-175) is applied on the fly to each node the gather reads, the particle is
-//                    advanced and immediately scattered into the next grid, and the grid after that is
-//                    zeroed in the same launch (three grids rotate), so v and C never leave registers.
-//   k_g2p            G2P of the last step, writing the full particle state.
+// Here one step is two launches and the grid update needs no pass of its own:
+//   k_p2g            P2G: each block accumulates its particles' 3x3 stencils in a shared-memory node tile
+//                    (lanes that share a stencil base node first sum their contributions with a segmented
+//                    shuffle reduction, so one lane per run touches the tile) and flushes every touched node
+//                    with one vector global atomic (red.v4.f32); particles are kept sorted by base node, so a
+//                    block's stencils cover a small tile.
+//   k_g2p            G2P on the raw momentum grid: the grid update (v = p/m + g dt, walls, MPM.cu:150-175) is
+//                    applied on the fly to each node the gather reads, and the grid read two steps earlier is
+//                    zeroed in the same launch (three grids rotate).
+// (A G2P fused with the next step's P2G in one kernel measured slower: 0.300 against 0.279 ms per step at 4M
+// particles, its 62 registers and shared tile halving the occupancy of either pass.)
 // Stage kernels (k_clear, k_p2g, k_grid, k_g2p on an updated grid) reproduce the reference's four kernels
 // one to one for stage-level parity tests.
 #include <cuda_runtime.h>
@@ -503,40 +504,6 @@ __global__ void __launch_bounds__(T_MPM)
     if (keeps_j(m)) { J[i] = ps.J; }
 }
 
-// G2P of one step fused with P2G of the next; zeroes the grid used two steps later
-template <int MODE>
-__global__ void __launch_bounds__(T_MPM)
-    k_g2p_p2g(const MpmK k, const float4* __restrict__ grid_in, float4* __restrict__ grid_out,
-              float4* __restrict__ grid_zero, int64_t nn, float2* __restrict__ x, float4* __restrict__ F,
-              float* __restrict__ J, const int32_t* __restrict__ mat, uint32_t* status)
-{
-    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
-    {
-        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-        for (int64_t z = i; z < nn; z += stride) { grid_zero[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
-    }
-    const bool valid   = i < count_of(k);
-    const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
-    Stencil s{};
-    float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 vv = make_float2(0.f, 0.f);
-    if (valid) {
-        const int m = mat_of(k, MODE, mat, i);
-        PState ps;
-        ps.x = x[i];
-        ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
-        ps.J = keeps_j(m) ? J[i] : 1.f;
-        g2p_body<true>(k, m, track_f, grid_in, ps, status);
-        x[i] = ps.x;
-        if (keeps_f(m, track_f)) { F[i] = ps.F; }
-        if (keeps_j(m)) { J[i] = ps.J; }
-        Q  = affine(k, m, ps.C, (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : ps.F, ps.J);
-        vv = ps.v;
-        s  = stencil(k, ps.x, status);
-    }
-    p2g_block(k, valid, s, vv, Q, grid_out);
-}
-
 // ----- spatial sort of the particles (keeps P2G tiles small) ---------------------------------------------
 __global__ void __launch_bounds__(T_MPM)
     k_mpm_key(const MpmK k, const float2* __restrict__ x, uint2* __restrict__ keyrank, uint32_t* __restrict__ count,
@@ -854,30 +821,6 @@ int32_t launch_g2p(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st
     }
 }
 
-template <int MODE>
-int32_t launch_fused_t(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero, cudaStream_t st)
-{
-    const int c      = s->cur;
-    const unsigned g = std::max(mblocks(lsz(s)), grid_blocks(s->nn));
-    k_g2p_p2g<MODE><<<g, T_MPM, 0, st>>>(s->k, gin, gout, gzero, s->nn, s->x[c], s->F[c], s->J[c], s->mat[c],
-                                         s->status);
-    GPE_CHECK_LAUNCH("k_g2p_p2g");
-    return GPE_OK;
-}
-
-int32_t launch_fused(gpe_mpm* s, const float4* gin, float4* gout, float4* gzero, cudaStream_t st)
-{
-    s->launches += 1;
-    switch (mode_of(s)) {
-        case MODE_FLUID: return launch_fused_t<MODE_FLUID>(s, gin, gout, gzero, st);
-        case MODE_COROT: return launch_fused_t<MODE_COROT>(s, gin, gout, gzero, st);
-        case MODE_SNOW: return launch_fused_t<MODE_SNOW>(s, gin, gout, gzero, st);
-        case MODE_NEOHOOKEAN: return launch_fused_t<MODE_NEOHOOKEAN>(s, gin, gout, gzero, st);
-        case MODE_SAND: return launch_fused_t<MODE_SAND>(s, gin, gout, gzero, st);
-        default: return launch_fused_t<MODE_MIXED>(s, gin, gout, gzero, st);
-    }
-}
-
 int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
 {
     if (lsz(s) <= 1) { return GPE_OK; }
@@ -897,7 +840,7 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
     return GPE_OK;
 }
 
-// n_steps steps: [sort], P2G, (n-1) x fused G2P+P2G, G2P. Grids ga+1 and ga+2 are zero on entry and exit.
+// n_steps steps: [sort], P2G, (n-1) x (G2P, P2G), G2P. Grids ga+1 and ga+2 are zero on entry and exit.
 int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
 {
     int32_t rc = GPE_OK;
@@ -908,7 +851,9 @@ int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
     for (int32_t t = 1; t < n_steps && rc == GPE_OK; ++t) {
         const int b = (a + 1) % 3, z = (a + 2) % 3;
         if (lsz(s) > 0) {
-            rc = launch_fused(s, s->grid[a], s->grid[b], s->grid[z], st);
+            // G2P of this step (zeroing the grid read two steps ago), P2G of the next into the zero grid b
+            rc = launch_g2p<true>(s, s->grid[a], s->grid[z], st);
+            if (rc == GPE_OK) { rc = launch_p2g(s, s->grid[b], st); }
         } else {
             k_clear<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->grid[z], s->nn);
             GPE_CHECK_LAUNCH("k_clear");

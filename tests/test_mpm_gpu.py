@@ -111,7 +111,7 @@ def test_grid_and_g2p_stages(gpe_mod, oracle, cuda_ok, kind):
 
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("steps", [1, 4])
-def test_fused_steps(gpe_mod, oracle, cuda_ok, kind, steps):
+def test_multi_step_calls(gpe_mod, oracle, cuda_ok, kind, steps):
     p, x, v, Cm, F, J, mat = _scene(kind)
     e = _engine(gpe_mod, p, x, v, Cm, F, J, mat)
     e.step(steps)
