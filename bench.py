@@ -498,6 +498,11 @@ def run_gpe(args, rank, ws):
     o_vel = torch.empty((n, 2), dtype=torch.float32).pin_memory()
 
     eng.set_state(pos, vel, stream=sh)
+    # the engine's autotuner picks cell size, block size, persistent solve and mask skin for this scene (it
+    # restores the state afterwards); untimed
+    best, _ = eng.autotune(trial_steps=3, stream=sh)
+    cfg["tuning"] = {"cell_over_h": round(best.cell / p.h, 3), "block": best.block,
+                     "persistent": bool(best.persistent), "skin": round(best.skin, 3)}
     for _ in range(args.warmup):
         eng.step(1, stream=sh)
     torch.cuda.synchronize()
@@ -522,7 +527,8 @@ def run_gpe(args, rank, ws):
 
     # ---- stage-by-stage pass for the per-kernel roofline ----
     stage_ms = {k: [] for k in ALG_BYTES}
-    stage_launches = {"predict_sort": 6, "lambda": 1, "delta_p": 1, "xsph": 1}
+    # the sort stage's launches: the step's, less one λ and one Δp per iteration and the XSPH pass
+    stage_launches = {"predict_sort": launches - 2 * p.iters - 1, "lambda": 1, "delta_p": 1, "xsph": 1}
     for _ in range(args.steps):
         flush_l2()
         seq = [("predict_sort", gpe.PBF_STAGE_PREDICT_SORT)]
@@ -552,7 +558,12 @@ def run_gpe(args, rank, ws):
                 "peak_source": peak_kind, "traffic": NCU_TRAFFIC.get(dom_name),
                 "alg_bytes_per_launch": ALG_BYTES[dom_name] * n, "launch_ms": per_launch_ms,
                 "share": {k: v / tot for k, v in share.items()},
-                "stage_ms_per_step": {k: statistics.mean(v) for k, v in stage_ms.items()}}
+                "stage_ms_per_step": {k: statistics.mean(v) for k, v in stage_ms.items()},
+                # every stage's algorithmic bytes (per pass; the sort stage's for its whole group of launches)
+                # over its time, and that against the peak
+                "stage_gbs": {k: ALG_BYTES[k] * n / (statistics.mean(v) / 1e3) / 1e9 for k, v in stage_ms.items()},
+                "stage_frac": {k: ALG_BYTES[k] * n / (statistics.mean(v) / 1e3) / 1e9 / peak
+                               for k, v in stage_ms.items()}}
 
     # ---- end to end through the C ABI with host buffers ----
     e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))

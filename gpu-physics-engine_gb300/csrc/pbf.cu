@@ -2188,10 +2188,18 @@ int32_t gpe_pbf_status(gpe_pbf* s, uint32_t* status, void* stream)
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
 {
     if (!s || !launches) { return GPE_ERR_BAD_ARG; }
-    const bool warm = s->prm.iters > 0;
+    const bool warm      = s->prm.iters > 0;
+    const bool vort      = s->prm.vort_eps != 0.f;
+    const int32_t sorted = 3 + gpe::scan_launches(s->ncells); // predict + histogram, scan, scatter, place
+    if (s->persistent && !accumulating(s)) {
+        // the passes (and XSPH without vorticity) in one cooperative launch; with vorticity XSPH and the
+        // confinement keep their launches
+        *launches = sorted + 1 + (vort ? 2 : 0);
+        return GPE_OK;
+    }
     // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network
     const int32_t first = (warm && s->warm == GPE_WARM_PREV) ? -1 : ((warm && s->warm == GPE_WARM_MLP) ? 1 : 0);
-    *launches = 6 + 2 * s->prm.iters + 1 + (s->prm.vort_eps != 0.f ? 1 : 0) + first;
+    *launches = sorted + 2 * s->prm.iters + 1 + (vort ? 1 : 0) + first;
     return GPE_OK;
 }
 
