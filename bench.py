@@ -397,7 +397,8 @@ def mpm_leg(args, stream, flush_l2):
            material and plastic state read and written once) plus 64 per grid node;
     library: the same grid and particle count with a fifth each of water, jelly, snow, Neo-Hookean and
            Drucker-Prager sand (two discs each);
-    elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid, dt = 1e-4 (launch-bound)."""
+    elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid, dt = 1e-4 (launch-bound);
+    batched_32: 32 mixed scenes of 64k-512k particles in one engine (batched_mpm)."""
     import torch
 
     import gpe
@@ -406,10 +407,10 @@ def mpm_leg(args, stream, flush_l2):
     sh = stream.cuda_stream
     peak, _ = peaks()
 
-    def timed(p, pos, vel, mat, alg_bytes):
+    def timed(p, pos, vel, mat, alg_bytes, scene_list=None, sid=None):
         n = len(pos)
-        e = gpe.Mpm(p, capacity=n)
-        e.set_state(pos, vel, material=mat, stream=sh)
+        e = gpe.Mpm(p, capacity=n, scenes=scene_list)
+        e.set_state(pos, vel, material=mat, stream=sh, scene_id=sid)
         for _ in range(args.warmup):
             e.step(1, stream=sh)
         torch.cuda.synchronize()
@@ -441,7 +442,51 @@ def mpm_leg(args, stream, flush_l2):
     pe = scenes.elastic_params()
     pos, vel = scenes.two_squares()
     out["elastic_65k"] = timed(pe, pos, vel, None, 120.0 * len(pos) + 64.0 * pe.nx * pe.ny)
+    out["batched_32"] = batched_mpm(timed, sh, stream)
     return out
+
+
+def batched_mpm(timed, sh, stream):
+    """32 mixed-material scenes of 64k-512k particles (log-uniform, seed 6), each on its own square grid at
+    the 4M scene's particle density, in one engine (one set of launches per step over all scenes); beside
+    it the same scenes as 32 engines stepped one after the other on the stream."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+
+    p, sc, pos, mat, sid = scenes.mixed_batch()
+    table = [gpe.make_mpm_scene(*s) for s in sc]
+    nodes = sum(s[0] * s[1] for s in sc)
+    n = len(pos)
+    r = timed(p, pos, np.zeros_like(pos), mat, 136.0 * n + 64.0 * nodes, scene_list=table, sid=sid)
+    r.update({"scenes": len(sc), "nodes": nodes})
+    solo = []
+    for q, s in enumerate(sc):
+        ps = p.copy()
+        ps.nx, ps.ny = s[0], s[1]
+        ps.clamp_lo[0], ps.clamp_lo[1] = s[2]
+        ps.clamp_hi[0], ps.clamp_hi[1] = s[3]
+        sel = sid == q
+        e = gpe.Mpm(ps, capacity=int(sel.sum()))
+        e.set_state(pos[sel], np.zeros_like(pos[sel]), material=mat[sel], stream=sh)
+        solo.append(e)
+    for _ in range(3):
+        for e in solo:
+            e.step(1, stream=sh)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    a.record(stream)
+    for _ in range(reps):
+        for e in solo:
+            e.step(1, stream=sh)
+    b.record(stream)
+    torch.cuda.synchronize()
+    r["solo_engines_ms_per_step"] = a.elapsed_time(b) / reps
+    for e in solo:
+        e.close()
+    return r
 
 
 def run_reference(args, rank, ws):

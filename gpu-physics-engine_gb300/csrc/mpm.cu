@@ -28,13 +28,23 @@
 
 namespace gpe {
 
+// One scene's node grid: nodes [goff, goff + nx * ny) of the node array, row-major; its particles are
+// clamped to [lo, hi] (handleOOB, MPM.cu:267-301).
+struct MpmScene {
+    int32_t nx, ny;
+    uint32_t goff;
+    float lo_x, lo_y, hi_x, hi_y;
+};
+
 struct MpmK {
     float dx, inv_dx, goff, dt;
-    int32_t nx, ny;
     float gdt_x, gdt_y;
     float mass, vol0;
     int32_t bc_type, bc_width;
-    float lo_x, lo_y, hi_x, hi_y, mid_x, mid_y;
+    MpmScene s0;            // the scene when there is one
+    const MpmScene* scenes; // device table when there are several (particles carry their scene)
+    int32_t n_scenes;
+    int64_t nn;             // nodes of all scenes
     int32_t material;
     uint32_t flags;
     float k_bulk, gamma, p_min, p_max, J_min, J_max;
@@ -61,6 +71,31 @@ __device__ __forceinline__ bool keeps_j(int m) { return m == MODE_FLUID || m == 
 
 __device__ __forceinline__ int32_t count_of(const MpmK& k) { return k.n_dev ? __ldg(k.n_dev) : k.n; }
 
+// the scene of particle i (ids are checked when set; clamped here as well, so that no id reads past the table).
+// MS: the engine holds several scenes (kernels for one scene compile without the lookup).
+template <bool MS = true>
+__device__ __forceinline__ MpmScene scene_of(const MpmK& k, const int32_t* __restrict__ sid, int32_t i)
+{
+    if (!MS || k.n_scenes <= 1) { return k.s0; }
+    return k.scenes[min(max(__ldg(&sid[i]), 0), k.n_scenes - 1)];
+}
+
+// the scene that owns node idx (the last whose first node is not past idx)
+__device__ __forceinline__ MpmScene scene_of_node(const MpmK& k, int64_t idx)
+{
+    if (k.n_scenes <= 1) { return k.s0; }
+    int32_t lo = 0, hi = k.n_scenes - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if ((int64_t)k.scenes[mid].goff <= idx) {
+            lo = mid;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    return k.scenes[lo];
+}
+
 struct Stencil {
     int32_t bx, by;
     float fx, fy;
@@ -68,19 +103,19 @@ struct Stencil {
 };
 
 // quadratic B-spline weights, MPM.cu:92-110 (gridCoord MPM.cu:84)
-__device__ __forceinline__ Stencil stencil(const MpmK& k, float2 p, uint32_t* status)
+__device__ __forceinline__ Stencil stencil(const MpmK& k, const MpmScene& sc, float2 p, uint32_t* status)
 {
     Stencil s;
     const float gx = p.x * k.inv_dx + k.goff;
     const float gy = p.y * k.inv_dx + k.goff;
     int32_t bx     = (int32_t)floorf(gx - 0.5f);
     int32_t by     = (int32_t)floorf(gy - 0.5f);
-    if (bx < 0 || by < 0 || bx > k.nx - 3 || by > k.ny - 3) {
+    if (bx < 0 || by < 0 || bx > sc.nx - 3 || by > sc.ny - 3) {
         // outside the halo: clamp the stencil to the grid and report it (the reference relies on its 2-node
         // halo instead, MPM.cu:84 / cuda-engine.h:192-194)
         atomicOr(status, GPE_STATUS_CAPACITY);
-        bx = min(max(bx, 0), k.nx - 3);
-        by = min(max(by, 0), k.ny - 3);
+        bx = min(max(bx, 0), sc.nx - 3);
+        by = min(max(by, 0), sc.ny - 3);
     }
     s.bx     = bx;
     s.by     = by;
@@ -180,14 +215,14 @@ __device__ __forceinline__ float4 affine(const MpmK& k, int m, float4 Cp, float4
 }
 
 // node velocity as the reference's gridKernel leaves it (MPM.cu:150-175), from the raw accumulated node
-__device__ __forceinline__ float2 node_velocity(const MpmK& k, float4 g, int32_t x, int32_t y)
+__device__ __forceinline__ float2 node_velocity(const MpmK& k, const MpmScene& sc, float4 g, int32_t x, int32_t y)
 {
     if (!(g.z > 0.f)) { return make_float2(0.f, 0.f); }
     const float inv_m = 1.f / g.z;
     float vx          = g.x * inv_m + k.gdt_x;
     float vy          = g.y * inv_m + k.gdt_y;
-    const bool wl = x <= k.bc_width, wr = x >= k.nx - 1 - k.bc_width;
-    const bool wb = y <= k.bc_width, wt = y >= k.ny - 1 - k.bc_width;
+    const bool wl = x <= k.bc_width, wr = x >= sc.nx - 1 - k.bc_width;
+    const bool wb = y <= k.bc_width, wt = y >= sc.ny - 1 - k.bc_width;
     if (k.bc_type == GPE_MPM_BC_STICKY) {
         if (wl || wr || wb || wt) { vx = vy = 0.f; }
     } else {
@@ -214,10 +249,10 @@ struct PState {
 // G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301). RAW: the grid holds accumulated
 // momentum/mass and the node update is applied on the fly; otherwise it holds velocities.
 template <bool RAW>
-__device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, const float4* __restrict__ grid,
-                                         PState& ps, uint32_t* status)
+__device__ __forceinline__ void g2p_body(const MpmK& k, const MpmScene& sc, int m, bool track_f,
+                                         const float4* __restrict__ grid, PState& ps, uint32_t* status)
 {
-    const Stencil s = stencil(k, ps.x, status);
+    const Stencil s = stencil(k, sc, ps.x, status);
     float2 vel      = make_float2(0.f, 0.f);
     float4 B        = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -228,10 +263,10 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
             const float dpx     = ((float)i - s.fx) * k.dx;
             const float dpy     = ((float)j - s.fy) * k.dx;
             const int32_t nxi   = s.bx + i, nyj = s.by + j;
-            const float4 g      = __ldg(&grid[(size_t)nyj * (size_t)k.nx + (size_t)nxi]);
+            const float4 g      = __ldg(&grid[(size_t)sc.goff + (size_t)nyj * (size_t)sc.nx + (size_t)nxi]);
             float2 vi;
             if (RAW) {
-                vi = node_velocity(k, g, nxi, nyj);
+                vi = node_velocity(k, sc, g, nxi, nyj);
             } else {
                 vi = make_float2(g.x, g.y);
             }
@@ -248,29 +283,29 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
     ps.C       = make_float4(k.apic_s * B.x, k.apic_s * B.y, k.apic_s * B.z, k.apic_s * B.w);
     // handleOOB
     if (!isfinite(pos.x) || !isfinite(vel.x)) {
-        pos.x = k.mid_x;
+        pos.x = 0.5f * (sc.lo_x + sc.hi_x);
         vel.x = 0.f;
         atomicOr(status, GPE_STATUS_NONFINITE);
     }
     if (!isfinite(pos.y) || !isfinite(vel.y)) {
-        pos.y = k.mid_y;
+        pos.y = 0.5f * (sc.lo_y + sc.hi_y);
         vel.y = 0.f;
         atomicOr(status, GPE_STATUS_NONFINITE);
     }
-    if (pos.x < k.lo_x) {
-        pos.x = k.lo_x;
+    if (pos.x < sc.lo_x) {
+        pos.x = sc.lo_x;
         vel.x = fmaxf(vel.x, 0.f);
     }
-    if (pos.x > k.hi_x) {
-        pos.x = k.hi_x;
+    if (pos.x > sc.hi_x) {
+        pos.x = sc.hi_x;
         vel.x = fminf(vel.x, 0.f);
     }
-    if (pos.y < k.lo_y) {
-        pos.y = k.lo_y;
+    if (pos.y < sc.lo_y) {
+        pos.y = sc.lo_y;
         vel.y = fmaxf(vel.y, 0.f);
     }
-    if (pos.y > k.hi_y) {
-        pos.y = k.hi_y;
+    if (pos.y > sc.hi_y) {
+        pos.y = sc.hi_y;
         vel.y = fminf(vel.y, 0.f);
     }
     ps.x = pos;
@@ -333,16 +368,21 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, int m, bool track_f, con
 
 // Scatter of one block's particles through a shared-memory tile (particleToGrid, MPM.cu:116-126). All threads of the block must call it;
 // `valid` marks threads that carry a particle.
-__device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stencil& s, float2 v, float4 Q,
-                                          float4* __restrict__ grid)
+template <bool MS>
+__device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s,
+                                          float2 v, float4 Q, float4* __restrict__ grid)
 {
     __shared__ float s_x[TILE_CAP], s_y[TILE_CAP], s_m[TILE_CAP];
     __shared__ int32_t s_box[4];
+    __shared__ uint32_t s_goff[2]; // the block's lowest and highest scene (first node): one scene to tile
+    __shared__ int32_t s_nx;
     if (threadIdx.x == 0) {
-        s_box[0] = INT32_MAX;
-        s_box[1] = INT32_MAX;
-        s_box[2] = INT32_MIN;
-        s_box[3] = INT32_MIN;
+        s_box[0]  = INT32_MAX;
+        s_box[1]  = INT32_MAX;
+        s_box[2]  = INT32_MIN;
+        s_box[3]  = INT32_MIN;
+        s_goff[0] = 0xffffffffu;
+        s_goff[1] = 0u;
     }
     __syncthreads();
     // bounding box of the block's stencil bases
@@ -361,11 +401,23 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
         atomicMax(&s_box[2], mxx);
         atomicMax(&s_box[3], mxy);
     }
+    if (MS && k.n_scenes > 1) { // uniform: the scenes of the block's particles, a warp at a time
+        const uint32_t glo = __reduce_min_sync(0xffffffffu, valid ? sc.goff : 0xffffffffu);
+        const uint32_t ghi = __reduce_max_sync(0xffffffffu, valid ? sc.goff : 0u);
+        if ((threadIdx.x & 31) == 0 && glo != 0xffffffffu) {
+            atomicMin(&s_goff[0], glo);
+            atomicMax(&s_goff[1], ghi);
+        }
+        if (valid && glo == sc.goff) { s_nx = sc.nx; } // read only when the block holds one scene
+    }
     __syncthreads();
     const int32_t tx0 = s_box[0], ty0 = s_box[1];
     if (tx0 == INT32_MAX) { return; } // no particle in this block (uniform)
     const int32_t tw = s_box[2] - tx0 + 3, th = s_box[3] - ty0 + 3;
-    const bool tiled = tw * th <= TILE_CAP;
+    const bool one       = !MS || k.n_scenes <= 1;
+    const uint32_t bgoff = one ? 0u : s_goff[0];
+    const int32_t bnx    = one ? k.s0.nx : s_nx;
+    const bool tiled     = tw * th <= TILE_CAP && (one || bgoff == s_goff[1]); // across scenes: scatter directly
     if (tiled) {
         for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
             s_x[t] = 0.f;
@@ -379,7 +431,7 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
     // segmented shuffle reduction, and only the run's first lane updates the tile (or the grid): float
     // atomics on one shared address serialise, and the lanes of a run would otherwise all hit the same 9.
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t key  = valid ? (uint32_t)s.by * (uint32_t)k.nx + (uint32_t)s.bx : 0xffffffffu;
+    const uint32_t key  = valid ? sc.goff + (uint32_t)s.by * (uint32_t)sc.nx + (uint32_t)s.bx : 0xffffffffu;
     const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
     const bool head     = lane == 0u || prev != key;
     const uint32_t heads = __ballot_sync(0xffffffffu, head);
@@ -415,7 +467,8 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
                 atomicAdd(&s_y[t], cy);
                 atomicAdd(&s_m[t], cm);
             } else {
-                atomicAdd(&grid[(size_t)(s.by + j) * (size_t)k.nx + (size_t)(s.bx + i)], make_float4(cx, cy, cm, 0.f));
+                atomicAdd(&grid[(size_t)sc.goff + (size_t)(s.by + j) * (size_t)sc.nx + (size_t)(s.bx + i)],
+                          make_float4(cx, cy, cm, 0.f));
             }
         }
     }
@@ -425,7 +478,8 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, bool valid, const Stenc
             const float m = s_m[t];
             if (m != 0.f) {
                 const int32_t gx = tx0 + t % tw, gy = ty0 + t / tw;
-                atomicAdd(&grid[(size_t)gy * (size_t)k.nx + (size_t)gx], make_float4(s_x[t], s_y[t], m, 0.f));
+                atomicAdd(&grid[(size_t)bgoff + (size_t)gy * (size_t)bnx + (size_t)gx],
+                          make_float4(s_x[t], s_y[t], m, 0.f));
             }
         }
     }
@@ -441,14 +495,15 @@ __global__ void k_clear(float4* __restrict__ grid, int64_t nn)
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(T_MPM)
+template <int MODE, bool MS>
+__global__ void __launch_bounds__(T_MPM, 8) // 8 blocks per SM (32 registers, 8 x 24 KB of node tiles)
     k_p2g(const MpmK k, const float2* __restrict__ x, const float2* __restrict__ v, const float4* __restrict__ C,
           const float4* __restrict__ F, const float* __restrict__ J, const int32_t* __restrict__ mat,
-          float4* __restrict__ grid, uint32_t* status)
+          const int32_t* __restrict__ sid, float4* __restrict__ grid, uint32_t* status)
 {
     const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < count_of(k);
+    const MpmScene sc = valid ? scene_of<MS>(k, sid, i) : k.s0;
     Stencil s{};
     float2 vv = make_float2(0.f, 0.f);
     float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -458,19 +513,21 @@ __global__ void __launch_bounds__(T_MPM)
         const float Jp  = keeps_j(m) ? J[i] : 1.f;
         Q               = affine(k, m, C[i], Fp, Jp);
         vv              = v[i];
-        s               = stencil(k, x[i], status);
+        s               = stencil(k, sc, x[i], status);
     }
-    p2g_block(k, valid, s, vv, Q, grid);
+    p2g_block<MS>(k, sc, valid, s, vv, Q, grid);
 }
 
 // gridKernel, MPM.cu:131-177 (in place)
 __global__ void k_grid(const MpmK k, float4* __restrict__ grid)
 {
-    const int64_t nn     = (int64_t)k.nx * k.ny;
+    const int64_t nn     = k.nn;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn; idx += stride) {
         float4 g        = grid[idx];
-        const float2 vv = node_velocity(k, g, (int32_t)(idx % k.nx), (int32_t)(idx / k.nx));
+        const MpmScene sc    = scene_of_node(k, idx);
+        const int64_t local  = idx - (int64_t)sc.goff;
+        const float2 vv      = node_velocity(k, sc, g, (int32_t)(local % sc.nx), (int32_t)(local / sc.nx));
         g.x             = vv.x;
         g.y             = vv.y;
         grid[idx]       = g;
@@ -478,11 +535,11 @@ __global__ void k_grid(const MpmK k, float4* __restrict__ grid)
 }
 
 // G2P on a grid of velocities (RAW=false) or of raw momentum (RAW=true); writes the whole particle state
-template <int MODE, bool RAW>
+template <int MODE, bool RAW, bool MS>
 __global__ void __launch_bounds__(T_MPM)
     k_g2p(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ x, float2* __restrict__ v,
           float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
-          float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
+          const int32_t* __restrict__ sid, float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (zero_grid) {
@@ -496,7 +553,7 @@ __global__ void __launch_bounds__(T_MPM)
     ps.x = x[i];
     ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
     ps.J = keeps_j(m) ? J[i] : 1.f;
-    g2p_body<RAW>(k, m, track_f, grid, ps, status);
+    g2p_body<RAW>(k, scene_of<MS>(k, sid, i), m, track_f, grid, ps, status);
     x[i] = ps.x;
     v[i] = ps.v;
     C[i] = ps.C;
@@ -506,16 +563,17 @@ __global__ void __launch_bounds__(T_MPM)
 
 // ----- spatial sort of the particles (keeps P2G tiles small) ---------------------------------------------
 __global__ void __launch_bounds__(T_MPM)
-    k_mpm_key(const MpmK k, const float2* __restrict__ x, uint2* __restrict__ keyrank, uint32_t* __restrict__ count,
-              uint32_t* status)
+    k_mpm_key(const MpmK k, const float2* __restrict__ x, const int32_t* __restrict__ sid, uint2* __restrict__ keyrank,
+              uint32_t* __restrict__ count, uint32_t* status)
 {
     const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid   = i < count_of(k);
     const int32_t lane = threadIdx.x & 31;
     uint32_t key       = 0xffffffffu;
     if (valid) {
-        const Stencil s = stencil(k, x[i], status);
-        key             = (uint32_t)s.by * (uint32_t)k.nx + (uint32_t)s.bx;
+        const MpmScene sc = scene_of(k, sid, i);
+        const Stencil s   = stencil(k, sc, x[i], status);
+        key               = sc.goff + (uint32_t)s.by * (uint32_t)sc.nx + (uint32_t)s.bx;
     }
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
     const int32_t leader = __ffs(peers) - 1;
@@ -532,7 +590,8 @@ __global__ void __launch_bounds__(T_MPM)
                  const float4* __restrict__ C0, const float4* __restrict__ F0, const float* __restrict__ J0,
                  const int32_t* __restrict__ m0, const uint32_t* __restrict__ id0, float2* __restrict__ x1,
                  float2* __restrict__ v1, float4* __restrict__ C1, float4* __restrict__ F1, float* __restrict__ J1,
-                 int32_t* __restrict__ m1, uint32_t* __restrict__ id1)
+                 int32_t* __restrict__ m1, uint32_t* __restrict__ id1, const int32_t* __restrict__ sid0,
+                 int32_t* __restrict__ sid1)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= __ldg(n_dev)) { return; }
@@ -549,6 +608,23 @@ __global__ void __launch_bounds__(T_MPM)
     J1[d]            = J0[i];
     m1[d]            = m0[i];
     id1[d]           = id0[i];
+    if (sid0) { sid1[d] = sid0[i]; }
+}
+
+// scene ids in the caller's order (ids_in[original index]) into storage order; ids out of range are reported
+// (GPE_STATUS_CAPACITY) and stored as 0
+__global__ void k_mpm_scene_ids(int32_t n, int32_t n_scenes, const uint32_t* __restrict__ id,
+                                const int32_t* __restrict__ ids_in, int32_t* __restrict__ sid, uint32_t* status)
+{
+    const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) { return; }
+    const uint32_t o = id[j];
+    int32_t q        = (o < (uint32_t)n) ? ids_in[o] : -1;
+    if (q < 0 || q >= n_scenes) {
+        atomicOr(status, GPE_STATUS_CAPACITY);
+        q = 0;
+    }
+    sid[j] = q;
 }
 
 // get_state helper: put particle i back at its original index id[i]
@@ -661,6 +737,9 @@ struct gpe_mpm {
     float* J[2]     = {};
     int32_t* mat[2] = {};
     uint32_t* id[2] = {};
+    int32_t* sid[2] = {};          // scene of each particle (several scenes only)
+    std::vector<MpmScene> scenes;  // several scenes: their grids, in the order of the node array
+    MpmScene* d_scenes = nullptr;
     float4* grid[3] = {};
     uint2* keyrank  = nullptr;
     uint32_t* bucket = nullptr;
@@ -706,20 +785,15 @@ MpmK mpm_make_k(const gpe_mpm_params& p)
     k.inv_dx    = 1.f / p.dx;
     k.goff      = p.grid_offset;
     k.dt        = p.dt;
-    k.nx        = p.nx;
-    k.ny        = p.ny;
+    k.s0        = MpmScene{p.nx, p.ny, 0u, p.clamp_lo[0], p.clamp_lo[1], p.clamp_hi[0], p.clamp_hi[1]};
+    k.n_scenes  = 1;
+    k.nn        = (int64_t)p.nx * p.ny;
     k.gdt_x     = p.gravity[0] * p.dt;
     k.gdt_y     = p.gravity[1] * p.dt;
     k.mass      = p.mass;
     k.vol0      = p.vol0;
     k.bc_type   = p.bc_type;
     k.bc_width  = p.bc_width;
-    k.lo_x      = p.clamp_lo[0];
-    k.lo_y      = p.clamp_lo[1];
-    k.hi_x      = p.clamp_hi[0];
-    k.hi_y      = p.clamp_hi[1];
-    k.mid_x     = 0.5f * (p.clamp_lo[0] + p.clamp_hi[0]);
-    k.mid_y     = 0.5f * (p.clamp_lo[1] + p.clamp_hi[1]);
     k.material  = p.material;
     k.flags     = p.flags;
     k.k_bulk    = p.k_bulk;
@@ -775,8 +849,13 @@ template <int MODE>
 int32_t launch_p2g_t(gpe_mpm* s, float4* grid, cudaStream_t st)
 {
     const int c = s->cur;
-    k_p2g<MODE><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
-                                                  grid, s->status);
+    if (s->scenes.size() > 1) {
+        k_p2g<MODE, true><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+                                                            s->mat[c], s->sid[c], grid, s->status);
+    } else {
+        k_p2g<MODE, false><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+                                                             s->mat[c], nullptr, grid, s->status);
+    }
     GPE_CHECK_LAUNCH("k_p2g");
     return GPE_OK;
 }
@@ -800,8 +879,13 @@ int32_t launch_g2p_t(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t 
 {
     const int c      = s->cur;
     const unsigned g = std::max(mblocks(lsz(s)), zero ? grid_blocks(s->nn) : 1u);
-    k_g2p<MODE, RAW><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c], s->mat[c],
-                                          zero, zero ? s->nn : 0, s->status);
+    if (s->scenes.size() > 1) {
+        k_g2p<MODE, RAW, true><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+                                                    s->mat[c], s->sid[c], zero, zero ? s->nn : 0, s->status);
+    } else {
+        k_g2p<MODE, RAW, false><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+                                                     s->mat[c], nullptr, zero, zero ? s->nn : 0, s->status);
+    }
     GPE_CHECK_LAUNCH("k_g2p");
     return GPE_OK;
 }
@@ -825,7 +909,7 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
 {
     if (lsz(s) <= 1) { return GPE_OK; }
     const int c = s->cur, o = c ^ 1;
-    k_mpm_key<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->keyrank, s->count, s->status);
+    k_mpm_key<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->sid[c], s->keyrank, s->count, s->status);
     GPE_CHECK_LAUNCH("k_mpm_key");
     int32_t rc = launch_exclusive_scan(s->count, (uint32_t)s->nn, s->bsum, s->start, st);
     if (rc) { return rc; }
@@ -833,7 +917,8 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
     if (rc) { return rc; }
     k_mpm_gather<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->d_count, s->keyrank, s->start, s->bucket, s->x[c], s->v[c],
                                                    s->C[c], s->F[c], s->J[c], s->mat[c], s->id[c], s->x[o],
-                                                   s->v[o], s->C[o], s->F[o], s->J[o], s->mat[o], s->id[o]);
+                                                   s->v[o], s->C[o], s->F[o], s->J[o], s->mat[o], s->id[o],
+                                                   s->sid[c], s->sid[o]);
     GPE_CHECK_LAUNCH("k_mpm_gather");
     s->cur ^= 1;
     s->launches += 3 + scan_launches((uint32_t)s->nn); // key, scan, scatter, gather
@@ -867,6 +952,18 @@ int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
     return rc;
 }
 
+// the engine's buffers and scene table in the kernel constants
+void bind_scenes(gpe_mpm* s)
+{
+    s->k.n_dev = s->d_count;
+    if (s->scenes.size() > 1) {
+        s->k.scenes   = s->d_scenes;
+        s->k.n_scenes = (int32_t)s->scenes.size();
+        s->k.s0       = s->scenes[0];
+        s->k.nn       = s->nn;
+    }
+}
+
 int32_t mpm_alloc(gpe_mpm* s)
 {
     const size_t N = (size_t)s->cap;
@@ -890,6 +987,13 @@ int32_t mpm_alloc(gpe_mpm* s)
     const size_t obs = c.take<uint32_t>(scan_blocks((uint32_t)M) + 1);
     const size_t oss = c.take<uint32_t>(4);
     const size_t ocnt = c.take<int32_t>(2);
+    const bool several = s->scenes.size() > 1;
+    size_t osid[2] = {0, 0}, osc = 0;
+    if (several) {
+        osid[0] = c.take<int32_t>(N);
+        osid[1] = c.take<int32_t>(N);
+        osc     = c.take<MpmScene>(s->scenes.size());
+    }
     GPE_TRY_CUDA(cudaMalloc(&s->base, c.off));
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
@@ -910,7 +1014,14 @@ int32_t mpm_alloc(gpe_mpm* s)
     s->bsum    = reinterpret_cast<uint32_t*>(b + obs);
     s->status  = reinterpret_cast<uint32_t*>(b + oss);
     s->d_count = reinterpret_cast<int32_t*>(b + ocnt);
-    s->k.n_dev = s->d_count;
+    if (several) {
+        s->sid[0]   = reinterpret_cast<int32_t*>(b + osid[0]);
+        s->sid[1]   = reinterpret_cast<int32_t*>(b + osid[1]);
+        s->d_scenes = reinterpret_cast<MpmScene*>(b + osc);
+        GPE_TRY_CUDA(cudaMemcpy(s->d_scenes, s->scenes.data(), sizeof(MpmScene) * s->scenes.size(),
+                                cudaMemcpyHostToDevice));
+    }
+    bind_scenes(s);
     return GPE_OK;
 }
 
@@ -923,21 +1034,56 @@ extern "C" {
 
 int32_t gpe_mpm_create(const gpe_mpm_params* params, int64_t capacity, gpe_mpm** out)
 {
+    return gpe_mpm_create_scenes(params, nullptr, 0, capacity, out);
+}
+
+int32_t gpe_mpm_create_scenes(const gpe_mpm_params* params, const gpe_mpm_scene* scenes, int32_t n_scenes,
+                              int64_t capacity, gpe_mpm** out)
+{
     gpe::clear_error();
-    if (!out || capacity < 0 || capacity > (int64_t)INT32_MAX / 2) { return GPE_ERR_BAD_ARG; }
-    *out       = nullptr;
-    int32_t rc = mpm_validate(params);
+    if (!out || capacity < 0 || capacity > (int64_t)INT32_MAX / 2 || n_scenes < 0 || (n_scenes > 0 && !scenes)) {
+        return GPE_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    // several scenes: their grids one after the other; the first scene's size stands in for params' grid
+    std::vector<MpmScene> table;
+    gpe_mpm_params prm = params ? *params : gpe_mpm_params{};
+    int64_t nodes      = 0;
+    for (int32_t q = 0; q < n_scenes; ++q) {
+        const gpe_mpm_scene& sc = scenes[q];
+        if (sc.nx < 3 || sc.ny < 3) {
+            gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_create_scenes: scene %d needs at least 3 x 3 nodes", q);
+            return GPE_ERR_BAD_ARG;
+        }
+        table.push_back(MpmScene{sc.nx, sc.ny, (uint32_t)nodes, sc.clamp_lo[0], sc.clamp_lo[1], sc.clamp_hi[0],
+                                 sc.clamp_hi[1]});
+        nodes += (int64_t)sc.nx * sc.ny;
+        if (nodes > ((int64_t)1 << 30)) {
+            gpe::set_error(GPE_ERR_CAPACITY, "gpe_mpm_create_scenes: more than 2^30 nodes");
+            return GPE_ERR_CAPACITY;
+        }
+    }
+    if (n_scenes > 0) {
+        prm.nx           = scenes[0].nx;
+        prm.ny           = scenes[0].ny;
+        prm.clamp_lo[0]  = scenes[0].clamp_lo[0];
+        prm.clamp_lo[1]  = scenes[0].clamp_lo[1];
+        prm.clamp_hi[0]  = scenes[0].clamp_hi[0];
+        prm.clamp_hi[1]  = scenes[0].clamp_hi[1];
+    }
+    int32_t rc = mpm_validate(params ? &prm : nullptr);
     if (rc) { return rc; }
     int dev = 0;
     rc      = gpe::current_device(&dev);
     if (rc) { return rc; }
     gpe_mpm* s = new gpe_mpm();
     s->device  = dev;
-    s->prm     = *params;
-    s->k       = mpm_make_k(*params);
-    s->dynamic = (params->flags & GPE_MPM_FLAG_DYNAMIC_COUNT) != 0;
+    s->prm     = prm;
+    s->k       = mpm_make_k(prm);
+    s->dynamic = (prm.flags & GPE_MPM_FLAG_DYNAMIC_COUNT) != 0;
     s->cap     = capacity;
-    s->nn      = (int64_t)params->nx * params->ny;
+    s->nn      = n_scenes > 0 ? nodes : (int64_t)prm.nx * prm.ny;
+    if (n_scenes > 1) { s->scenes = std::move(table); }
     rc         = mpm_alloc(s);
     if (rc) {
         if (s->base) { cudaFree(s->base); }
@@ -963,7 +1109,7 @@ int32_t gpe_mpm_set_params(gpe_mpm* s, const gpe_mpm_params* params)
     if (!s) { return GPE_ERR_BAD_ARG; }
     int32_t rc = mpm_validate(params);
     if (rc) { return rc; }
-    if (params->nx != s->prm.nx || params->ny != s->prm.ny) {
+    if (s->scenes.size() <= 1 && (params->nx != s->prm.nx || params->ny != s->prm.ny)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_params: the node grid is fixed at creation");
         return GPE_ERR_BAD_ARG;
     }
@@ -971,7 +1117,7 @@ int32_t gpe_mpm_set_params(gpe_mpm* s, const gpe_mpm_params* params)
     const int32_t n = s->k.n;
     s->k          = mpm_make_k(*params);
     s->k.n        = n;
-    s->k.n_dev    = s->d_count;
+    bind_scenes(s);
     s->dynamic    = (params->flags & GPE_MPM_FLAG_DYNAMIC_COUNT) != 0;
     s->drop_graphs();
     return GPE_OK;
@@ -1012,6 +1158,8 @@ int32_t gpe_mpm_set_state(gpe_mpm* s, const float* pos, const float* vel, const 
         k_mpm_init<<<mblocks(n), T_MPM, 0, st>>>((int32_t)n, s->id[0], s->v[0], s->C[0], s->F[0], s->J[0], s->mat[0],
                                                   !vel, !C, !F, !J, !material, s->prm.material);
         GPE_CHECK_LAUNCH("k_mpm_init");
+        // several scenes: every particle in scene 0 until gpe_mpm_set_scene_ids says otherwise
+        if (s->sid[0]) { GPE_TRY_CUDA(cudaMemsetAsync(s->sid[0], 0, sizeof(int32_t) * (size_t)n, st)); }
     }
     k_mpm_set_count<<<1, 1, 0, st>>>(s->d_count, (int32_t)n);
     GPE_CHECK_LAUNCH("k_mpm_set_count");
@@ -1052,6 +1200,45 @@ int32_t gpe_mpm_get_state(gpe_mpm* s, float* pos, float* vel, float* C, float* F
         if (J) { GPE_TRY_CUDA(cudaMemcpyAsync(J, s->J[o], sizeof(float) * (size_t)n, mk_out(mem), st)); }
     }
     if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
+    return GPE_OK;
+}
+
+int32_t gpe_mpm_set_scene_ids(gpe_mpm* s, const int32_t* scene_id, int64_t n, int32_t mem, void* stream)
+{
+    gpe::clear_error();
+    if (!s || (n > 0 && !scene_id) || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    int32_t rc      = mpm_sync_count(s, st);
+    if (rc) { return rc; }
+    if (!s->have_state || n != s->n) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_scene_ids: n must equal the particle count");
+        return GPE_ERR_BAD_ARG;
+    }
+    const int32_t ns = s->scenes.empty() ? 1 : (int32_t)s->scenes.size();
+    if (mem == GPE_MEM_HOST) {
+        for (int64_t i = 0; i < n; ++i) {
+            if (scene_id[i] < 0 || scene_id[i] >= ns) {
+                gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_scene_ids: ids must be in [0, %d)", ns);
+                return GPE_ERR_BAD_ARG;
+            }
+        }
+    }
+    if (ns == 1 || n == 0) { return GPE_OK; } // one scene: every particle is in it
+    // the caller's ids go through the other storage set, then into storage order
+    const int c = s->cur, o = c ^ 1;
+    GPE_TRY_CUDA(cudaMemcpyAsync(s->sid[o], scene_id, sizeof(int32_t) * (size_t)n, mk_in(mem), st));
+    uint32_t* flag = s->status + 1; // a word of its own, so the engine's status bits stay as they are
+    GPE_TRY_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t), st));
+    k_mpm_scene_ids<<<mblocks(n), T_MPM, 0, st>>>((int32_t)n, ns, s->id[c], s->sid[o], s->sid[c], flag);
+    GPE_CHECK_LAUNCH("k_mpm_scene_ids");
+    uint32_t bad = 0;
+    GPE_TRY_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    if (bad) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_mpm_set_scene_ids: ids must be in [0, %d)", ns);
+        return GPE_ERR_BAD_ARG;
+    }
+    s->steps_since_sort = s->prm.sort_interval; // the particles' keys changed: sort again first
     return GPE_OK;
 }
 
@@ -1180,6 +1367,10 @@ int32_t gpe_mpm_emit(gpe_mpm* s, const gpe_hose* hose, uint64_t seed, int32_t* r
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_emit: needs GPE_MPM_FLAG_DYNAMIC_COUNT");
         return GPE_ERR_NOT_READY;
     }
+    if (s->scenes.size() > 1) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_emit: an engine of one scene only");
+        return GPE_ERR_NOT_READY;
+    }
     HoseK h{};
     const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
     if (requested) { *requested = cnt; }
@@ -1205,6 +1396,10 @@ int32_t gpe_mpm_publish(gpe_mpm* s, const gpe_view* view, int32_t view_mem, void
     if (s->prm.sort_interval > 0) {
         // publish order is the storage order; re-sorting would shuffle it between ticks
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_publish: needs sort_interval == 0");
+        return GPE_ERR_NOT_READY;
+    }
+    if (s->scenes.size() > 1) { // positions are scene-local: a chunk view covers one scene
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_mpm_publish: an engine of one scene only");
         return GPE_ERR_NOT_READY;
     }
     cudaStream_t st = as_stream(stream);

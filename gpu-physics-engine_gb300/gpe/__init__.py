@@ -68,6 +68,18 @@ class MpmParams(C.Structure):
         return o
 
 
+class MpmScene(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("clamp_lo", C.c_float * 2), ("clamp_hi", C.c_float * 2)]
+
+
+def make_mpm_scene(nx: int, ny: int, clamp_lo, clamp_hi) -> MpmScene:
+    s = MpmScene()
+    s.nx, s.ny = int(nx), int(ny)
+    s.clamp_lo[0], s.clamp_lo[1] = clamp_lo
+    s.clamp_hi[0], s.clamp_hi[1] = clamp_hi
+    return s
+
+
 class Hose(C.Structure):
     _fields_ = [("origin", C.c_float * 2), ("velocity", C.c_float * 2), ("nozzle_width", C.c_float),
                 ("spacing", C.c_float), ("jitter", C.c_float), ("steps_per_call", C.c_int32)]
@@ -161,6 +173,8 @@ def lib() -> C.CDLL:
             "gpe_pbf_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_pbf_launches_per_step": [vp, C.POINTER(i32)],
             "gpe_mpm_create": [C.POINTER(MpmParams), i64, C.POINTER(vp)],
+            "gpe_mpm_create_scenes": [C.POINTER(MpmParams), C.POINTER(MpmScene), i32, i64, C.POINTER(vp)],
+            "gpe_mpm_set_scene_ids": [vp, vp, i64, i32, vp],
             "gpe_mpm_destroy": [vp],
             "gpe_mpm_set_params": [vp, C.POINTER(MpmParams)],
             "gpe_mpm_set_state": [vp, vp, vp, vp, vp, vp, vp, i64, i32, vp],
@@ -461,10 +475,18 @@ class Mlp:
 class Mpm:
     """One MLS-MPM engine handle (gpe_mpm)."""
 
-    def __init__(self, params: MpmParams, capacity: int):
+    def __init__(self, params: MpmParams, capacity: int, scenes=None):
+        """scenes: a list of MpmScene (gpe_mpm_create_scenes); None for one scene of params' grid."""
         self.params = params.copy()
         h = C.c_void_p()
-        check(lib().gpe_mpm_create(C.byref(self.params), int(capacity), C.byref(h)), "gpe_mpm_create")
+        if scenes:
+            arr = (MpmScene * len(scenes))(*scenes)
+            check(lib().gpe_mpm_create_scenes(C.byref(self.params), arr, len(scenes), int(capacity), C.byref(h)),
+                  "gpe_mpm_create_scenes")
+            self.nodes = sum(s.nx * s.ny for s in scenes)
+        else:
+            check(lib().gpe_mpm_create(C.byref(self.params), int(capacity), C.byref(h)), "gpe_mpm_create")
+            self.nodes = params.nx * params.ny
         self.h = h
         self.capacity = int(capacity)
 
@@ -483,7 +505,7 @@ class Mpm:
         check(lib().gpe_mpm_set_params(self.h, C.byref(params)), "gpe_mpm_set_params")
         self.params = params.copy()
 
-    def set_state(self, pos, vel=None, Cm=None, F=None, J=None, material=None, stream=None) -> None:
+    def set_state(self, pos, vel=None, Cm=None, F=None, J=None, material=None, stream=None, scene_id=None) -> None:
         if isinstance(pos, np.ndarray):
             pos = _f32(pos, 2)
             vel = None if vel is None else _f32(vel, 2)
@@ -495,6 +517,15 @@ class Mpm:
         check(lib().gpe_mpm_set_state(self.h, _ptr(pos), _ptr(vel), _ptr(Cm), _ptr(F), _ptr(J), _ptr(material), n,
                                       _mem(pos), stream), "gpe_mpm_set_state")
         self._keep = (pos, vel, Cm, F, J, material)
+        if scene_id is not None:
+            self.set_scene_ids(scene_id, stream=stream)
+
+    def set_scene_ids(self, scene_id, stream=None) -> None:
+        if isinstance(scene_id, np.ndarray):
+            scene_id = np.ascontiguousarray(scene_id, dtype=np.int32)
+        check(lib().gpe_mpm_set_scene_ids(self.h, _ptr(scene_id), len(scene_id), _mem(scene_id), stream),
+              "gpe_mpm_set_scene_ids")
+        self._keep_sid = scene_id
 
     @property
     def n(self) -> int:
@@ -524,7 +555,7 @@ class Mpm:
         check(lib().gpe_mpm_stage(self.h, int(stage), stream), f"gpe_mpm_stage({stage})")
 
     def grid(self, stream=None) -> np.ndarray:
-        nn = self.params.nx * self.params.ny
+        nn = self.nodes
         out = np.empty((nn, 4), np.float32)
         check(lib().gpe_mpm_get_grid(self.h, out.ctypes.data, nn, MEM_HOST, stream), "gpe_mpm_get_grid")
         return out

@@ -328,3 +328,28 @@ def mixed_discs(n: int = 4194304, seed: int = 4, discs_per_material: int = 3, ar
     cell = (np.floor(pos[:, 1] * 1024).astype(np.int64) * 1024 + np.floor(pos[:, 0] * 1024).astype(np.int64))
     order = np.argsort(cell, kind="stable")
     return pos[order], mat[order]
+
+
+def mixed_batch(n_scenes: int = 32, seed: int = 6, lo: int = 65536, hi: int = 524288, total_ref: int = 4194304):
+    """Independent mixed-material scenes for one batched engine: particle counts log-uniform in [lo, hi],
+    each scene water, snow and jelly discs (mixed_discs) covering 0.3 of its square box. Every scene has the
+    particle density of the total_ref-particle scene on the 1024^2 grid (mixed_params(total_ref)), so they
+    share dx, dt, mass and vol0; scene q's grid is g_q x g_q nodes, g_q = 1024 sqrt(n_q / total_ref) rounded
+    up to a multiple of 8 (128 nodes for 64k particles, 368 for 512k).
+    Returns (params, scenes, pos, mat, scene_id): scenes as (nx, ny, clamp_lo, clamp_hi) tuples, positions
+    in each scene's own coordinates, scene-major."""
+    g = rng(seed)
+    counts = np.exp(g.uniform(math.log(lo), math.log(hi), n_scenes)).astype(np.int64)
+    p = mixed_params(total_ref)
+    dx = p.dx
+    scenes, pos_l, mat_l, sid_l = [], [], [], []
+    for q in range(n_scenes):
+        n = int(counts[q])
+        side = int(math.ceil(1024.0 * math.sqrt(n / total_ref) / 8.0)) * 8
+        L = side * dx
+        pos, mat = mixed_discs(n, seed=1000 + seed * 64 + q)
+        scenes.append((side, side, (2 * dx, 2 * dx), (L - 3 * dx, L - 3 * dx)))
+        pos_l.append(pos * F32(L))
+        mat_l.append(mat)
+        sid_l.append(np.full(n, q, np.int32))
+    return p, scenes, np.concatenate(pos_l).astype(F32), np.concatenate(mat_l), np.concatenate(sid_l)

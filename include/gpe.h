@@ -417,6 +417,22 @@ typedef struct gpe_mpm gpe_mpm;
 #define GPE_MPM_STAGE_SORT 4  /* spatial re-sort of the particles         */
 
 int32_t gpe_mpm_create(const gpe_mpm_params* params, int64_t capacity, gpe_mpm** out);
+
+/* Several independent scenes in one engine (a batch; the reference runs one scene per arena). Scene q has its
+ * own node grid of nx x ny nodes (the node array holds the scenes' grids one after the other, in the order
+ * given) and its own particle clamp; the scenes share every other parameter (dx, dt, mass, materials, walls of
+ * bc_width nodes along each grid's edges). Particle positions are in their scene's coordinates, and each step
+ * is one set of launches over all scenes. params->nx, ny and the clamps are taken from scenes[0] and otherwise
+ * unused. Emitters and publish need an engine of one scene. */
+typedef struct gpe_mpm_scene {
+    int32_t nx, ny;
+    float clamp_lo[2], clamp_hi[2];
+} gpe_mpm_scene;
+int32_t gpe_mpm_create_scenes(const gpe_mpm_params* params, const gpe_mpm_scene* scenes, int32_t n_scenes,
+                              int64_t capacity, gpe_mpm** out);
+/* The scene of each particle, in the order gpe_mpm_set_state received them (which puts every particle in
+ * scene 0): n = the particle count, ids in [0, n_scenes); GPE_ERR_BAD_ARG (and no change) otherwise. */
+int32_t gpe_mpm_set_scene_ids(gpe_mpm* mpm, const int32_t* scene_id, int64_t n, int32_t mem, void* stream);
 int32_t gpe_mpm_destroy(gpe_mpm* mpm);
 int32_t gpe_mpm_set_params(gpe_mpm* mpm, const gpe_mpm_params* params);
 /* pos, vel: n float2; C, F: n float4 row-major (xx, xy, yx, yy); J: n float (for snow it is the plastic

@@ -167,3 +167,103 @@ def test_mpm_edge_cases(gpe_mod, cuda_ok):
     assert np.all(np.isfinite(x))  # handleOOB resets non-finite particles to the box centre
     assert e.status() & gpe_mod.STATUS_NONFINITE
     e.close()
+
+
+# ----- several scenes in one engine --------------------------------------------------------------------
+def _batch(gpe_mod, seed=3):
+    """Three scenes of different grids (32 x 48, 64 x 64, 40 x 40 nodes over one dx), every material mixed,
+    particles in each scene's interior, given in an order that interleaves the scenes."""
+    g = np.random.default_rng(seed)
+    p = _scene("mixed")[0]
+    sizes = [(32, 48), (64, 64), (40, 40)]
+    scenes, parts = [], []
+    for q, (nx, ny) in enumerate(sizes):
+        lo = (2 * p.dx, 2 * p.dx)
+        hi = ((nx - 3) * p.dx, (ny - 3) * p.dx)
+        scenes.append(gpe_mod.make_mpm_scene(nx, ny, lo, hi))
+        n = 700 + 300 * q
+        x = np.stack([g.uniform(0.25, 0.75, n) * nx * p.dx, g.uniform(0.25, 0.75, n) * ny * p.dx], 1)
+        v = g.normal(0, 0.5, (n, 2))
+        Cm = g.normal(0, 2.0, (n, 4))
+        F = np.tile(np.eye(2).ravel(), (n, 1)) + g.normal(0, 0.02, (n, 4))
+        J = g.uniform(0.97, 1.03, n)
+        mat = g.integers(0, 5, n)
+        parts.append((x, v, Cm, F, J, mat, np.full(n, q)))
+    cat = [np.concatenate([pp[k] for pp in parts]) for k in range(7)]
+    order = g.permutation(len(cat[0]))
+    x, v, Cm, F, J, mat, sid = (a[order] for a in cat)
+    f32 = np.float32
+    return (p, scenes, x.astype(f32), v.astype(f32), Cm.astype(f32), F.astype(f32), J.astype(f32),
+            mat.astype(np.int32), sid.astype(np.int32))
+
+
+def _scene_params(p, sc):
+    q = p.copy()
+    q.nx, q.ny = sc.nx, sc.ny
+    q.clamp_lo[0], q.clamp_lo[1] = sc.clamp_lo[0], sc.clamp_lo[1]
+    q.clamp_hi[0], q.clamp_hi[1] = sc.clamp_hi[0], sc.clamp_hi[1]
+    return q
+
+
+@pytest.mark.parametrize("sort_interval", [0, 2])
+def test_batched_scenes_match_each_scene_alone(gpe_mod, oracle, cuda_ok, sort_interval):
+    """Each scene of a batched engine against the oracle run on that scene alone (its own grid and clamp),
+    over several steps, with and without the periodic sort."""
+    p, scenes, x, v, Cm, F, J, mat, sid = _batch(gpe_mod)
+    p = p.copy()
+    p.sort_interval = sort_interval
+    e = gpe_mod.Mpm(p, capacity=len(x), scenes=scenes)
+    e.set_state(x, v, Cm, F, J, mat, scene_id=sid)
+    steps = 4
+    e.step(steps)
+    x1, v1, C1, F1, J1 = e.get_state()
+    assert e.status() == 0
+    for q, sc in enumerate(scenes):
+        sel = sid == q
+        wx, wv, wC, wF, wJ = oracle.MpmOracle(_scene_params(p, sc)).step(x[sel], v[sel], Cm[sel], F[sel], J[sel],
+                                                                        mat[sel], n_steps=steps)
+        rel = 1e-5 * steps
+        _close(x1[sel], wx, np.abs(wx), f"scene {q} x", rel=rel, floor=8 * EPS32 * np.abs(wx).max())
+        _close(v1[sel], wv, np.abs(wv).max(), f"scene {q} v", rel=10 * rel)
+        _close(C1[sel], wC, np.abs(wC).max(), f"scene {q} C", rel=10 * rel)
+        keep = mat[sel] != gpe_mod.MPM_MAT_FLUID
+        _close(F1[sel][keep], wF[keep], np.abs(wF[keep]).max(), f"scene {q} F", rel=10 * rel)
+
+
+def test_batched_grid_holds_each_scene_grid(gpe_mod, oracle, cuda_ok):
+    """P2G of a batched engine: the node array is the scenes' grids one after the other, each the oracle's
+    P2G of that scene's particles alone."""
+    p, scenes, x, v, Cm, F, J, mat, sid = _batch(gpe_mod, seed=5)
+    e = gpe_mod.Mpm(p, capacity=len(x), scenes=scenes)
+    e.set_state(x, v, Cm, F, J, mat, scene_id=sid)
+    e.stage(gpe_mod.MPM_STAGE_CLEAR)
+    e.stage(gpe_mod.MPM_STAGE_P2G)
+    g = e.grid()
+    off = 0
+    for q, sc in enumerate(scenes):
+        sel = sid == q
+        want = oracle.MpmOracle(_scene_params(p, sc)).p2g(x[sel], v[sel], Cm[sel], F[sel], J[sel], mat[sel])
+        got = g[off:off + sc.nx * sc.ny]
+        _close(got[:, 2], want[:, 2], np.abs(want[:, 2]).max(), f"scene {q} grid mass")
+        _close(got[:, :2], want[:, :2], np.abs(want[:, :2]).max(), f"scene {q} grid momentum", rel=2e-5)
+        off += sc.nx * sc.ny
+    assert e.status() == 0
+
+
+def test_batched_scene_ids_are_checked(gpe_mod, cuda_ok):
+    torch = pytest.importorskip("torch")
+    p, scenes, x, v, Cm, F, J, mat, sid = _batch(gpe_mod)
+    e = gpe_mod.Mpm(p, capacity=len(x), scenes=scenes)
+    e.set_state(x, v, Cm, F, J, mat)
+    bad = sid.copy()
+    bad[7] = 3
+    with pytest.raises(gpe_mod.GpeError):
+        e.set_scene_ids(bad)  # host ids: checked on the host
+    dbad = torch.from_numpy(bad).cuda()
+    with pytest.raises(gpe_mod.GpeError):
+        e.set_scene_ids(dbad)  # device ids: checked by a kernel, reported without a fault
+    e.set_scene_ids(torch.from_numpy(sid).cuda())
+    e.step(2)
+    assert e.status() == 0
+    with pytest.raises(gpe_mod.GpeError):
+        e.emit(gpe_mod.make_hose((0.2, 0.2), (1.0, 0.0), 0.05, 0.01, 0.0, 4))
