@@ -248,11 +248,18 @@ struct PState {
 
 // G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301). RAW: the grid holds accumulated
 // momentum/mass and the node update is applied on the fly; otherwise it holds velocities.
+// node velocity of a RAW (accumulated momentum and mass) or updated grid node, at scene-local node (x, y)
 template <bool RAW>
-__device__ __forceinline__ void g2p_body(const MpmK& k, const MpmScene& sc, int m, bool track_f,
-                                         const float4* __restrict__ grid, PState& ps, uint32_t* status)
+__device__ __forceinline__ float2 grid_velocity(const MpmK& k, const MpmScene& sc, float4 g, int32_t x, int32_t y)
 {
-    const Stencil s = stencil(k, sc, ps.x, status);
+    return RAW ? node_velocity(k, sc, g, x, y) : make_float2(g.x, g.y);
+}
+
+// G2P of one particle whose stencil is s; nv(x, y) gives the velocity of scene-local node (x, y)
+template <class NodeVel>
+__device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, int m, bool track_f, const Stencil& s,
+                                           NodeVel nv, PState& ps, uint32_t* status)
+{
     float2 vel      = make_float2(0.f, 0.f);
     float4 B        = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -262,14 +269,7 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, const MpmScene& sc, int 
             const float w       = s.wx[i] * s.wy[j];
             const float dpx     = ((float)i - s.fx) * k.dx;
             const float dpy     = ((float)j - s.fy) * k.dx;
-            const int32_t nxi   = s.bx + i, nyj = s.by + j;
-            const float4 g      = __ldg(&grid[(size_t)sc.goff + (size_t)nyj * (size_t)sc.nx + (size_t)nxi]);
-            float2 vi;
-            if (RAW) {
-                vi = node_velocity(k, sc, g, nxi, nyj);
-            } else {
-                vi = make_float2(g.x, g.y);
-            }
+            const float2 vi     = nv(s.bx + i, s.by + j);
             vel.x += w * vi.x;
             vel.y += w * vi.y;
             const float wvx = w * vi.x, wvy = w * vi.y;
@@ -366,16 +366,21 @@ __device__ __forceinline__ void g2p_body(const MpmK& k, const MpmScene& sc, int 
     }
 }
 
-// Scatter of one block's particles through a shared-memory tile (particleToGrid, MPM.cu:116-126). All threads of the block must call it;
-// `valid` marks threads that carry a particle.
+// The node box that one block's particles touch: nodes [tx0, tx0 + tw) x [ty0, ty0 + th) of scene sc.
+// tiled: the box fits TILE_CAP nodes and holds one scene. empty: no thread of the block carries a particle.
+struct BlockBox {
+    int32_t tx0, ty0, tw, th;
+    bool tiled, empty;
+    MpmScene sc;
+};
+
+// All threads of the block must call it; `valid` marks threads that carry a particle (stencil s, scene sc).
 template <bool MS>
-__device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s,
-                                          float2 v, float4 Q, float4* __restrict__ grid)
+__device__ __forceinline__ BlockBox block_box(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s)
 {
-    __shared__ float s_x[TILE_CAP], s_y[TILE_CAP], s_m[TILE_CAP];
     __shared__ int32_t s_box[4];
     __shared__ uint32_t s_goff[2]; // the block's lowest and highest scene (first node): one scene to tile
-    __shared__ int32_t s_nx;
+    __shared__ MpmScene s_sc;
     if (threadIdx.x == 0) {
         s_box[0]  = INT32_MAX;
         s_box[1]  = INT32_MAX;
@@ -408,16 +413,34 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
             atomicMin(&s_goff[0], glo);
             atomicMax(&s_goff[1], ghi);
         }
-        if (valid && glo == sc.goff) { s_nx = sc.nx; } // read only when the block holds one scene
+        if (valid && glo == sc.goff) { s_sc = sc; } // read only when the block holds one scene
     }
     __syncthreads();
-    const int32_t tx0 = s_box[0], ty0 = s_box[1];
-    if (tx0 == INT32_MAX) { return; } // no particle in this block (uniform)
-    const int32_t tw = s_box[2] - tx0 + 3, th = s_box[3] - ty0 + 3;
-    const bool one       = !MS || k.n_scenes <= 1;
-    const uint32_t bgoff = one ? 0u : s_goff[0];
-    const int32_t bnx    = one ? k.s0.nx : s_nx;
-    const bool tiled     = tw * th <= TILE_CAP && (one || bgoff == s_goff[1]); // across scenes: scatter directly
+    BlockBox b;
+    b.tx0          = s_box[0];
+    b.ty0          = s_box[1];
+    b.empty        = b.tx0 == INT32_MAX;
+    b.tw           = s_box[2] - b.tx0 + 3;
+    b.th           = s_box[3] - b.ty0 + 3;
+    const bool one = !MS || k.n_scenes <= 1;
+    b.tiled        = !b.empty && b.tw * b.th <= TILE_CAP && (one || s_goff[0] == s_goff[1]);
+    b.sc           = one ? k.s0 : (b.tiled ? s_sc : sc);
+    return b;
+}
+
+// Scatter of one block's particles through a shared-memory tile (particleToGrid, MPM.cu:116-126). All threads
+// of the block must call it; `valid` marks threads that carry a particle.
+template <bool MS>
+__device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s,
+                                          float2 v, float4 Q, float4* __restrict__ grid)
+{
+    __shared__ float s_x[TILE_CAP], s_y[TILE_CAP], s_m[TILE_CAP];
+    const BlockBox bb = block_box<MS>(k, sc, valid, s);
+    if (bb.empty) { return; } // no particle in this block (uniform)
+    const int32_t tx0 = bb.tx0, ty0 = bb.ty0, tw = bb.tw, th = bb.th;
+    const bool tiled     = bb.tiled; // across scenes or too wide: scatter directly
+    const uint32_t bgoff = bb.sc.goff;
+    const int32_t bnx    = bb.sc.nx;
     if (tiled) {
         for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
             s_x[t] = 0.f;
@@ -541,19 +564,51 @@ __global__ void __launch_bounds__(T_MPM)
           float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
           const int32_t* __restrict__ sid, float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
 {
+    __shared__ float2 s_v[TILE_CAP];
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (zero_grid) {
         const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (int64_t z = i; z < zero_nodes; z += stride) { zero_grid[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
     }
-    if (i >= count_of(k)) { return; }
-    const int m        = mat_of(k, MODE, mat, i);
+    if ((int64_t)blockIdx.x * blockDim.x >= count_of(k)) { return; } // uniform: the block holds no particle
+    const bool valid   = i < count_of(k);
+    const int m        = valid ? mat_of(k, MODE, mat, i) : 0;
     const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
+    const MpmScene sc  = valid ? scene_of<MS>(k, sid, i) : k.s0;
     PState ps;
-    ps.x = x[i];
-    ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
-    ps.J = keeps_j(m) ? J[i] : 1.f;
-    g2p_body<RAW>(k, scene_of<MS>(k, sid, i), m, track_f, grid, ps, status);
+    Stencil s{};
+    if (valid) {
+        ps.x = x[i];
+        ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+        ps.J = keeps_j(m) ? J[i] : 1.f;
+        s    = stencil(k, sc, ps.x, status);
+    }
+    // The block's nodes go through shared memory once, each node's velocity computed once (the particles of
+    // a cell share their 9 nodes, and sorted neighbours overlap); a box wider than the tile or spread over
+    // several scenes gathers from global memory.
+    const BlockBox bb = block_box<MS>(k, sc, valid, s);
+    if (bb.tiled) {
+        const MpmScene& bs = bb.sc;
+        for (int t = threadIdx.x; t < bb.tw * bb.th; t += blockDim.x) {
+            const int32_t gx = bb.tx0 + t % bb.tw, gy = bb.ty0 + t / bb.tw;
+            const float4 g   = __ldg(&grid[(size_t)bs.goff + (size_t)gy * (size_t)bs.nx + (size_t)gx]);
+            s_v[t]           = grid_velocity<RAW>(k, bs, g, gx, gy);
+        }
+        __syncthreads();
+    }
+    if (!valid) { return; }
+    if (bb.tiled) {
+        g2p_finish(k, sc, m, track_f, s,
+                   [&](int32_t nxi, int32_t nyj) { return s_v[(nyj - bb.ty0) * bb.tw + (nxi - bb.tx0)]; }, ps,
+                   status);
+    } else {
+        g2p_finish(k, sc, m, track_f, s,
+                   [&](int32_t nxi, int32_t nyj) {
+                       const float4 g = __ldg(&grid[(size_t)sc.goff + (size_t)nyj * (size_t)sc.nx + (size_t)nxi]);
+                       return grid_velocity<RAW>(k, sc, g, nxi, nyj);
+                   },
+                   ps, status);
+    }
     x[i] = ps.x;
     v[i] = ps.v;
     C[i] = ps.C;
