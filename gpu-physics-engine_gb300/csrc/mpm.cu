@@ -166,7 +166,8 @@ __device__ __forceinline__ void svd2(float4 F, float4& U, float2& s, float4& V)
 __device__ __forceinline__ float4 affine(const MpmK& k, int m, float4 Cp, float4 F, float J)
 {
     if (m == MODE_FLUID) {
-        const float p_hat    = k.k_bulk * (powf(1.f / J, k.gamma) - 1.f);
+        const float inv_j    = 1.f / J;
+        const float p_hat    = k.k_bulk * ((k.gamma == 1.f ? inv_j : powf(inv_j, k.gamma)) - 1.f);
         const float pressure = fminf(fmaxf(p_hat, k.p_min), k.p_max);
         const float V_p      = k.vol0 * J;
         const float coeff    = -k.dt * V_p * 4 * k.inv_dx * k.inv_dx;
@@ -519,7 +520,8 @@ __global__ void k_clear(float4* __restrict__ grid, int64_t nn)
 }
 
 template <int MODE, bool MS>
-__global__ void __launch_bounds__(T_MPM, 8) // 8 blocks per SM (32 registers, 8 x 24 KB of node tiles)
+// 8 blocks per SM (32 registers, 8 x 24 KB of node tiles); 6 with the scene lookup
+__global__ void __launch_bounds__(T_MPM, MS ? 6 : 8)
     k_p2g(const MpmK k, const float2* __restrict__ x, const float2* __restrict__ v, const float4* __restrict__ C,
           const float4* __restrict__ F, const float* __restrict__ J, const int32_t* __restrict__ mat,
           const int32_t* __restrict__ sid, float4* __restrict__ grid, uint32_t* status)
@@ -558,8 +560,8 @@ __global__ void k_grid(const MpmK k, float4* __restrict__ grid)
 }
 
 // G2P on a grid of velocities (RAW=false) or of raw momentum (RAW=true); writes the whole particle state
-template <int MODE, bool RAW, bool MS>
-__global__ void __launch_bounds__(T_MPM)
+template <int MODE, bool RAW, bool MS> // 5 blocks per SM in 48 registers (4 with the scene lookup)
+__global__ void __launch_bounds__(T_MPM, MS ? 4 : 5)
     k_g2p(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ x, float2* __restrict__ v,
           float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
           const int32_t* __restrict__ sid, float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
