@@ -153,11 +153,12 @@ __device__ __forceinline__ void for_neighbours_at(const DomDev& d, const PbfK& k
 enum { MASK_OFF = 0, MASK_BUILD = 1, MASK_USE = 2 };
 constexpr uint32_t MASK_BAD = 0x80000000u; // in word 0: this particle's masks are not usable
 
-// The full scan of a particle whose base cell is (bx, by) (cell h, R = 1), recording its masks. f(j)
-// returns whether candidate j lies within h + skin.
+// The full scan of particle i whose base cell is (bx, by) (cell h, R = 1), recording its masks. f(j)
+// returns whether candidate j lies within h + skin. The particle's own slot is not recorded: no pass takes
+// a term from the self pair inside its loop (the density's self term is added after it).
 template <class F>
 __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
-                                            int32_t by, F&& f)
+                                            int32_t by, int32_t i, F&& f)
 {
     const int32_t x0 = max(bx - 1, 0);
     const int32_t x1 = min(bx + 1, d.ncx - 1);
@@ -173,7 +174,7 @@ __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __r
         bad                = bad || (e - b > 31u);
         uint32_t wr        = 0u;
         for (uint32_t j = b; j < e; ++j) {
-            const bool near = f(j);
+            const bool near  = f(j) && j != (uint32_t)i;
             const uint32_t t = j - b;
             wr |= (near && t < 31u) ? (1u << t) : 0u;
         }
@@ -183,12 +184,12 @@ __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __r
 }
 
 // Visits the candidates of the masks m around base cell (bx, by), in scan order.
-template <class F>
+template <class L, class A>
 __device__ __forceinline__ void scan_masked(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
-                                            int32_t by, const uint4 m, F&& f)
+                                            int32_t by, const uint4 m, L&& ld, A&& ap)
 {
     const int32_t x0    = max(bx - 1, 0);
-    const uint32_t w[3] = {m.x, m.y, m.z};
+    const uint32_t w[3] = {m.x & ~MASK_BAD, m.y, m.z};
 #pragma unroll
     for (int32_t r = 0; r < 3; ++r) {
         const int32_t y = by - 1 + r;
@@ -198,17 +199,20 @@ __device__ __forceinline__ void scan_masked(const DomDev& d, const uint32_t* __r
         while (bits) {
             const uint32_t t = (uint32_t)__ffs(bits) - 1u;
             bits &= bits - 1u;
-            f(b + t);
+            ap(b + t, ld(b + t));
         }
     }
 }
 
-// The neighbour scan of particle i at (px, py) in mask mode MASK. f(j) returns whether j lies within
-// h + skin (used by MASK_BUILD only).
-template <int MASK, bool CG, class F>
-__device__ __forceinline__ void scan(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start, float px,
-                                     float py, int32_t i, F&& f)
+// The neighbour scan of particle i at (px, py) in mask mode MASK: ap(j, ld(j)) for every candidate j in
+// scan order. ap returns whether j lies within h + skin (used by MASK_BUILD only). Returns true when the
+// candidates came from the masks, which skip the particle's own slot: masks are used only while the
+// particle is in its sort cell, so the full scan would have met that slot.
+template <int MASK, bool CG, class L, class A>
+__device__ __forceinline__ bool scan_ld(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
+                                        float px, float py, int32_t i, L&& ld, A&& ap)
 {
+    auto f = [&](uint32_t j) -> bool { return ap(j, ld(j)); };
     if constexpr (MASK == MASK_OFF) {
         for_neighbours(d, k, start, px, py, f);
     } else {
@@ -216,18 +220,29 @@ __device__ __forceinline__ void scan(const DomDev& d, const PbfK& k, const uint3
         const int32_t by   = cell_coord(py, d.oy, k.inv_cell, d.ncy);
         const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
         if constexpr (MASK == MASK_BUILD) {
-            uint4 m = scan_build(d, start, bx, by, f);
+            uint4 m = scan_build(d, start, bx, by, i, f);
             if (key != __ldg(&k.keys[i])) { m.x |= MASK_BAD; } // built around another cell than the sort cell
             k.nmask[i] = m;
         } else {
             const uint4 m = ldn<CG>(&k.nmask[i]);
             if (!(m.x & MASK_BAD) && key == __ldg(&k.keys[i]) && ldn<CG>(&k.mflag[key]) == 0) {
-                scan_masked(d, start, bx, by, m, f);
+                scan_masked(d, start, bx, by, m, ld, ap);
+                return true;
             } else {
                 for_neighbours_at(d, k, start, bx, by, f);
             }
         }
     }
+    return false;
+}
+
+// scan_ld with one functor f(j) that loads and applies
+template <int MASK, bool CG, class F>
+__device__ __forceinline__ bool scan(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start, float px,
+                                     float py, int32_t i, F&& f)
+{
+    return scan_ld<MASK, CG>(d, k, start, px, py, i, [](uint32_t j) { return j; },
+                             [&](uint32_t j, uint32_t) -> bool { return f(j); });
 }
 
 // A delta p pass moved particle i (sort cell key) by at least skin / (2 iters): the particles of the 3 x 3
@@ -364,8 +379,8 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     // Branch-free body: every lane of a warp runs the same instructions for every candidate and the terms of
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
-    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float2 q  = ldn<CG>(&xs[j]);
+    const bool self_masked = scan_ld<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xs[j]); },
+                                               [&](uint32_t j, const float2 q) -> bool {
         const float rx = p.x - q.x, ry = p.y - q.y;
         const float r2  = fmaf(rx, rx, ry * ry);
         const bool self = j == (uint32_t)i;
@@ -395,6 +410,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         }
         return r2 < k.skin2;
     });
+    self_seen = self_seen || self_masked;
     if (self_seen) {
         s6 = fmaf(k.h2 * k.h2, k.h2, s6);
         if (SELFG) {
@@ -426,8 +442,9 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     }
 }
 
+// the mask pass in 32 registers, the masked passes in 40
 template <bool MULTI, bool SELFG, int ACC, int MASK>
-__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : 1) // the mask pass in 32 registers
+__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (MASK == MASK_USE ? 3 : 1))
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
              const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
              const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
@@ -455,9 +472,14 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     // closer than 1e-6 (the self pair included) have a zero direction there and are skipped here.
     const float c6w = k.c6 * k.inv_w_dq;
     float sx = 0.f, sy = 0.f;
-    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float2 q  = ldn<CG>(&xs[j]);
-        const float lj  = ldn<CG>(&lam[j]);
+    scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
+                      [&](uint32_t j) {
+                          const float2 q = ldn<CG>(&xs[j]);
+                          return make_float3(q.x, q.y, ldn<CG>(&lam[j]));
+                      },
+                      [&](uint32_t, const float3 ql) -> bool {
+        const float2 q  = make_float2(ql.x, ql.y);
+        const float lj  = ql.z;
         const float rx = p.x - q.x, ry = p.y - q.y;
         const float r2  = fmaf(rx, rx, ry * ry);
         const bool ok   = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
@@ -734,14 +756,22 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     // dv = c sum (v_j - v_i) W6 (PBF.cu:602-615) with the poly6 coefficient hoisted; the self pair adds 0.
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float dvx = 0.f, dvy = 0.f, w = 0.f;
-    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float2 q  = ldn<CG>(&xs[j]);
-        const float2 qo = ldn<CG>(&x[j]);
+    scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
+                      [&](uint32_t j) {
+                          const float2 q  = ldn<CG>(&xs[j]);
+                          const float2 qo = ldn<CG>(&x[j]);
+                          return make_float4(q.x, q.y, qo.x, qo.y);
+                      },
+                      [&](uint32_t j, const float4 qq4) -> bool {
+        const float2 q  = make_float2(qq4.x, qq4.y);
+        const float2 qo = make_float2(qq4.z, qq4.w);
         const float rx = p.x - q.x, ry = p.y - q.y;
         // explicit fused forms: the result must not depend on how the compiler contracts this body in the
         // kernel it is inlined into (separate launches and the persistent solve are compared bit for bit)
         const float r2  = fmaf(rx, rx, ry * ry);
-        const bool in   = r2 <= k.h2; // masked, branch-free (see k_lambda)
+        // masked, branch-free (see k_lambda); the self pair adds nothing in exact arithmetic (v_i - v_i) and is
+        // left out (masked scans skip the particle's own slot)
+        const bool in   = (r2 <= k.h2) && j != (uint32_t)i;
         const float dx = fmaf(q.x - qo.x, k.inv_dt, -vax), dy = fmaf(q.y - qo.y, k.inv_dt, -vay);
         const float qq  = in ? k.h2 - r2 : 0.f;
         const float p6  = qq * qq * qq;
@@ -790,9 +820,14 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
     const float wi = omega[i];
     const float aw = fabsf(wi);
     float ex = 0.f, ey = 0.f;
-    scan<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float2 q   = ldn<CG>(&xs[j]);
-        const float wj   = ldn<CG>(&omega[j]);
+    scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
+                      [&](uint32_t j) {
+                          const float2 q = ldn<CG>(&xs[j]);
+                          return make_float3(q.x, q.y, ldn<CG>(&omega[j]));
+                      },
+                      [&](uint32_t, const float3 qw) -> bool {
+        const float2 q   = make_float2(qw.x, qw.y);
+        const float wj   = qw.z;
         const float rx = p.x - q.x, ry = p.y - q.y;
         const float r2   = fmaf(rx, rx, ry * ry); // explicit fused forms, as in xsph_one
         const bool ok    = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
