@@ -544,8 +544,12 @@ def run_gpe(args, rank, ws):
 
     eng.set_state(pos, vel, stream=sh)
     # the engine's autotuner picks cell size, block size, persistent solve and mask skin for this scene (it
-    # restores the state afterwards); untimed
-    best, _ = eng.autotune(trial_steps=3, stream=sh)
+    # restores the state afterwards); untimed. --no-autotune keeps the engine's default tuning (for profiler
+    # launch lists, which would otherwise fill with the tuner's trials)
+    if args.no_autotune:
+        best = eng.tuning()
+    else:
+        best, _ = eng.autotune(trial_steps=3, stream=sh)
     cfg["tuning"] = {"cell_over_h": round(best.cell / p.h, 3), "block": best.block,
                      "persistent": bool(best.persistent), "skin": round(best.skin, 3)}
     for _ in range(args.warmup):
@@ -690,6 +694,7 @@ def main():
     ap.add_argument("--no-mpm", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
