@@ -47,9 +47,10 @@ ALG_BYTES = {  # algorithmic bytes per particle per launch (FP32 SoA, each field
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the 1M-particle step's neighbour
-# kernels from one ncu capture (profiles/pbf_k_lambda_k_delta_p_1m.md); below the algorithmic bytes because
-# the outputs stay in L2 for the next kernel
-NCU_TRAFFIC = {"lambda": 9.532416e6, "delta_p": 13.72416e6}
+# kernels from ncu captures of this workload (cold caches: ncu flushes them before each replay). lambda: the
+# mean over a step's four launches, the mask-recording pass (13.7 MB) and three masked passes (30.7 MB each,
+# which also read the 16 MB candidate-mask array and the cell starts that stay in L2 in a live step)
+NCU_TRAFFIC = {"lambda": 26.46e6, "delta_p": 35.01e6, "xsph": 39.12e6}
 
 
 def peaks():
