@@ -389,7 +389,7 @@ def batched_leg(args, stream, flush_l2):
     e.close()
     return {"workload": "pbf_batched_256_scenes", "scenes": 256, "particles": n, "unit": "particle-steps/s",
             "default": default, "tuned": tuned,
-            "tuning": {"cell_over_h": best.cell / p.h, "block": best.block, "persistent": bool(best.persistent),
+            "tuning": {"cell_over_h": best.cell / p.h, "block": best.block, "persistent": int(best.persistent),
                        "trial_ms_per_step": trial_ms, "autotune_s": tune_s}}
 
 
@@ -554,7 +554,7 @@ def run_gpe(args, rank, ws):
     else:
         best, _ = eng.autotune(trial_steps=3, stream=sh)
     cfg["tuning"] = {"cell_over_h": round(best.cell / p.h, 3), "block": best.block,
-                     "persistent": bool(best.persistent), "skin": round(best.skin, 3)}
+                     "persistent": int(best.persistent), "skin": round(best.skin, 3)}
     for _ in range(args.warmup):
         eng.step(1, stream=sh)
     torch.cuda.synchronize()

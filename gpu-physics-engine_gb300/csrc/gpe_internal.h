@@ -57,15 +57,17 @@ int32_t sm_count();
 // ----- counting sort of 32-bit keys (shared by PBF and the MPM spatial sort) -----
 // Workspace sizes for a sort of up to n_max items into n_keys buckets.
 size_t scan_blocks(uint32_t n_keys);
-// count[n_keys] -> start[n_keys+1] exclusive scan; zeroes count. bsum needs scan_blocks(n_keys) entries.
+// count[n_keys] -> start[n_keys+1] exclusive scan; zeroes count (and zero_bytes[n_keys] when given). bsum
+// needs scan_blocks(n_keys) entries.
 int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, uint32_t* start,
-                              cudaStream_t st);
+                              cudaStream_t st, uint8_t* zero_bytes = nullptr);
 // kernel launches of launch_exclusive_scan for n_keys buckets (2, or 3 beyond 2048 tiles)
 int32_t scan_launches(uint32_t n_keys);
 // bucket[start[key] + rank] = i for every (key, rank) pair. n sizes the launch; with n_dev the kernel takes
 // the live count from the device (which must not exceed n).
 int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket,
                        cudaStream_t st, const int32_t* n_dev = nullptr);
+
 
 // ----- warm-start network (mlp.cu) as the PBF engine sees it -----
 struct MlpDev;

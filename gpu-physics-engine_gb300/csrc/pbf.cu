@@ -290,15 +290,14 @@ __device__ __forceinline__ float2 predict(const PbfK& k, float2 p, float2 w)
     return make_float2(__fadd_rn(__fmaf_rn(k.dt, w.x, p.x), k.g2x), __fadd_rn(__fmaf_rn(k.dt, w.y, p.y), k.g2y));
 }
 
-// Lanes of a warp that share a cell take consecutive ranks in lane order from one atomicAdd.
+// Lanes of a warp that share a cell take consecutive ranks in lane order from one atomicAdd. All lanes of
+// the warp call it; `valid` marks those that carry particle i.
 template <bool MULTI>
-__global__ void __launch_bounds__(T_PART)
-    k_predict_hist(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                   const float2* __restrict__ x, const float2* __restrict__ v, uint2* __restrict__ keyrank,
-                   uint32_t* __restrict__ count)
+__device__ __forceinline__ void predict_hist_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                                 const int32_t* __restrict__ dom, const float2* __restrict__ x,
+                                                 const float2* __restrict__ v, uint2* __restrict__ keyrank,
+                                                 uint32_t* __restrict__ count, int32_t i, bool valid)
 {
-    const int32_t i    = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid   = i < count_of(k);
     const int32_t lane = threadIdx.x & 31;
     uint32_t key       = 0xffffffffu;
     float2 ps          = make_float2(0.f, 0.f);
@@ -320,24 +319,35 @@ __global__ void __launch_bounds__(T_PART)
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(T_PART)
+    k_predict_hist(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                   const float2* __restrict__ x, const float2* __restrict__ v, uint2* __restrict__ keyrank,
+                   uint32_t* __restrict__ count)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    predict_hist_one<MULTI>(k, doms, dom, x, v, keyrank, count, i, i < count_of(k));
+}
+
 // ----- stable placement + gather (PBF.cu:801-833) -------------------------------------------------------
 // The atomic ranks are unique but depend on warp scheduling; the stable slot of particle i is the number of
 // entries of its cell's bucket with a smaller pre-sort index.
-__global__ void __launch_bounds__(T_PART)
-    k_place(const PbfK k, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
-            const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
-            const float2* __restrict__ v_in, float2* __restrict__ x_out, float2* __restrict__ xs_out,
-            uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
-            uint32_t* __restrict__ id_out, const float* __restrict__ acc_in, float* __restrict__ prev_out,
-            float* __restrict__ lam_out)
+// CG: start and bucket were written earlier in the same (persistent) kernel, so they are read from L2
+template <bool CG = false>
+__device__ __forceinline__ void place_one(const PbfK& k, const uint2* __restrict__ keyrank,
+                                          const uint32_t* __restrict__ start, const uint32_t* __restrict__ bucket,
+                                          const float2* __restrict__ x_in, const float2* __restrict__ v_in,
+                                          float2* __restrict__ x_out, float2* __restrict__ xs_out,
+                                          uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out,
+                                          const uint32_t* __restrict__ id_in, uint32_t* __restrict__ id_out,
+                                          const float* __restrict__ acc_in, float* __restrict__ prev_out,
+                                          float* __restrict__ lam_out, int32_t i)
 {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count_of(k)) { return; }
     const uint2 kr   = keyrank[i];
-    const uint32_t s = __ldg(&start[kr.x]);
-    const uint32_t e = __ldg(&start[kr.x + 1]);
+    const uint32_t s = ldn<CG>(&start[kr.x]);
+    const uint32_t e = ldn<CG>(&start[kr.x + 1]);
     uint32_t rank    = 0;
-    for (uint32_t t = s; t < e; ++t) { rank += (__ldg(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
+    for (uint32_t t = s; t < e; ++t) { rank += (ldn<CG>(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
     const uint32_t dst = s + rank;
     const float2 p     = x_in[i];
     x_out[dst]         = p;
@@ -351,6 +361,20 @@ __global__ void __launch_bounds__(T_PART)
         prev_out[dst] = a;
         if (lam_out) { lam_out[dst] = a; }
     }
+}
+
+__global__ void __launch_bounds__(T_PART)
+    k_place(const PbfK k, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
+            const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
+            const float2* __restrict__ v_in, float2* __restrict__ x_out, float2* __restrict__ xs_out,
+            uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
+            uint32_t* __restrict__ id_out, const float* __restrict__ acc_in, float* __restrict__ prev_out,
+            float* __restrict__ lam_out)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count_of(k)) { return; }
+    place_one(k, keyrank, start, bucket, x_in, v_in, x_out, xs_out, perm, key_out, id_in, id_out, acc_in, prev_out,
+              lam_out, i);
 }
 
 // ----- lambda (PBF.cu:243-294) --------------------------------------------------------------------------
@@ -867,10 +891,21 @@ __global__ void __launch_bounds__(T_MAX)
 // as the work; here the passes run back to back in one cooperative launch, separated by a grid barrier in
 // global memory. Each thread handles the same particles in every pass (grid-stride loop), so its own
 // values are read back from where it wrote them; other particles' values are read from L2 (ldn<true>).
+// The arrival counter and the generation word sit in separate 128-byte lines, so that the blocks polling
+// the generation do not contend with the arrivals.
 struct GridSync {
     unsigned int count;
+    unsigned int pad0[31];
     unsigned int gen;
+    unsigned int pad1[31];
 };
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 constexpr uint64_t GRID_WAIT_NS = 100ull * 1000ull * 1000ull; // a barrier wait gives up after 100 ms
 
 // All threads of every block. False when this block gave up waiting (GPE_STATUS_TIMEOUT is set); the
@@ -889,7 +924,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
             atomicExch(&g->gen, target);
         } else {
             const uint64_t t0 = tc::globaltimer();
-            while (atomicAdd(&g->gen, 0u) != target) {
+            while (ld_acquire(&g->gen) != target) {
                 if (tc::globaltimer() - t0 > GRID_WAIT_NS) {
                     ok = 0;
                     atomicOr(status, GPE_STATUS_TIMEOUT);
@@ -908,18 +943,20 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
 
 // XSPH: the velocity pass runs here too; with vorticity confinement it runs as its usual launch after the
 // kernel instead (the omega-carrying pass inlined here differs from its own kernel in the last bit).
+// The Jacobi passes (and XSPH) of a step inside a persistent kernel; gen is the kernel's barrier count.
+// False when a barrier wait gave up (the caller returns).
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
-__global__ void __launch_bounds__(T_MAX)
-    k_solve_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                       const uint32_t* __restrict__ start, float2* __restrict__ xs_a, float2* __restrict__ xs_b,
-                       const float2* __restrict__ x, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
-                       float2* __restrict__ v, float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
-                       uint32_t* __restrict__ status)
+__device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __restrict__ doms,
+                                             const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
+                                             float2* __restrict__ xs_a, float2* __restrict__ xs_b,
+                                             const float2* __restrict__ x, float* __restrict__ lam,
+                                             const uint32_t* __restrict__ pair_id, float2* __restrict__ v,
+                                             float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
+                                             unsigned int& gen, uint32_t* __restrict__ status)
 {
     const int32_t n      = count_of(k);
     const int32_t stride = (int32_t)(gridDim.x * blockDim.x);
     const int32_t i0     = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
-    unsigned int gen     = 0u; // the barrier word is zeroed before every launch
     float2* cur          = xs_a;
     float2* nxt          = xs_b;
     constexpr int MU = MASKS ? MASK_USE : MASK_OFF;
@@ -933,11 +970,11 @@ __global__ void __launch_bounds__(T_MAX)
                 lambda_one<MULTI, SELFG, ACC_NONE, true, MU>(k, doms, dom, start, cur, lam, pair_id, nullptr, i);
             }
         }
-        if (!grid_barrier(gs, gen, status)) { return; }
+        if (!grid_barrier(gs, gen, status)) { return false; }
         for (int32_t i = i0; i < n; i += stride) {
             delta_p_one<MULTI, SCORR, false, true, MU>(k, doms, dom, start, cur, lam, nxt, nullptr, i);
         }
-        if (!grid_barrier(gs, gen, status)) { return; }
+        if (!grid_barrier(gs, gen, status)) { return false; }
         float2* t = cur;
         cur       = nxt;
         nxt       = t;
@@ -947,6 +984,161 @@ __global__ void __launch_bounds__(T_MAX)
             xsph_one<MULTI, false, true, MU>(k, doms, dom, start, x, cur, v, omega, status, i);
         }
     }
+    return true;
+}
+
+template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
+__global__ void __launch_bounds__(T_MAX)
+    k_solve_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                       const uint32_t* __restrict__ start, float2* __restrict__ xs_a, float2* __restrict__ xs_b,
+                       const float2* __restrict__ x, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
+                       float2* __restrict__ v, float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
+                       uint32_t* __restrict__ status)
+{
+    unsigned int gen = 0u; // the barrier word is zeroed before every launch
+    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, start, xs_a, xs_b, x, lam, pair_id, v, omega, iters,
+                                                   gs, gen, status);
+}
+
+// ----- the whole step in one persistent launch ------------------------------------------------------------
+// Predict + cell histogram, the scan of the histogram, the bucket scatter and the stable placement (the
+// same algorithm as the separate sort launches, so keys and order are the same bit for bit), then the
+// solve phases, all separated by grid barriers: a step is one cooperative launch (plus the barrier word's
+// reset). The scan works on tiles of STEP_TILE cells; each block adds up the tile totals before its tile
+// itself, as the separate scan does while the tiles are few.
+constexpr int STEP_TILE = 2048;
+
+// exclusive scan of one value per thread across the block (any multiple of 32 threads up to 1024); the
+// block total in *total
+__device__ __forceinline__ uint32_t block_excl_scan_any(uint32_t v, uint32_t* total)
+{
+    __shared__ uint32_t s_warp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) { inc += t; }
+    }
+    if (lane == 31) { s_warp[warp] = inc; }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) { w += t; }
+        }
+        if (lane < nw) { s_warp[lane] = w; }
+    }
+    __syncthreads();
+    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    *total                = s_warp[nw - 1];
+    __syncthreads();
+    return before + inc - v;
+}
+
+struct SortBufs {
+    const float2* x;         // current positions (unsorted order)
+    const float2* v;         // velocities (unsorted order)
+    uint2* keyrank;
+    uint32_t* count;         // histogram, zero on entry and on exit
+    uint32_t* bsum;          // tile totals
+    uint32_t* start;         // cell starts (ncells + 1)
+    uint32_t* bucket;
+    float2* x_sorted;        // placed x
+    float2* xs_sorted;       // placed x* (the solve's first input)
+    uint32_t* perm;
+    uint32_t* keys;
+    const uint32_t* id_in;   // ids to carry (or null)
+    uint32_t* id_out;
+    uint8_t* mflag;          // candidate-mask cell marks to clear (or null)
+    uint32_t ncells;
+};
+
+template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
+__global__ void __launch_bounds__(T_MAX)
+    k_step_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
+                      const SortBufs sb, float2* __restrict__ xs_b, float* __restrict__ lam,
+                      const uint32_t* __restrict__ pair_id, float2* __restrict__ v_out, float* __restrict__ omega,
+                      int32_t iters, GridSync* __restrict__ gs, uint32_t* __restrict__ status)
+{
+    __shared__ uint32_t s_tile[STEP_TILE];
+    const int32_t n      = count_of(k);
+    const int32_t stride = (int32_t)(gridDim.x * blockDim.x);
+    const int32_t i0     = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+    unsigned int gen     = 0u; // the barrier word is zeroed before every launch
+    const uint32_t M     = sb.ncells;
+    const uint32_t tiles = (M + STEP_TILE - 1) / STEP_TILE;
+    // predict, cell key and histogram (whole blocks iterate together: the warp ranks need full warps)
+    for (int32_t base = (int32_t)(blockIdx.x * blockDim.x); base < n; base += stride) {
+        const int32_t i = base + (int32_t)threadIdx.x;
+        predict_hist_one<MULTI>(k, doms, dom, sb.x, sb.v, sb.keyrank, sb.count, i, i < n);
+    }
+    if (MASKS) {
+        for (uint32_t c = (uint32_t)i0; c < M; c += (uint32_t)stride) { sb.mflag[c] = 0u; }
+    }
+    if (!grid_barrier(gs, gen, status)) { return; }
+    // tile totals
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        uint32_t s = 0u;
+        for (uint32_t c = t * STEP_TILE + threadIdx.x; c < min((t + 1) * STEP_TILE, M); c += blockDim.x) {
+            s += __ldcg(&sb.count[c]);
+        }
+        uint32_t total;
+        block_excl_scan_any(s, &total);
+        if (threadIdx.x == 0) { sb.bsum[t] = total; }
+    }
+    if (!grid_barrier(gs, gen, status)) { return; }
+    // exclusive scan: cell starts, and the histogram is zeroed for the next sort
+    const uint32_t per = STEP_TILE / blockDim.x; // cells per thread, consecutive
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        uint32_t part = 0u;
+        for (uint32_t b = threadIdx.x; b < t; b += blockDim.x) { part += __ldcg(&sb.bsum[b]); }
+        uint32_t prefix;
+        block_excl_scan_any(part, &prefix);
+        const uint32_t base = t * STEP_TILE;
+        for (uint32_t li = threadIdx.x; li < STEP_TILE; li += blockDim.x) {
+            const uint32_t c = base + li;
+            uint32_t cnt     = 0u;
+            if (c < M) {
+                cnt         = __ldcg(&sb.count[c]);
+                sb.count[c] = 0u;
+            }
+            s_tile[li] = cnt;
+        }
+        __syncthreads();
+        uint32_t s = 0u;
+        for (uint32_t q = 0; q < per; ++q) {
+            const uint32_t c = s_tile[threadIdx.x * per + q];
+            s_tile[threadIdx.x * per + q] = s;
+            s += c;
+        }
+        uint32_t total;
+        const uint32_t ex = block_excl_scan_any(s, &total);
+        for (uint32_t q = 0; q < per; ++q) { s_tile[threadIdx.x * per + q] += prefix + ex; }
+        __syncthreads();
+        for (uint32_t li = threadIdx.x; li < STEP_TILE; li += blockDim.x) {
+            if (base + li < M) { sb.start[base + li] = s_tile[li]; }
+        }
+        if (t == tiles - 1u && threadIdx.x == 0) { sb.start[M] = prefix + total; }
+        __syncthreads();
+    }
+    if (!grid_barrier(gs, gen, status)) { return; }
+    // bucket scatter
+    for (int32_t i = i0; i < n; i += stride) {
+        const uint2 kr                        = __ldcg(&sb.keyrank[i]);
+        sb.bucket[__ldcg(&sb.start[kr.x]) + kr.y] = (uint32_t)i;
+    }
+    if (!grid_barrier(gs, gen, status)) { return; }
+    // stable placement and gather
+    for (int32_t i = i0; i < n; i += stride) {
+        place_one<true>(k, sb.keyrank, sb.start, sb.bucket, sb.x, sb.v, sb.x_sorted, sb.xs_sorted, sb.perm, sb.keys,
+                        sb.id_in, sb.id_out, nullptr, nullptr, nullptr, i);
+    }
+    if (!grid_barrier(gs, gen, status)) { return; }
+    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, sb.start, sb.xs_sorted, xs_b, sb.x_sorted, lam,
+                                                   pair_id, v_out, omega, iters, gs, gen, status);
 }
 
 // ----- density for the density-error metric --------------------------------------------------------------
@@ -1201,6 +1393,7 @@ struct gpe_pbf {
     int32_t lam_grid  = 0;        // persistent grid of k_mlp_apply
     int32_t block     = 256;      // threads per block of the neighbour kernels (tuning)
     bool persistent   = false;    // plain steps run their passes in one persistent launch (tuning)
+    bool step_kernel  = false;    // ... and the predict + sort phases in that same launch (tuning)
     int32_t coop_grid = 0;        // blocks of the persistent launch (all resident)
     const void* coop_fn = nullptr; // the kernel coop_grid was sized for
     GridSync* gsync   = nullptr;  // its barrier word
@@ -1393,7 +1586,8 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
         }
         GPE_CHECK_LAUNCH("k_predict_hist");
     }
-    int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st);
+    // the scan also clears the candidate masks' cell marks for this step
+    int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st, masks_on(s) ? s->mflag : nullptr);
     if (rc) { return rc; }
     rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st, s->d_count);
     if (rc) { return rc; }
@@ -1414,20 +1608,24 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 }
 
 // Template dispatch tables: [multi scene][flag][accumulation mode]
-using LamFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using LamFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                        const float2*, float*, const uint32_t*, float*, int);
 template <bool M, bool S, int A>
-void lam_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+cudaError_t lam_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                 const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc, int mask)
 {
     if constexpr (A == ACC_PROJ) { // the projected-increment ablation keeps full scans
         k_lambda<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+        return cudaGetLastError();
     } else if (mask == MASK_BUILD) {
         k_lambda<M, S, A, MASK_BUILD><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+        return cudaGetLastError();
     } else if (mask == MASK_USE) {
         k_lambda<M, S, A, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+        return cudaGetLastError();
     } else {
         k_lambda<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
+        return cudaGetLastError();
     }
 }
 #define GPE_LAM3(M, S) {lam_launch<M, S, ACC_NONE>, lam_launch<M, S, ACC_SUM>, lam_launch<M, S, ACC_PROJ>}
@@ -1435,16 +1633,18 @@ const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
                              {GPE_LAM3(true, false), GPE_LAM3(true, true)}};
 #undef GPE_LAM3
 
-using DpFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using DpFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                       const float2*, const float*, float2*, float*, int);
 template <bool M, bool S, bool A>
-void dp_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+cudaError_t dp_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc, int mask)
 {
     if (mask == MASK_USE) {
         k_delta_p<M, S, A, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+        return cudaGetLastError();
     } else {
         k_delta_p<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
+        return cudaGetLastError();
     }
 }
 const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, false, true>},
@@ -1480,17 +1680,19 @@ void col_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const 
 const ColFn kCol[2][2] = {{col_launch<false, false>, col_launch<false, true>},
                           {col_launch<true, false>, col_launch<true, true>}};
 
-using XsFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
+using XsFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
                       const float2*, const float2*, float2*, float*, uint32_t*, int);
 template <bool M, bool V>
-void xs_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
+cudaError_t xs_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
                const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status,
                int mask)
 {
     if (mask == MASK_USE) {
         k_xsph<M, V, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+        return cudaGetLastError();
     } else {
         k_xsph<M, V, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+        return cudaGetLastError();
     }
 }
 const XsFn kXs[2][2] = {{xs_launch<false, false>, xs_launch<false, true>},
@@ -1512,12 +1714,12 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st, int acc)
     const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
     int mask = MASK_OFF;
     if (masks_on(s) && acc != ACC_PROJ) {
+        // the cell marks were cleared by this step's sort (marks left by a stage sequence without one only
+        // make scans full, never skip a candidate)
         mask = s->masks_valid ? MASK_USE : MASK_BUILD;
-        if (mask == MASK_BUILD) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
     }
-    kLam[multi(s) ? 1 : 0][sg][acc](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS],
-                                    s->lam, pid, s->acc, mask);
-    GPE_CHECK_LAUNCH("k_lambda");
+    GPE_TRY_CUDA(kLam[multi(s) ? 1 : 0][sg][acc](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
+                                                 s->pos[s->XS], s->lam, pid, s->acc, mask));
     if (mask == MASK_BUILD) {
         s->masks_valid    = true;
         s->dp_since_build = 0;
@@ -1540,7 +1742,6 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
         const gpe::MlpDev* md = gpe::mlp_device(s->mlp);
         // the feature pass scans every neighbour on the sorted positions: it makes the step's masks
         const int mask = masks_on(s) ? MASK_BUILD : MASK_OFF;
-        if (mask == MASK_BUILD) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
         kFeat[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
                       s->prev, pid, md, s->feat, mask);
         GPE_CHECK_LAUNCH("k_lambda_feat");
@@ -1571,9 +1772,9 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
         if (s->masks_valid && s->dp_since_build >= s->mask_passes) { s->masks_valid = false; }
         const int mask = s->masks_valid ? MASK_USE : MASK_OFF;
         s->dp_since_build += 1;
-        kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
-                                                   s->pos[s->XS], s->lam, s->pos[s->XO], s->acc, mask);
-        GPE_CHECK_LAUNCH("k_delta_p");
+        GPE_TRY_CUDA(kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](nblk(s), (unsigned)s->block, st, s->k, s->d_doms,
+                                                                s->dom, s->start, s->pos[s->XS], s->lam,
+                                                                s->pos[s->XO], s->acc, mask));
         s->launches += 1;
     }
     std::swap(s->XS, s->XO);
@@ -1584,9 +1785,9 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
-    kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->SX],
-                                s->pos[s->XS], s->vel, s->omega, s->status, s->masks_valid ? MASK_USE : MASK_OFF);
-    GPE_CHECK_LAUNCH("k_xsph");
+    GPE_TRY_CUDA(kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
+                                             s->pos[s->SX], s->pos[s->XS], s->vel, s->omega, s->status,
+                                             s->masks_valid ? MASK_USE : MASK_OFF));
     s->launches += 1;
     return GPE_OK;
 }
@@ -1653,6 +1854,14 @@ const void* solve_kernel(const gpe_pbf* s)
     return masks_on(s) ? solve_kernel_k<true>(m, sg, sc, v) : solve_kernel_k<false>(m, sg, sc, v);
 }
 
+// Blocks of a persistent launch: one per block of particles, at most as many as are resident at once (a
+// small scene's barriers then wait on few blocks)
+unsigned coop_blocks(const gpe_pbf* s)
+{
+    const int64_t need = (lsize(s) + s->block - 1) / s->block;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, s->coop_grid));
+}
+
 int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
 {
     if (lsize(s) > 0) {
@@ -1673,10 +1882,90 @@ int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
                                &s->lam, &pid, &s->vel, &s->omega, &iters, &s->gsync, &s->status};
         GPE_TRY_CUDA(cudaMemsetAsync(s->gsync, 0, sizeof(GridSync), st));
         if (masks_on(s)) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
-        GPE_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3((unsigned)s->coop_grid), dim3((unsigned)s->block), args, 0,
-                                                 st));
+        GPE_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(coop_blocks(s)), dim3((unsigned)s->block), args, 0, st));
         s->launches += 1;
     }
+    if (s->prm.iters & 1) { std::swap(s->XS, s->XO); } // the kernel's final x* is in the other buffer
+    return GPE_OK;
+}
+
+// The whole step in one cooperative launch (k_step_persistent): the host side of stage_predict_sort (buffer
+// roles, id buffers) and of stage_solve_persistent.
+template <bool M, bool S, bool C, bool V, bool K>
+const void* step_fn()
+{
+    return reinterpret_cast<const void*>(k_step_persistent<M, S, C, V, K>);
+}
+template <bool K>
+const void* step_kernel_k(bool m, bool sg, bool sc, bool v)
+{
+    const void* tab[16] = {
+        step_fn<false, false, false, false, K>(), step_fn<false, false, false, true, K>(),
+        step_fn<false, false, true, false, K>(),  step_fn<false, false, true, true, K>(),
+        step_fn<false, true, false, false, K>(),  step_fn<false, true, false, true, K>(),
+        step_fn<false, true, true, false, K>(),   step_fn<false, true, true, true, K>(),
+        step_fn<true, false, false, false, K>(),  step_fn<true, false, false, true, K>(),
+        step_fn<true, false, true, false, K>(),   step_fn<true, false, true, true, K>(),
+        step_fn<true, true, false, false, K>(),   step_fn<true, true, false, true, K>(),
+        step_fn<true, true, true, false, K>(),    step_fn<true, true, true, true, K>()};
+    return tab[(m ? 8 : 0) + (sg ? 4 : 0) + (sc ? 2 : 0) + (v ? 1 : 0)];
+}
+
+int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
+{
+    s->masks_valid = false;
+    int fr[3], c = 0;
+    for (int b = 0; b < 4; ++b) {
+        if (b != s->X) { fr[c++] = b; }
+    }
+    s->SX  = fr[0];
+    s->XS  = fr[1];
+    s->XO  = fr[2];
+    s->k.n = (int32_t)s->n;
+    const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
+    if (lsize(s) > 0) {
+        const bool m = multi(s), sg = (s->prm.flags & GPE_PBF_SELF_GRAD) != 0, sc = s->prm.scorr_k != 0.f,
+                   v = s->prm.vort_eps == 0.f; // XSPH inside the kernel
+        const void* fn = masks_on(s) ? step_kernel_k<true>(m, sg, sc, v) : step_kernel_k<false>(m, sg, sc, v);
+        if (s->coop_grid <= 0 || s->coop_fn != fn) {
+            s->coop_fn = fn;
+            int per_sm = 0;
+            GPE_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, s->block, 0));
+            s->coop_grid = std::max(1, per_sm) * gpe::sm_count();
+        }
+        SortBufs sb{};
+        sb.x         = s->pos[s->X];
+        sb.v         = s->vel;
+        sb.keyrank   = s->keyrank;
+        sb.count     = s->count;
+        sb.bsum      = s->bsum;
+        sb.start     = s->start;
+        sb.bucket    = s->bucket;
+        sb.x_sorted  = s->pos[s->SX];
+        sb.xs_sorted = s->pos[s->XS];
+        sb.perm      = s->perm;
+        sb.keys      = s->keys;
+        sb.id_in     = ids ? s->ids[s->id_cur] : nullptr;
+        sb.id_out    = ids ? s->ids[s->id_cur ^ 1] : nullptr;
+        sb.mflag     = masks_on(s) ? s->mflag : nullptr;
+        sb.ncells    = (uint32_t)s->ncells;
+        const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? sb.id_out : nullptr;
+        PbfK k              = s->k;
+        float2* xb          = s->pos[s->XO];
+        int32_t iters       = s->prm.iters;
+        void* args[]        = {&k, &s->d_doms, &s->dom, &sb, &xb, &s->lam, &pid, &s->vel, &s->omega, &iters,
+                               &s->gsync, &s->status};
+        GPE_TRY_CUDA(cudaMemsetAsync(s->gsync, 0, sizeof(GridSync), st));
+        GPE_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(coop_blocks(s)), dim3((unsigned)s->block), args, 0, st));
+        s->launches += 1;
+    } else {
+        // no particle: the cell starts are all zero (as the separate scan leaves them)
+        int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st);
+        if (rc) { return rc; }
+        s->launches += scan_launches(s->ncells);
+    }
+    if (ids) { s->id_cur ^= 1; }
+    s->have_sort = true;
     if (s->prm.iters & 1) { std::swap(s->XS, s->XO); } // the kernel's final x* is in the other buffer
     return GPE_OK;
 }
@@ -1684,6 +1973,15 @@ int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
 int32_t run_step(gpe_pbf* s, cudaStream_t st)
 {
     const bool acc = accumulating(s);
+    if (s->step_kernel && s->persistent && !acc) {
+        int32_t rc = stage_step_persistent(s, st);
+        if (rc == GPE_OK && s->prm.vort_eps != 0.f) {
+            rc = stage_xsph(s, st);
+            if (rc == GPE_OK) { rc = stage_vorticity(s, st); }
+        }
+        if (rc == GPE_OK) { rc = stage_finish(s); }
+        return rc;
+    }
     int32_t rc     = stage_predict_sort(s, st);
     if (rc == GPE_OK && s->persistent && !acc) {
         rc = stage_solve_persistent(s, st);
@@ -2227,9 +2525,9 @@ int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
     const bool vort      = s->prm.vort_eps != 0.f;
     const int32_t sorted = 3 + gpe::scan_launches(s->ncells); // predict + histogram, scan, scatter, place
     if (s->persistent && !accumulating(s)) {
-        // the passes (and XSPH without vorticity) in one cooperative launch; with vorticity XSPH and the
-        // confinement keep their launches
-        *launches = sorted + 1 + (vort ? 2 : 0);
+        // the passes (and XSPH without vorticity) in one cooperative launch, with the sort in that launch too
+        // for the whole-step kernel; with vorticity XSPH and the confinement keep their launches
+        *launches = (s->step_kernel ? 0 : sorted) + 1 + (vort ? 2 : 0);
         return GPE_OK;
     }
     // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network
@@ -2335,9 +2633,9 @@ namespace {
 int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
 {
     if (!(t.cell >= 0.f) || (t.block != 128 && t.block != 256 && t.block != 512) ||
-        (t.persistent != 0 && t.persistent != 1) || !(t.skin >= 0.f && t.skin <= 1.f)) {
+        (t.persistent < 0 || t.persistent > 2) || !(t.skin >= 0.f && t.skin <= 1.f)) {
         gpe::set_error(GPE_ERR_BAD_ARG,
-                       "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0 or 1, skin in [0, 1]");
+                       "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0, 1 or 2, skin in [0, 1]");
         return GPE_ERR_BAD_ARG;
     }
     const float c_old = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
@@ -2362,8 +2660,9 @@ int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
     }
     if (t.block != s->block) { s->coop_grid = 0; }
     s->block      = t.block;
-    s->persistent = t.persistent != 0;
-    s->skin       = t.skin;
+    s->persistent  = t.persistent != 0;
+    s->step_kernel = t.persistent == 2;
+    s->skin        = t.skin;
     bind_k(s);
     s->drop_graphs();
     return GPE_OK;
@@ -2387,7 +2686,7 @@ extern "C" int32_t gpe_pbf_get_tuning(const gpe_pbf* s, gpe_pbf_tuning* t)
     if (!s || !t) { return GPE_ERR_BAD_ARG; }
     t->cell       = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
     t->block      = s->block;
-    t->persistent = s->persistent ? 1 : 0;
+    t->persistent = s->step_kernel ? 2 : (s->persistent ? 1 : 0);
     t->skin       = s->skin;
     return GPE_OK;
 }
@@ -2469,7 +2768,7 @@ extern "C" int32_t gpe_pbf_autotune(gpe_pbf* s, int32_t trial_steps, gpe_pbf_tun
     const int32_t blocks[3] = {128, 256, 512};
     for (int ci = 0; ci < 3 && rc == GPE_OK; ++ci) {
         for (int bi = 0; bi < 3 && rc == GPE_OK; ++bi) {
-            for (int pi = 0; pi < 2 && rc == GPE_OK; ++pi) {
+            for (int pi = 0; pi < 3 && rc == GPE_OK; ++pi) {
                 const gpe_pbf_tuning cand{cells[ci], blocks[bi], pi, skins[ci]};
                 if (apply_tuning(s, cand) != GPE_OK) { continue; } // e.g. the h/2 grid does not fit
                 rc = restore();

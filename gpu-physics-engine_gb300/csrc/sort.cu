@@ -86,7 +86,7 @@ constexpr uint32_t FUSED_MAX_TILES = 2048;
 template <bool SUMS>
 __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ count, uint32_t M,
                                                       const uint32_t* __restrict__ bsum,
-                                                      uint32_t* __restrict__ start)
+                                                      uint32_t* __restrict__ start, uint8_t* __restrict__ zero8)
 {
     __shared__ uint32_t s_tile[SCAN_TILE];
     const uint32_t base = blockIdx.x * SCAN_TILE;
@@ -107,6 +107,7 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
         if (idx < M) {
             c          = count[idx];
             count[idx] = 0u;
+            if (zero8) { zero8[idx] = 0u; }
         }
         s_tile[li] = c;
     }
@@ -149,19 +150,19 @@ __global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n_host, con
 size_t scan_blocks(uint32_t n_keys) { return (n_keys + SCAN_TILE - 1) / SCAN_TILE; }
 
 int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, uint32_t* start,
-                              cudaStream_t st)
+                              cudaStream_t st, uint8_t* zero_bytes)
 {
     const uint32_t nb = (uint32_t)scan_blocks(n_keys);
     if (nb == 0) { return GPE_ERR_BAD_ARG; }
     k_scan_reduce<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
     GPE_CHECK_LAUNCH("k_scan_reduce");
     if (nb <= FUSED_MAX_TILES) {
-        k_scan_down<true><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
+        k_scan_down<true><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start, zero_bytes);
         GPE_CHECK_LAUNCH("k_scan_down");
     } else {
         k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
         GPE_CHECK_LAUNCH("k_scan_bsum");
-        k_scan_down<false><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start);
+        k_scan_down<false><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start, zero_bytes);
         GPE_CHECK_LAUNCH("k_scan_down");
     }
     return GPE_OK;

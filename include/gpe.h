@@ -316,8 +316,10 @@ typedef struct gpe_pbf_tuning {
     int32_t block;      /* threads per block of the neighbour kernels: 128, 256 or 512                 */
     int32_t persistent; /* 1: the Jacobi passes and XSPH of a plain step run in one cooperative launch
                            with grid barriers between them (for many small scenes, whose steps are
-                           otherwise launch-bound; vorticity keeps its own launches); 0: one launch
-                           per pass                                                                     */
+                           otherwise launch-bound; vorticity keeps its own launches); 2: the predict +
+                           cell sort runs inside that launch too (the sort strategy: its histogram,
+                           scan, scatter and stable placement as phases between grid barriers instead of
+                           five launches), so a plain step is one launch; 0: one launch per pass       */
     float skin;         /* candidate masks, in units of h, in [0, 1] (cell h only; default 0.1): the
                            first lambda pass of a step records per particle which candidates of its
                            3 x 3 cells lie within h + skin * h, and the later passes of the step visit
@@ -331,7 +333,7 @@ int32_t gpe_pbf_get_tuning(const gpe_pbf* pbf, gpe_pbf_tuning* tuning);
  * size it was created with). */
 int32_t gpe_pbf_set_tuning(gpe_pbf* pbf, const gpe_pbf_tuning* tuning);
 /* Times trial_steps steps of every candidate (cell h with skin 0.1 or without masks, or h/2; block 128,
- * 256 or 512; persistent or not) on
+ * 256 or 512; persistent 0, 1 or 2) on
  * the current state, which is restored after every trial and at the end, and applies the fastest;
  * *best and *ms_per_step receive it and its time (-1 when the choice came from the cache). Choices are
  * cached for the process per (scenes, particle count and mean scene aspect to the nearest power of two,

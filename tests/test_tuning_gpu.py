@@ -45,10 +45,31 @@ def _run(gpe_mod, p, pos, vel, dom, boxes, steps=3, tuning=None, vort=0.0):
 def test_persistent_and_block_sizes_are_bit_exact(gpe_mod, cuda_ok, kind, block, vort):
     p, pos, vel, dom, boxes = _scene(kind)
     ref = _run(gpe_mod, p, pos, vel, dom, boxes, vort=vort)
-    for persistent in (False, True):
+    for persistent in (0, 1, 2):  # per-pass launches, persistent solve, whole step in one launch
         got = _run(gpe_mod, p, pos, vel, dom, boxes, tuning=dict(block=block, persistent=persistent), vort=vort)
         for a, b in zip(ref, got):
             np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("kind", ["dam", "batched"])
+def test_whole_step_launch_keeps_sort_outputs(gpe_mod, cuda_ok, kind):
+    """The whole-step kernel sorts inside the launch: after a step, the sort's keys, order and cell starts
+    equal those of the separate sort launches, and a plain step (no vorticity) is one launch."""
+    p, pos, vel, dom, boxes = _scene(kind)
+    out = {}
+    for persistent in (1, 2):
+        e = gpe_mod.Pbf(p, boxes, capacity=len(pos))
+        e.set_tuning(block=256, persistent=persistent)
+        e.set_state(pos, vel, dom)
+        e.step(2)
+        out[persistent] = [e.field(f) for f in (gpe_mod.PBF_FIELD_KEY, gpe_mod.PBF_FIELD_PERM,
+                                                     gpe_mod.PBF_FIELD_CELL_START)]
+        if persistent == 2:
+            assert e.launches_per_step() == 1
+        assert e.status() == 0
+        e.close()
+    for a, b in zip(out[1], out[2]):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_half_cell_tuning_equals_half_cell_creation(gpe_mod, cuda_ok):
@@ -79,7 +100,7 @@ def test_autotune_restores_state_and_caches(gpe_mod, cuda_ok):
     e.set_state(pos, vel, dom)
     before = e.get_state()
     best, ms = e.autotune(trial_steps=3)
-    assert best.block in (128, 256, 512) and best.persistent in (0, 1) and ms > 0
+    assert best.block in (128, 256, 512) and best.persistent in (0, 1, 2) and ms > 0
     after = e.get_state()
     for a, b in zip(before, after):
         np.testing.assert_array_equal(a, b)
