@@ -102,6 +102,27 @@ __device__ __forceinline__ T ldn(const T* p)
     }
 }
 
+// Packed FP32 pairs (sm_100 and later): two IEEE round-to-nearest operations in one instruction, with the
+// same results as the scalar forms component by component.
+__device__ __forceinline__ float2 sub2(const float2 a, const float2 b)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(const float2 a, const float2 b, const float2 c)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tmov.b64 c, {%6, %7};\n\t"
+        "fma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+
 // Visits every particle index in the cells within R of the base cell of (px, py) (the reference scans the
 // 3x3 cells around clamp(floorf(x)/kCellDim), PBF.cu:252-263). Each row of cells is one contiguous range.
 template <class F>
@@ -398,15 +419,16 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     // Constants are hoisted: sx, sy = sum (h-r)^2 r/|r|, s4 = sum (h-r)^4 (= |sv|^2 / (cs m)^2 since r/|r| is a
     // unit vector), s6 = sum (h^2 - r^2)^3. The self pair (r = 0) is added after the loop: it contributes
     // h^6 to the density and, in the reference, a gradient of length cs m h^2 along pairDirection(i, i).
-    float sx = 0.f, sy = 0.f, s4 = 0.f, s6 = 0.f;
+    float2 sg = make_float2(0.f, 0.f); // (sx, sy)
+    float s4 = 0.f, s6 = 0.f;
     bool self_seen = false; // the atom's own slot can fall outside the scanned cells after large moves
     // Branch-free body: every lane of a warp runs the same instructions for every candidate and the terms of
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
     const bool self_masked = scan_ld<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xs[j]); },
                                                [&](uint32_t j, const float2 q) -> bool {
-        const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = fmaf(rx, rx, ry * ry);
+        const float2 r  = sub2(p, q);
+        const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool self = j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
@@ -417,8 +439,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         const float dif = dir ? k.h - r2 * inv : 0.f;
         const float d2  = dif * dif;
         const float w   = d2 * inv;
-        sx              = fmaf(w, rx, sx);
-        sy              = fmaf(w, ry, sy);
+        sg              = fma2(make_float2(w, w), r, sg);
         s4              = fmaf(d2, d2, s4);
         if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
             // a distinct atom at the same position: the reference's pseudo-random pair direction
@@ -428,8 +449,8 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
             } else {
                 pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
             }
-            sx = fmaf(k.h2, nx, sx);
-            sy = fmaf(k.h2, ny, sy);
+            sg.x = fmaf(k.h2, nx, sg.x);
+            sg.y = fmaf(k.h2, ny, sg.y);
             s4 = fmaf(k.h2, k.h2, s4);
         }
         return r2 < k.skin2;
@@ -441,14 +462,14 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
             float nx, ny;
             const uint32_t a = pair_id ? __ldg(&pair_id[i]) : (uint32_t)i - pbase;
             pair_direction(a, a, nx, ny);
-            sx = fmaf(k.h2, nx, sx);
-            sy = fmaf(k.h2, ny, sy);
+            sg.x = fmaf(k.h2, nx, sg.x);
+            sg.y = fmaf(k.h2, ny, sg.y);
             s4 = fmaf(k.h2, k.h2, s4);
         }
     }
     const float csm  = k.cs * k.mass;
     const float rho  = k.mass * k.c6 * s6;
-    const float gx = csm * sx, gy = csm * sy;
+    const float gx = csm * sg.x, gy = csm * sg.y;
     const float gsq  = k.inv_mass * (csm * csm) * s4;
     const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
     const float self = k.inv_mass * (gx * gx + gy * gy);
@@ -495,7 +516,7 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     // dp = omega/(m rho0) sum (m lambda_i + m lambda_j - s_corr) * (-cs (h-r)^2 r/|r|) (PBF.cu:415-437); pairs
     // closer than 1e-6 (the self pair included) have a zero direction there and are skipped here.
     const float c6w = k.c6 * k.inv_w_dq;
-    float sx = 0.f, sy = 0.f;
+    float2 sg = make_float2(0.f, 0.f); // (sx, sy)
     scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
                       [&](uint32_t j) {
                           const float2 q = ldn<CG>(&xs[j]);
@@ -504,8 +525,8 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
                       [&](uint32_t, const float3 ql) -> bool {
         const float2 q  = make_float2(ql.x, ql.y);
         const float lj  = ql.z;
-        const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = fmaf(rx, rx, ry * ry);
+        const float2 r  = sub2(p, q);
+        const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool ok   = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
         const float inv = rsqrtf(ok ? r2 : 1.f);
         float l         = fmaf(lj, k.mass, mli);
@@ -517,12 +538,11 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
         }
         const float diff = k.h - r2 * inv;
         const float w    = ok ? diff * diff * inv * l : 0.f;
-        sx               = fmaf(w, rx, sx);
-        sy               = fmaf(w, ry, sy);
+        sg               = fma2(make_float2(w, w), r, sg);
         return false;
     });
     const float s = -k.cs * k.dp_scale;
-    float ox = fmaf(s, sx, p.x), oy = fmaf(s, sy, p.y);
+    float ox = fmaf(s, sg.x, p.x), oy = fmaf(s, sg.y, p.y);
     // clamp<float>(v, lb, ub), PBF.cu:496-497
     oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
     ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
@@ -779,7 +799,8 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     const float vax = (p.x - po.x) * k.inv_dt, vay = (p.y - po.y) * k.inv_dt;
     // dv = c sum (v_j - v_i) W6 (PBF.cu:602-615) with the poly6 coefficient hoisted; the self pair adds 0.
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
-    float dvx = 0.f, dvy = 0.f, w = 0.f;
+    float2 dvs = make_float2(0.f, 0.f); // (dvx, dvy)
+    float w    = 0.f;
     scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
                       [&](uint32_t j) {
                           const float2 q  = ldn<CG>(&xs[j]);
@@ -789,18 +810,19 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
                       [&](uint32_t j, const float4 qq4) -> bool {
         const float2 q  = make_float2(qq4.x, qq4.y);
         const float2 qo = make_float2(qq4.z, qq4.w);
-        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float2 r  = sub2(p, q);
+        const float rx = r.x, ry = r.y;
         // explicit fused forms: the result must not depend on how the compiler contracts this body in the
         // kernel it is inlined into (separate launches and the persistent solve are compared bit for bit)
         const float r2  = fmaf(rx, rx, ry * ry);
         // masked, branch-free (see k_lambda); the self pair adds nothing in exact arithmetic (v_i - v_i) and is
         // left out (masked scans skip the particle's own slot)
         const bool in   = (r2 <= k.h2) && j != (uint32_t)i;
-        const float dx = fmaf(q.x - qo.x, k.inv_dt, -vax), dy = fmaf(q.y - qo.y, k.inv_dt, -vay);
+        const float2 dv = fma2(sub2(q, qo), make_float2(k.inv_dt, k.inv_dt), make_float2(-vax, -vay));
+        const float dx = dv.x, dy = dv.y;
         const float qq  = in ? k.h2 - r2 : 0.f;
         const float p6  = qq * qq * qq;
-        dvx             = fmaf(dx, p6, dvx);
-        dvy             = fmaf(dy, p6, dvy);
+        dvs             = fma2(dv, make_float2(p6, p6), dvs);
         if (VORT) {
             const bool dir   = in && (r2 > 1e-12f);
             const float inv  = rsqrtf(dir ? r2 : 1.f);
@@ -812,8 +834,8 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     });
     w *= k.cs;
     const float cx = k.xsph_c * k.c6;
-    float vx       = fmaf(dvx, cx, vax);
-    float vy       = fmaf(dvy, cx, vay);
+    float vx       = fmaf(dvs.x, cx, vax);
+    float vy       = fmaf(dvs.y, cx, vay);
     if (!VORT && (k.flags & GPE_PBF_VEL_CLAMP)) { velocity_clamp(k, vx, vy); }
     if (!(isfinite(vx) && isfinite(vy) && isfinite(p.x) && isfinite(p.y))) {
         atomicOr(status, GPE_STATUS_NONFINITE);
