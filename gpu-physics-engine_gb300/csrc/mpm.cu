@@ -261,8 +261,8 @@ template <class NodeVel>
 __device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, int m, bool track_f, const Stencil& s,
                                            NodeVel nv, PState& ps, uint32_t* status)
 {
-    float2 vel      = make_float2(0.f, 0.f);
-    float4 B        = make_float4(0.f, 0.f, 0.f, 0.f);
+    // the 2D terms as packed FP32 pairs: vel, (B.x, B.z) and (B.y, B.w)
+    float2 vel = make_float2(0.f, 0.f), bxz = make_float2(0.f, 0.f), byw = make_float2(0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
 #pragma unroll
@@ -271,15 +271,14 @@ __device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, in
             const float dpx     = ((float)i - s.fx) * k.dx;
             const float dpy     = ((float)j - s.fy) * k.dx;
             const float2 vi     = nv(s.bx + i, s.by + j);
-            vel.x += w * vi.x;
-            vel.y += w * vi.y;
-            const float wvx = w * vi.x, wvy = w * vi.y;
-            B.x += wvx * dpx;
-            B.y += wvx * dpy;
-            B.z += wvy * dpx;
-            B.w += wvy * dpy;
+            const float2 ww     = make_float2(w, w);
+            vel                 = fma2(ww, vi, vel);
+            const float2 wv     = mul2(ww, vi);
+            bxz                 = fma2(wv, make_float2(dpx, dpx), bxz);
+            byw                 = fma2(wv, make_float2(dpy, dpy), byw);
         }
     }
+    const float4 B = make_float4(bxz.x, byw.x, bxz.y, byw.y);
     float2 pos = make_float2(ps.x.x + vel.x * k.dt, ps.x.y + vel.y * k.dt);
     ps.C       = make_float4(k.apic_s * B.x, k.apic_s * B.y, k.apic_s * B.z, k.apic_s * B.w);
     // handleOOB
@@ -461,29 +460,33 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
     const uint32_t heads = __ballot_sync(0xffffffffu, head);
     const uint32_t later = lane == 31u ? 0u : (heads & (0xffffffffu << (lane + 1u)));
     const uint32_t run_end = later ? (uint32_t)(__ffs(later) - 1) : 32u; // first lane of the next run
+    // momentum terms as packed FP32 pairs: (v.x, v.y) m + (Q.x, Q.z) dpx + (Q.y, Q.w) dpy
+    const float2 qa = make_float2(Q.x, Q.z), qb = make_float2(Q.y, Q.w);
+    const float2 mm = make_float2(k.mass, k.mass);
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const int i = q % 3, j = q / 3;
-        float cx = 0.f, cy = 0.f, cm = 0.f;
+        float2 c = make_float2(0.f, 0.f);
+        float cm = 0.f;
         if (valid) {
             const float w   = s.wx[i] * s.wy[j];
             const float dpx = ((float)i - s.fx) * k.dx;
             const float dpy = ((float)j - s.fy) * k.dx;
-            cx              = w * (v.x * k.mass + (dpx * Q.x + dpy * Q.y));
-            cy              = w * (v.y * k.mass + (dpx * Q.z + dpy * Q.w));
+            const float2 a  = fma2(qb, make_float2(dpy, dpy), mul2(qa, make_float2(dpx, dpx)));
+            c               = mul2(make_float2(w, w), fma2(v, mm, a));
             cm              = w * k.mass;
         }
 #pragma unroll
         for (uint32_t d = 1u; d < 32u; d <<= 1) {
-            const float ox = __shfl_down_sync(0xffffffffu, cx, d);
-            const float oy = __shfl_down_sync(0xffffffffu, cy, d);
+            const float ox = __shfl_down_sync(0xffffffffu, c.x, d);
+            const float oy = __shfl_down_sync(0xffffffffu, c.y, d);
             const float om = __shfl_down_sync(0xffffffffu, cm, d);
             if (lane + d < run_end) {
-                cx += ox;
-                cy += oy;
+                c = add2(c, make_float2(ox, oy));
                 cm += om;
             }
         }
+        const float cx = c.x, cy = c.y;
         if (head && valid) {
             if (tiled) {
                 const int t = (s.by + j - ty0) * tw + (s.bx + i - tx0);
