@@ -164,7 +164,8 @@ def workload(iters: int = 4):
 
 def learned_leg(args, stream, flush_l2):
     """The learned warm start against the plain form on the same scene: the network is trained first (pairs
-    from 41 plain 20-iteration steps, every 20th particle, 30 epochs on the GPU; untimed), then the
+    from 41 plain 20-iteration steps, every 20th particle, 30 epochs on the GPU, best of three seeds on a
+    held-out stretch of the scene; untimed), then the
     network-warm-started 2-iteration step (and the 1-iteration one, the network's multiplier alone) and the
     plain forms are timed like the headline."""
     import torch
@@ -176,16 +177,44 @@ def learned_leg(args, stream, flush_l2):
     n = len(pos)
     e = gpe.Pbf(p20, boxes, capacity=n)
     e.set_state(pos, vel, stream=sh)
-    net = gpe.Mlp(max_pairs=2_200_000, seed=1)
+    col = gpe.Mlp(max_pairs=2_200_000, seed=1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    net.collect(e, n_steps=41, stride=20, seed=3, stream=sh)
+    col.collect(e, n_steps=41, stride=20, seed=3, stream=sh)
     t_col = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    tl, vl = net.train(gpe.make_train_params(epochs=30, batch=8192, lr=2e-3, val_fraction=0.1, seed=1), stream=sh)
-    t_tr = time.perf_counter() - t0
-    pairs = net.num_pairs
+    X, T, _ = col.pairs()
+    col.close()
+    # the state after the collection steps: a later stretch of the scene, on which the candidates are judged
+    vx, vv, _ = e.get_state()
     e.close()
+
+    def held_out_error(net):
+        p2, _, _, _, _ = workload(iters=2)
+        eng = gpe.Pbf(p2, boxes, capacity=n)
+        eng.set_state(vx, vv, stream=sh)
+        eng.set_warm_start(gpe.WARM_MLP, net)
+        eng.step(10, stream=sh)
+        dmax, _ = eng.density_error(stream=sh)
+        eng.close()
+        return dmax
+
+    # three networks from three seeds on the same pairs; the one with the smallest max density error over 10
+    # warm-started steps from the held-out state is kept (the training order varies from run to run with the
+    # atomic appends of the pair collection, and so does the worst particle's error)
+    t0 = time.perf_counter()
+    cands = []
+    for seed in (1, 2, 3):
+        cand = gpe.Mlp(max_pairs=len(T), seed=seed)
+        cand.set_pairs(X, T)
+        tl_c, vl_c = cand.train(gpe.make_train_params(epochs=30, batch=8192, lr=2e-3, val_fraction=0.1, seed=seed,
+                                                      lr_schedule=1), stream=sh)
+        cands.append((held_out_error(cand), seed, tl_c, vl_c, cand))
+    t_tr = time.perf_counter() - t0
+    cands.sort(key=lambda c: c[0])
+    held, best_seed, tl, vl, net = cands[0]
+    for c in cands[1:]:
+        c[4].close()
+    pairs = len(T)
 
     def timed(iters, warm):
         p, _, _, _, _ = workload(iters=iters)
@@ -223,8 +252,12 @@ def learned_leg(args, stream, flush_l2):
                     "speedup_vs_cheapest_plain_at_equal_error": (learned["value"] / cheapest["value"]) if cheapest
                     else None,
                     "train": {"pairs": pairs, "train_loss": tl, "val_loss": vl, "collect_s": t_col, "train_s": t_tr,
-                              "how": "pairs from 41 plain 20-iteration steps (every 20th particle), 30 epochs, "
-                                     "batch 8192, AdamW lr 2e-3, standardised MSE"}})
+                              "seed": best_seed,
+                              "held_out_max_density_error": {f"seed{c[1]}": c[0] for c in cands},
+                              "how": "pairs from 41 plain 20-iteration steps (every 20th particle); three networks "
+                                     "(seeds 1-3), 30 epochs each, batch 8192, AdamW lr 2e-3 with cosine decay, "
+                                     "standardised MSE; the one with the smallest max density error over 10 "
+                                     "warm-started steps from the state after collection is kept"}})
     return learned
 
 

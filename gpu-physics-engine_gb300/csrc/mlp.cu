@@ -695,7 +695,8 @@ int32_t gpe_mlp_train(gpe_mlp* m, const gpe_mlp_train_params* tp, float* train_l
 {
     gpe::clear_error();
     if (!m || !tp || tp->epochs < 0 || tp->batch <= 0 || !(tp->lr >= 0.f) || !(tp->val_fraction >= 0.f) ||
-        !(tp->val_fraction < 1.f) || !(tp->beta1 >= 0.f && tp->beta1 < 1.f) || !(tp->beta2 >= 0.f && tp->beta2 < 1.f)) {
+        !(tp->val_fraction < 1.f) || !(tp->beta1 >= 0.f && tp->beta1 < 1.f) || !(tp->beta2 >= 0.f && tp->beta2 < 1.f) ||
+        tp->lr_schedule < 0 || tp->lr_schedule > 1) {
         return GPE_ERR_BAD_ARG;
     }
     cudaStream_t st = as_stream(stream);
@@ -737,6 +738,8 @@ int32_t gpe_mlp_train(gpe_mlp* m, const gpe_mlp_train_params* tp, float* train_l
     uint64_t rs      = tp->seed ^ 0xBB67AE8584CAA73Bull;
     const int32_t B  = tp->batch;
     float last_epoch = 0.f;
+    const double steps_total = (double)tp->epochs * (double)((n_train + B - 1) / B);
+    int64_t step             = 0;
     for (int32_t ep = 0; ep < tp->epochs; ++ep) {
         GPE_TRY_CUDA(cudaStreamSynchronize(st)); // the pinned order buffer is rewritten below
         for (int64_t q = 0; q < n_train; ++q) { m->h_order[q] = (int32_t)q; }
@@ -754,7 +757,12 @@ int32_t gpe_mlp_train(gpe_mlp* m, const gpe_mlp_train_params* tp, float* train_l
             ++m->adam_t;
             const float bc1 = 1.f - (float)std::pow((double)tp->beta1, (double)m->adam_t);
             const float bc2 = 1.f - (float)std::pow((double)tp->beta2, (double)m->adam_t);
-            k_mlp_adamw<<<(MLP_NW + 255) / 256, 256, 0, st>>>(m->dev, m->master, m->grad, m->adam_m, m->adam_v, tp->lr,
+            const float lr = tp->lr_schedule == 1
+                                 ? (float)(0.5 * (double)tp->lr *
+                                           (1.0 + std::cos(3.141592653589793 * (double)step / steps_total)))
+                                 : tp->lr;
+            ++step;
+            k_mlp_adamw<<<(MLP_NW + 255) / 256, 256, 0, st>>>(m->dev, m->master, m->grad, m->adam_m, m->adam_v, lr,
                                                                tp->weight_decay, tp->beta1, tp->beta2, tp->adam_eps,
                                                                bc1, bc2);
             GPE_CHECK_LAUNCH("k_mlp_adamw");

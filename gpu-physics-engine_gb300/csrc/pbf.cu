@@ -555,14 +555,15 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
                                                int32_t i, uint32_t pbase, float (&f)[MLP_F])
 {
     const float2 p = xs[i];
-    float sx = 0.f, sy = 0.f, s4 = 0.f, s6 = 0.f, swl = 0.f;
+    float2 sg = make_float2(0.f, 0.f); // (sx, sy)
+    float s4 = 0.f, s6 = 0.f, swl = 0.f;
     int32_t nn     = 0;
     bool self_seen = false;
     scan<MASK, false>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
         const float2 q  = __ldg(&xs[j]);
         const float lp  = __ldg(&prev[j]);
-        const float rx = p.x - q.x, ry = p.y - q.y;
-        const float r2  = fmaf(rx, rx, ry * ry);
+        const float2 r  = sub2(p, q);
+        const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool self = j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
@@ -575,8 +576,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
         const float dif = dir ? k.h - r2 * inv : 0.f;
         const float d2  = dif * dif;
         const float w   = d2 * inv;
-        sx              = fmaf(w, rx, sx);
-        sy              = fmaf(w, ry, sy);
+        sg              = fma2(make_float2(w, w), r, sg);
         s4              = fmaf(d2, d2, s4);
         if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
             float nx, ny;
@@ -585,8 +585,8 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
             } else {
                 pair_direction((uint32_t)i - pbase, j - pbase, nx, ny);
             }
-            sx = fmaf(k.h2, nx, sx);
-            sy = fmaf(k.h2, ny, sy);
+            sg.x = fmaf(k.h2, nx, sg.x);
+            sg.y = fmaf(k.h2, ny, sg.y);
             s4 = fmaf(k.h2, k.h2, s4);
         }
         return r2 < k.skin2;
@@ -599,14 +599,14 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
             float nx, ny;
             const uint32_t a = pair_id ? __ldg(&pair_id[i]) : (uint32_t)i - pbase;
             pair_direction(a, a, nx, ny);
-            sx = fmaf(k.h2, nx, sx);
-            sy = fmaf(k.h2, ny, sy);
+            sg.x = fmaf(k.h2, nx, sg.x);
+            sg.y = fmaf(k.h2, ny, sg.y);
             s4 = fmaf(k.h2, k.h2, s4);
         }
     }
     const float csm  = k.cs * k.mass;
     const float rho  = k.mass * k.c6 * s6;
-    const float gx = csm * sx, gy = csm * sy;
+    const float gx = csm * sg.x, gy = csm * sg.y;
     const float gsq  = k.inv_mass * (csm * csm) * s4;
     const float C    = fmaxf(rho * k.inv_rho0 - 1.f, k.c_min);
     const float self = k.inv_mass * (gx * gx + gy * gy);
@@ -844,7 +844,7 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
     const float2 p = xs[i];
     const float wi = omega[i];
     const float aw = fabsf(wi);
-    float ex = 0.f, ey = 0.f;
+    float2 eg = make_float2(0.f, 0.f); // (ex, ey)
     scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
                       [&](uint32_t j) {
                           const float2 q = ldn<CG>(&xs[j]);
@@ -853,19 +853,19 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
                       [&](uint32_t, const float3 qw) -> bool {
         const float2 q   = make_float2(qw.x, qw.y);
         const float wj   = qw.z;
-        const float rx = p.x - q.x, ry = p.y - q.y;
+        const float2 r   = sub2(p, q);
+        const float rx = r.x, ry = r.y;
         const float r2   = fmaf(rx, rx, ry * ry); // explicit fused forms, as in xsph_one
         const bool ok    = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
         const float inv  = rsqrtf(ok ? r2 : 1.f);
         const float diff = k.h - r2 * inv;
         const float dwg  = ok ? (fabsf(wj) - aw) * (diff * diff * inv) : 0.f; // grad_i W = -cs (...)
-        ex               = fmaf(dwg, rx, ex);
-        ey               = fmaf(dwg, ry, ey);
+        eg               = fma2(make_float2(dwg, dwg), r, eg);
         return false;
     });
     // only the direction of eta = grad|omega| is used, so the positive factor cs drops out; the sign stays
-    ex             = -ex;
-    ey             = -ey;
+    const float ex = -eg.x;
+    const float ey = -eg.y;
     float2 vv      = v[i];
     const float e2 = fmaf(ex, ex, ey * ey);
     if (e2 > 1e-40f) {

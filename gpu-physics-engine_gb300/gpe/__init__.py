@@ -108,12 +108,13 @@ class Tuning(C.Structure):
 class TrainParams(C.Structure):
     _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("weight_decay", C.c_float),
                 ("beta1", C.c_float), ("beta2", C.c_float), ("adam_eps", C.c_float), ("val_fraction", C.c_float),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("lr_schedule", C.c_int32)]
 
 
 def make_train_params(epochs=20, batch=8192, lr=2e-3, weight_decay=1e-4, beta1=0.9, beta2=0.999, adam_eps=1e-8,
-                      val_fraction=0.1, seed=0) -> TrainParams:
-    return TrainParams(epochs, batch, lr, weight_decay, beta1, beta2, adam_eps, val_fraction, seed)
+                      val_fraction=0.1, seed=0, lr_schedule=0) -> TrainParams:
+    """lr_schedule: 0 constant, 1 cosine decay to 0 over the call's optimiser steps."""
+    return TrainParams(epochs, batch, lr, weight_decay, beta1, beta2, adam_eps, val_fraction, seed, lr_schedule)
 
 
 def make_hose(origin, velocity, nozzle_width, spacing, jitter=0.0, steps_per_call=1) -> Hose:

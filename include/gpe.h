@@ -243,6 +243,8 @@ typedef struct gpe_mlp_train_params {
     float beta1, beta2, adam_eps;
     float val_fraction;  /* the last pairs of the set are held out for the validation loss             */
     uint64_t seed;       /* shuffling of the training pairs                                            */
+    int32_t lr_schedule; /* 0: constant lr; 1: cosine decay from lr to 0 over the call's optimiser steps
+                            (Loshchilov & Hutter 2017), which settles the final weights                 */
 } gpe_mlp_train_params;
 
 #define GPE_WARM_NONE 0

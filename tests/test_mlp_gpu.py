@@ -85,6 +85,23 @@ def test_training_fits_a_smooth_target(gpe_mod, cuda_ok):
     assert np.abs(a - b).max() <= 1e-2 * np.abs(b - blob[5081]).max()
 
 
+def test_cosine_schedule_trains_and_is_checked(gpe_mod, cuda_ok):
+    """lr_schedule 1 (cosine decay to 0 over the call's optimiser steps) fits the same smooth target; other
+    schedule values are rejected."""
+    g = np.random.default_rng(12)
+    n = 40000
+    X = g.normal(0, 1, (n, 12)).astype(np.float32)
+    T = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2]).astype(np.float32)
+    m = gpe_mod.Mlp(max_pairs=n, seed=3)
+    m.set_pairs(X, T)
+    _, v0 = m.train(gpe_mod.make_train_params(epochs=0, val_fraction=0.1))
+    tl, vl = m.train(gpe_mod.make_train_params(epochs=15, batch=2048, lr=3e-3, val_fraction=0.1, seed=5,
+                                               lr_schedule=1))
+    assert np.isfinite(tl) and vl < 0.1 * v0, (v0, tl, vl)
+    with pytest.raises(gpe_mod.GpeError):
+        m.train(gpe_mod.make_train_params(epochs=1, lr_schedule=2))
+
+
 # ----- the warm-started PBF step --------------------------------------------------------------------------
 def _scene(gpe_mod, iters=4, n_side=48):
     from gpe import scenes
