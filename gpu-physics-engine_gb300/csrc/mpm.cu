@@ -393,13 +393,10 @@ __device__ __forceinline__ BlockBox block_box(const MpmK& k, const MpmScene& sc,
     // bounding box of the block's stencil bases
     int32_t mnx = valid ? s.bx : INT32_MAX, mny = valid ? s.by : INT32_MAX;
     int32_t mxx = valid ? s.bx : INT32_MIN, mxy = valid ? s.by : INT32_MIN;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-        mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-        mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-        mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-    }
+    mnx = __reduce_min_sync(0xffffffffu, mnx); // one warp reduction instruction each
+    mny = __reduce_min_sync(0xffffffffu, mny);
+    mxx = __reduce_max_sync(0xffffffffu, mxx);
+    mxy = __reduce_max_sync(0xffffffffu, mxy);
     if ((threadIdx.x & 31) == 0 && mnx != INT32_MAX) {
         atomicMin(&s_box[0], mnx);
         atomicMin(&s_box[1], mny);
