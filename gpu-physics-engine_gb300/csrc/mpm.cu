@@ -21,6 +21,7 @@
 #include <cstring>
 #include <map>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "emit.cuh"
@@ -460,6 +461,9 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
     // momentum terms as packed FP32 pairs: (v.x, v.y) m + (Q.x, Q.z) dpx + (Q.y, Q.w) dpy
     const float2 qa = make_float2(Q.x, Q.z), qb = make_float2(Q.y, Q.w);
     const float2 mm = make_float2(k.mass, k.mass);
+    // the reduction needs log2 of the warp's longest run rounds: 4 while no run is longer than 16 lanes
+    const uint32_t longest = __reduce_max_sync(0xffffffffu, head ? run_end - lane : 0u);
+    auto scatter = [&](auto rounds) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         const int i = q % 3, j = q / 3;
@@ -474,7 +478,7 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
             cm              = w * k.mass;
         }
 #pragma unroll
-        for (uint32_t d = 1u; d < 32u; d <<= 1) {
+        for (uint32_t d = 1u; d < (1u << decltype(rounds)::value); d <<= 1) {
             const float ox = __shfl_down_sync(0xffffffffu, c.x, d);
             const float oy = __shfl_down_sync(0xffffffffu, c.y, d);
             const float om = __shfl_down_sync(0xffffffffu, cm, d);
@@ -495,6 +499,12 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
                           make_float4(cx, cy, cm, 0.f));
             }
         }
+    }
+    };
+    if (longest <= 16u) {
+        scatter(std::integral_constant<int, 4>{});
+    } else {
+        scatter(std::integral_constant<int, 5>{});
     }
     if (tiled) {
         __syncthreads();
