@@ -23,6 +23,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "emit.cuh"
@@ -208,9 +209,9 @@ __device__ __forceinline__ void scan_masked(const DomDev& d, const uint32_t* __r
 // scan order. ap returns whether j lies within h + skin (used by MASK_BUILD only). Returns true when the
 // candidates came from the masks, which skip the particle's own slot: masks are used only while the
 // particle is in its sort cell, so the full scan would have met that slot.
-template <int MASK, bool CG, class L, class A>
-__device__ __forceinline__ bool scan_ld(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
-                                        float px, float py, int32_t i, L&& ld, A&& ap)
+template <int MASK, bool CG, class L, class A, class AM>
+__device__ __forceinline__ bool scan_ld2(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
+                                         float px, float py, int32_t i, L&& ld, A&& ap, AM&& apm)
 {
     auto f = [&](uint32_t j) -> bool { return ap(j, ld(j)); };
     if constexpr (MASK == MASK_OFF) {
@@ -226,7 +227,7 @@ __device__ __forceinline__ bool scan_ld(const DomDev& d, const PbfK& k, const ui
         } else {
             const uint4 m = ldn<CG>(&k.nmask[i]);
             if (!(m.x & MASK_BAD) && key == __ldg(&k.keys[i]) && ldn<CG>(&k.mflag[key]) == 0) {
-                scan_masked(d, start, bx, by, m, ld, ap);
+                scan_masked(d, start, bx, by, m, ld, apm);
                 return true;
             } else {
                 for_neighbours_at(d, k, start, bx, by, f);
@@ -234,6 +235,15 @@ __device__ __forceinline__ bool scan_ld(const DomDev& d, const PbfK& k, const ui
         }
     }
     return false;
+}
+
+// scan_ld2 with apm = ap. apm applies the candidates of masked scans, which never include the particle
+// itself, so it may leave out the self-pair test.
+template <int MASK, bool CG, class L, class A>
+__device__ __forceinline__ bool scan_ld(const DomDev& d, const PbfK& k, const uint32_t* __restrict__ start,
+                                        float px, float py, int32_t i, L&& ld, A&& ap)
+{
+    return scan_ld2<MASK, CG>(d, k, start, px, py, i, ld, ap, ap);
 }
 
 // scan_ld with one functor f(j) that loads and applies
@@ -404,11 +414,11 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     // Branch-free body: every lane of a warp runs the same instructions for every candidate and the terms of
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
-    const bool self_masked = scan_ld<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xs[j]); },
-                                               [&](uint32_t j, const float2 q) -> bool {
+    // ME: the candidate may be the particle itself (full scans); masked scans never visit it
+    auto body = [&](uint32_t j, const float2 q, auto me) -> bool {
         const float2 r  = sub2(p, q);
         const float r2  = fmaf(r.x, r.x, r.y * r.y);
-        const bool self = j == (uint32_t)i;
+        const bool self = decltype(me)::value && j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
         const bool dir  = in && (r2 > 1e-12f);
@@ -433,7 +443,11 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
             s4 = fmaf(k.h2, k.h2, s4);
         }
         return r2 < k.skin2;
-    });
+    };
+    const bool self_masked = scan_ld2<MASK, CG>(
+        d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xs[j]); },
+        [&](uint32_t j, const float2 q) -> bool { return body(j, q, std::true_type{}); },
+        [&](uint32_t j, const float2 q) -> bool { return body(j, q, std::false_type{}); });
     self_seen = self_seen || self_masked;
     if (self_seen) {
         s6 = fmaf(k.h2 * k.h2, k.h2, s6);
@@ -780,13 +794,8 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float2 dvs = make_float2(0.f, 0.f); // (dvx, dvy)
     float w    = 0.f;
-    scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
-                      [&](uint32_t j) {
-                          const float2 q  = ldn<CG>(&xs[j]);
-                          const float2 qo = ldn<CG>(&x[j]);
-                          return make_float4(q.x, q.y, qo.x, qo.y);
-                      },
-                      [&](uint32_t j, const float4 qq4) -> bool {
+    // ME: the candidate may be the particle itself (full scans); masked scans never visit it
+    auto xbody = [&](uint32_t j, const float4 qq4, auto me) -> bool {
         const float2 q  = make_float2(qq4.x, qq4.y);
         const float2 qo = make_float2(qq4.z, qq4.w);
         const float2 r  = sub2(p, q);
@@ -796,7 +805,7 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
         const float r2  = fmaf(rx, rx, ry * ry);
         // masked, branch-free (see k_lambda); the self pair adds nothing in exact arithmetic (v_i - v_i) and is
         // left out (masked scans skip the particle's own slot)
-        const bool in   = (r2 <= k.h2) && j != (uint32_t)i;
+        const bool in   = (r2 <= k.h2) && !(decltype(me)::value && j == (uint32_t)i);
         const float2 dv = fma2(sub2(q, qo), make_float2(k.inv_dt, k.inv_dt), make_float2(-vax, -vay));
         const float dx = dv.x, dy = dv.y;
         const float qq  = in ? k.h2 - r2 : 0.f;
@@ -810,7 +819,15 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
             w                = fmaf(gm, fmaf(dx, ry, -(dy * rx)), w);
         }
         return false;
-    });
+    };
+    scan_ld2<MASK, CG>(d, k, start, p.x, p.y, i,
+                       [&](uint32_t j) {
+                          const float2 q  = ldn<CG>(&xs[j]);
+                          const float2 qo = ldn<CG>(&x[j]);
+                          return make_float4(q.x, q.y, qo.x, qo.y);
+                      },
+                       [&](uint32_t j, const float4 qq4) -> bool { return xbody(j, qq4, std::true_type{}); },
+                       [&](uint32_t j, const float4 qq4) -> bool { return xbody(j, qq4, std::false_type{}); });
     w *= k.cs;
     const float cx = k.xsph_c * k.c6;
     float vx       = fmaf(dvs.x, cx, vax);
