@@ -423,6 +423,7 @@ def batched_leg(args, stream, flush_l2):
     return {"workload": "pbf_batched_256_scenes", "scenes": 256, "particles": n, "unit": "particle-steps/s",
             "default": default, "tuned": tuned,
             "tuning": {"cell_over_h": best.cell / p.h, "block": best.block, "persistent": int(best.persistent),
+                       "skin": round(best.skin, 3),
                        "trial_ms_per_step": trial_ms, "autotune_s": tune_s}}
 
 

@@ -2780,11 +2780,12 @@ extern "C" int32_t gpe_pbf_autotune(gpe_pbf* s, int32_t trial_steps, gpe_pbf_tun
     if (rc == GPE_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) {
         rc = GPE_ERR_CUDA;
     }
-    // cell h with and without candidate masks (skin 0.1 h), and h/2 (no masks: its scan has five rows)
-    const float cells[3] = {s->prm.h, s->prm.h, 0.5f * s->prm.h};
-    const float skins[3] = {0.1f, 0.f, 0.f};
+    // cell h with candidate masks (skin 0.1, 0.075 or 0.05 h) and without, and h/2 (no masks: its scan has
+    // five rows)
+    const float cells[5] = {s->prm.h, s->prm.h, s->prm.h, s->prm.h, 0.5f * s->prm.h};
+    const float skins[5] = {0.1f, 0.075f, 0.05f, 0.f, 0.f};
     const int32_t blocks[3] = {128, 256, 512};
-    for (int ci = 0; ci < 3 && rc == GPE_OK; ++ci) {
+    for (int ci = 0; ci < 5 && rc == GPE_OK; ++ci) {
         for (int bi = 0; bi < 3 && rc == GPE_OK; ++bi) {
             for (int pi = 0; pi < 3 && rc == GPE_OK; ++pi) {
                 const gpe_pbf_tuning cand{cells[ci], blocks[bi], pi, skins[ci]};
