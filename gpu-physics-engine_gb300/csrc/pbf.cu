@@ -482,7 +482,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
 
 // the mask pass in 32 registers, the masked passes in 40
 template <bool MULTI, bool SELFG, int ACC, int MASK>
-__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (MASK == MASK_USE ? 3 : 1))
+__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (MASK == MASK_USE ? 4 : 1))
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
              const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
              const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
@@ -1416,7 +1416,7 @@ struct gpe_pbf {
     const void* coop_fn = nullptr; // the kernel coop_grid was sized for
     GridSync* gsync   = nullptr;  // its barrier word
     uint16_t* feat    = nullptr;  // network operand tiles (GPE_WARM_MLP), allocated on demand
-    float skin        = 0.1f;     // candidate-mask skin in units of h (tuning; 0: full scans only)
+    float skin        = 0.075f;   // candidate-mask skin in units of h (tuning; 0: full scans only)
     uint4* nmask      = nullptr;  // candidate masks of the current step
     uint8_t* mflag    = nullptr;  // per cell: a particle of its 3 x 3 cells moved too far for the masks
     bool masks_valid  = false;    // the masks were made in this step

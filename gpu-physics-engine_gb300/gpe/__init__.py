@@ -382,7 +382,7 @@ class Pbf:
         check(lib().gpe_pbf_get_tuning(self.h, C.byref(t)), "gpe_pbf_get_tuning")
         return t
 
-    def set_tuning(self, cell: float = 0.0, block: int = 256, persistent: int = 0, skin: float = 0.1) -> None:
+    def set_tuning(self, cell: float = 0.0, block: int = 256, persistent: int = 0, skin: float = 0.075) -> None:
         """persistent: 0 one launch per pass, 1 (or True) the passes in one cooperative launch, 2 the whole step
         (predict + sort included) in one cooperative launch."""
         t = Tuning(cell, block, int(persistent), skin)

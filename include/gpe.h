@@ -322,7 +322,7 @@ typedef struct gpe_pbf_tuning {
                            cell sort runs inside that launch too (the sort strategy: its histogram,
                            scan, scatter and stable placement as phases between grid barriers instead of
                            five launches), so a plain step is one launch; 0: one launch per pass       */
-    float skin;         /* candidate masks, in units of h, in [0, 1] (cell h only; default 0.1): the
+    float skin;         /* candidate masks, in units of h, in [0, 1] (cell h only; default 0.075): the
                            first lambda pass of a step records per particle which candidates of its
                            3 x 3 cells lie within h + skin * h, and the later passes of the step visit
                            only those while no particle nearby has moved by skin * h / 2 (else that

@@ -123,7 +123,7 @@ def test_stage_by_stage_with_extra_passes_equals_full_scans(gpe_mod, cuda_ok):
 def test_skin_is_a_tuning_value(gpe_mod, cuda_ok):
     p, pos, vel, dom, boxes = _scene("calm")
     e = gpe_mod.Pbf(p, boxes, capacity=len(pos))
-    assert abs(e.tuning().skin - 0.1) < 1e-7  # on by default
+    assert abs(e.tuning().skin - 0.075) < 1e-7  # on by default
     e.set_tuning(skin=0.25)
     assert abs(e.tuning().skin - 0.25) < 1e-7
     with pytest.raises(gpe_mod.GpeError):
