@@ -50,7 +50,12 @@ ALG_BYTES = {  # algorithmic bytes per particle per launch (FP32 SoA, each field
 # kernels from ncu captures of this workload (cold caches: ncu flushes them before each replay). lambda: the
 # mean over a step's four launches, the mask-recording pass (13.7 MB) and three masked passes (30.7 MB each,
 # which also read the 16 MB candidate-mask array and the cell starts that stay in L2 in a live step)
-NCU_TRAFFIC = {"lambda": 26.46e6, "delta_p": 35.01e6, "xsph": 39.12e6}
+NCU_TRAFFIC = {"lambda": 26.48e6, "delta_p": 34.97e6, "xsph": 39.12e6}
+# warp instructions per launch (smsp__inst_executed.sum) of the same kernels from the same kind of capture;
+# lambda and delta p: the mean over a step's four launches (the mask-recording lambda executes 48.3 M, a
+# masked one 24.9 M). The neighbour kernels are bound by instruction issue, and the issue roofline is
+# these instructions over the live launch time against 4 schedulers x SMs x the sampled SM clock.
+NCU_WARP_INST = {"lambda": 30.75e6, "delta_p": 21.59e6, "xsph": 18.60e6}
 
 
 def peaks():
@@ -650,6 +655,15 @@ def run_gpe(args, rank, ws):
                 "stage_gbs": {k: ALG_BYTES[k] * n / (statistics.mean(v) / 1e3) / 1e9 for k, v in stage_ms.items()},
                 "stage_frac": {k: ALG_BYTES[k] * n / (statistics.mean(v) / 1e3) / 1e9 / peak
                                for k, v in stage_ms.items()}}
+    if dom_name in NCU_WARP_INST:
+        sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        issue_peak = 4.0 * sms * sm_mhz * 1e6
+        issue = NCU_WARP_INST[dom_name] / (per_launch_ms / 1e3)
+        roofline["issue"] = {"warp_inst_per_launch": NCU_WARP_INST[dom_name], "achieved": issue, "peak": issue_peak,
+                             "unit": "warp-instructions/s", "frac": issue / issue_peak,
+                             "how": "ncu smsp__inst_executed.sum per launch over the live launch time; peak = 4 "
+                                    "schedulers x SMs x the median SM clock sampled in the timed region"}
 
     # ---- end to end through the C ABI with host buffers ----
     e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
