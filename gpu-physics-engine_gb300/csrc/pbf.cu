@@ -2198,7 +2198,7 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
                           int32_t mem, void* stream)
 {
     gpe::clear_error();
-    if (!s || n < 0 || (n > 0 && !pos) || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+    if (!s || n < 0 || (n > 0 && !pos) || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE && mem != GPE_MEM_PINNED)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_state: bad arguments");
         return GPE_ERR_BAD_ARG;
     }
@@ -2211,7 +2211,7 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_state: domain_id is required with several scenes");
         return GPE_ERR_BAD_ARG;
     }
-    if (s->nd > 1 && mem == GPE_MEM_HOST) {
+    if (s->nd > 1 && mem != GPE_MEM_DEVICE) { // host or pinned: checked here
         for (int64_t i = 0; i < n; ++i) {
             if (domain_id[i] < 0 || domain_id[i] >= s->nd || (i > 0 && domain_id[i] < domain_id[i - 1])) {
                 gpe::set_error(GPE_ERR_BAD_ARG,
@@ -2270,7 +2270,7 @@ int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id
     cudaStream_t st = as_stream(stream);
     int32_t rc      = sync_count(s, st);
     if (rc) { return rc; }
-    if (n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) {
+    if (n != s->n || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE && mem != GPE_MEM_PINNED)) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_state: n must equal the particle count");
         return GPE_ERR_BAD_ARG;
     }
@@ -2281,7 +2281,7 @@ int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id
         if (domain_id) {
             if (s->nd > 1) {
                 GPE_TRY_CUDA(cudaMemcpyAsync(domain_id, s->dom, sizeof(int32_t) * (size_t)n, kind_out(mem), st));
-            } else if (mem == GPE_MEM_HOST) {
+            } else if (mem != GPE_MEM_DEVICE) {
                 GPE_TRY_CUDA(cudaStreamSynchronize(st));
                 std::memset(domain_id, 0, sizeof(int32_t) * (size_t)n);
             } else {

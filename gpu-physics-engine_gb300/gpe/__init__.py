@@ -16,7 +16,7 @@ LIB_PATH = PKG_DIR / "libgpe.so"
 # ----- constants (include/gpe.h) -------------------------------------------------------------------------
 OK, ERR_CUDA, ERR_DEVICE, ERR_NOT_READY, ERR_BAD_ARG, ERR_ALREADY, ERR_CAPACITY, ERR_NONFINITE, ERR_TIMEOUT = (
     0, -1, -2, -3, -4, -5, -6, -7, -8)
-MEM_HOST, MEM_DEVICE = 0, 1
+MEM_HOST, MEM_DEVICE, MEM_PINNED = 0, 1, 2
 STATUS_NONFINITE, STATUS_CAPACITY, STATUS_CELL_OVERFLOW, STATUS_TIMEOUT = 1, 2, 4, 8
 
 PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS, PBF_DYNAMIC_COUNT = 0x1, 0x2, 0x4, 0x8, 0x10
@@ -245,9 +245,13 @@ def _ptr(a) -> int | None:
     raise TypeError(f"cannot take the address of {type(a)}")
 
 
-def _mem(a) -> int:
+def _mem(a, pinned_ok: bool = False) -> int:
+    """Memory kind of a buffer: numpy arrays and CPU tensors are host memory (page-locked CPU tensors are
+    MEM_PINNED where the entry point takes it: the copy is then asynchronous), CUDA tensors and ints device."""
     if isinstance(a, np.ndarray):
         return MEM_HOST
+    if hasattr(a, "is_cuda") and not a.is_cuda:
+        return MEM_PINNED if (pinned_ok and a.is_pinned()) else MEM_HOST
     return MEM_DEVICE
 
 
@@ -300,7 +304,7 @@ class Pbf:
             n = pos.shape[0]
         else:
             n = pos.shape[0]
-        check(lib().gpe_pbf_set_state(self.h, _ptr(pos), _ptr(vel), _ptr(domain), n, _mem(pos), stream),
+        check(lib().gpe_pbf_set_state(self.h, _ptr(pos), _ptr(vel), _ptr(domain), n, _mem(pos, True), stream),
               "gpe_pbf_set_state")
         self._keep = (pos, vel, domain)
 
@@ -317,15 +321,16 @@ class Pbf:
         return v.value
 
     def get_state(self, pos=None, vel=None, stream=None):
-        """Returns (pos, vel, scene id) in the current sorted order. With caller buffers (host arrays or
-        device pointers) only pos/vel are written and the scene id is not read back."""
+        """Returns (pos, vel, scene id) in the current sorted order. With caller buffers (host arrays, CUDA
+        tensors or device pointers) only pos/vel are written and the scene id is not read back; into
+        page-locked CPU tensors the copy is asynchronous (synchronize the stream before reading them)."""
         n = self.n
         dom = None
         if pos is None:
             pos = np.empty((n, 2), np.float32)
             vel = np.empty((n, 2), np.float32)
             dom = np.empty(n, np.int32)
-        check(lib().gpe_pbf_get_state(self.h, _ptr(pos), _ptr(vel), _ptr(dom), n, _mem(pos), stream),
+        check(lib().gpe_pbf_get_state(self.h, _ptr(pos), _ptr(vel), _ptr(dom), n, _mem(pos, True), stream),
               "gpe_pbf_get_state")
         return pos, vel, dom
 

@@ -39,6 +39,11 @@ extern "C" {
 /* memory kinds for state transfer */
 #define GPE_MEM_HOST 0
 #define GPE_MEM_DEVICE 1
+/* page-locked host memory (cudaHostAlloc / cudaHostRegister), for gpe_pbf_set_state and gpe_pbf_get_state
+ * only: the copy is enqueued on the stream and the call returns without waiting, so copies of one engine
+ * can overlap another engine's work; the caller synchronizes the stream before reusing (set) or reading
+ * (get) the buffer. */
+#define GPE_MEM_PINNED 2
 
 /* device status word bits (gpe_*_status) */
 #define GPE_STATUS_NONFINITE 0x1u

@@ -261,3 +261,35 @@ def test_edge_cases(gpe_mod, cuda_ok):
     e.step(1)
     assert e.status() & gpe_mod.STATUS_NONFINITE
     e.close()
+
+
+def test_pinned_transfers_overlap_two_engines(gpe_mod, cuda_ok):
+    """GPE_MEM_PINNED: set_state / get_state with page-locked host buffers enqueue their copies and return;
+    two engines stepping on two streams with such copies give the same states as synchronous host copies."""
+    torch = pytest.importorskip("torch")
+    from gpe import scenes
+
+    p = scenes.dam_params(iters=3)
+    p.dt = 1.0 / 480.0
+    pos, vel, boxes = scenes.dam_break(n_side=48)
+    vel = np.random.default_rng(8).normal(0, 0.2, pos.shape).astype(np.float32)
+    ref = gpe_mod.Pbf(p, boxes, capacity=len(pos))
+    ref.set_state(pos, vel)
+    ref.step(2)
+    want = ref.get_state()
+    ref.close()
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_vel = torch.from_numpy(vel).pin_memory()
+    engines = [gpe_mod.Pbf(p, boxes, capacity=len(pos)) for _ in range(2)]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    outs = [(torch.empty((len(pos), 2)).pin_memory(), torch.empty((len(pos), 2)).pin_memory()) for _ in range(2)]
+    for e, s, (op, ov) in zip(engines, streams, outs):
+        e.set_state(h_pos, h_vel, stream=s.cuda_stream)
+        e.step(2, stream=s.cuda_stream)
+        e.get_state(op, ov, stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    for e, (op, ov) in zip(engines, outs):
+        np.testing.assert_array_equal(op.numpy(), want[0])
+        np.testing.assert_array_equal(ov.numpy(), want[1])
+        assert e.status() == 0
+        e.close()
