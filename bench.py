@@ -336,12 +336,72 @@ def reference_cuda_leg(args, stream, flush_l2):
     e.set_state(pos, vel, stream=sh)
     eng_s = timed(lambda: e.step(1, stream=sh))
     e.close()
-    return {"workload": "pbf_1m_reference_units_k2", "particles": n, "unit": "particle-steps/s",
-            "reference_value": n * args.steps / ref_s, "engine_value": n * args.steps / eng_s,
-            "speedup": ref_s / eng_s, "reference_ms_per_step": 1e3 * ref_s / args.steps,
-            "engine_ms_per_step": 1e3 * eng_s / args.steps, "reference_atoms_after": atoms_kept,
-            "how": "reference PBF.cu kernels (sm_103a cubin, 32x32 chunks) in a CUDA graph vs gpe_pbf_step, "
-                   "same scene and constants, L2 flushed before each timed substep"}
+    out = {"workload": "pbf_1m_reference_units_k2", "particles": n, "unit": "particle-steps/s",
+           "reference_value": n * args.steps / ref_s, "engine_value": n * args.steps / eng_s,
+           "speedup": ref_s / eng_s, "reference_ms_per_step": 1e3 * ref_s / args.steps,
+           "engine_ms_per_step": 1e3 * eng_s / args.steps, "reference_atoms_after": atoms_kept,
+           "how": "reference PBF.cu kernels (sm_103a cubin, 32x32 chunks) in a CUDA graph vs gpe_pbf_step, "
+                  "same scene and constants, L2 flushed before each timed substep"}
+    out["mpm"] = reference_mpm_leg(timed, stream, args.steps)
+    return out
+
+
+def reference_mpm_leg(timed, stream, steps):
+    """The reference's own MLS-MPM kernels (MPM.cu built for sm_103a, a 64 x 64-chunk world, 1028^2 grid
+    nodes) against the engine on the same 4,194,304-particle block with the reference's constants (J-EOS
+    fluid, dt = 0.032 / 20): the reference substep (clear, P2G, grid, G2P) captured into a CUDA graph at the
+    reference's launch shape (36 blocks of 256 threads) and at a full-GPU shape (8 blocks per SM), and
+    gpe_mpm_step."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+
+    cubin = ROOT / "oracle" / "_ref" / "MPM_ref_64x64_n4194304.cubin"
+    if not cubin.exists():
+        return {"unavailable": "reference kernels not built (oracle/build_ref.py needs the reference sources)"}
+    from oracle import refrun
+
+    side = 2048
+    g = np.random.default_rng(31)
+    ix, iy = np.meshgrid(np.arange(side), np.arange(side), indexing="xy")
+    x = np.stack([100.0 + ix.ravel() * 0.6, 100.0 + iy.ravel() * 0.6], 1) + g.uniform(-0.05, 0.05, (side * side, 2))
+    n = len(x)
+    v = g.uniform(-5.0, 5.0, (n, 2))
+    Cm = np.zeros((n, 4))
+    F = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), (n, 1))
+    J = np.ones(n)
+    x, v, Cm, F, J = (a.astype(np.float32) for a in (x, v, Cm, F, J))
+    sh = stream.cuda_stream
+    ref = refrun.RefMPM(n, (64, 64), cubin=cubin)
+    res = {}
+    for label, blocks in (("reference_launch_shape", 36), ("full_gpu", 8 * torch.cuda.get_device_properties(0)
+                                                             .multi_processor_count)):
+        ref.seed(x, v, Cm, F, J)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            ref.substep(0, stream=sh, blocks=blocks)
+
+        def replay():
+            with torch.cuda.stream(stream):
+                graph.replay()
+
+        res[label] = 1e3 * timed(replay) / steps
+        del graph
+    del ref
+    p = scenes.reference_mpm_params()
+    p.nx = p.ny = 64 * 32 // 2 + 4
+    p.clamp_hi[0] = p.clamp_hi[1] = 64.0 * 32.0
+    e = gpe.Mpm(p, capacity=n)
+    e.set_state(x, v, Cm, F, J, stream=sh)
+    eng_s = timed(lambda: e.step(1, stream=sh))
+    st = e.status()
+    e.close()
+    return {"workload": "mpm_4m_reference_units", "particles": n, "grid_nodes": p.nx * p.ny,
+            "reference_ms_per_step_36_blocks": res["reference_launch_shape"],
+            "reference_ms_per_step_full_gpu": res["full_gpu"], "engine_ms_per_step": 1e3 * eng_s / steps,
+            "speedup_vs_reference_launch_shape": res["reference_launch_shape"] / (1e3 * eng_s / steps),
+            "speedup_vs_reference_full_gpu": res["full_gpu"] / (1e3 * eng_s / steps), "engine_status": st}
 
 
 def render_leg(args, stream, flush_l2, eng):

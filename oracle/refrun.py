@@ -268,9 +268,11 @@ class RefMPM:
         self.num_points.copy_(torch.tensor([n, n], dtype=torch.int32))
         self.n = n
 
-    def substep(self, s=0, stream=0):
-        """P2G -> grid -> G2P on grid[s & 1] after clearing it (MPM.cu:357-368)."""
-        BD, GD = (256,), (36,)
+    def substep(self, s=0, stream=0, blocks=36):
+        """P2G -> grid -> G2P on grid[s & 1] after clearing it (MPM.cu:357-368). blocks: the reference launches
+        36 blocks of 256 threads (constants.h); its kernels loop over particles and nodes with a grid stride,
+        so any block count gives the same result."""
+        BD, GD = (256,), (int(blocks),)
         g = self.grid[s & 1]
         launch(self.k["resetGridKernel"], GD, BD, [_p(g)], stream)
         launch(self.k["P2GKernel"], GD, BD,
