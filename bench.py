@@ -12,8 +12,8 @@ learned: the network-warm-started 2-iteration step against the plain forms on th
 
 value: particle-steps/s through the graph-launched step (gpe_pbf_step), CUDA events on the launch stream.
 e2e:   the same metric through the C ABI with host buffers: per step set_state from pinned host memory,
-       one step, get_state back to pinned host memory, all inside the timed region; two engines on two
-       streams alternate steps so that one step's copies overlap the other's compute (the one-engine,
+       one step, get_state back to pinned host memory, all inside the timed region; three engines on three
+       streams take turns so that one step's copies overlap the others' compute (the one-engine,
        synchronous figure is reported beside it).
 roofline: the dominant kernel (largest share of step time) timed per launch in a stage-by-stage pass with
        CUDA events, against its algorithmic bytes per particle.
@@ -58,6 +58,10 @@ NCU_TRAFFIC = {"lambda": 26.48e6, "delta_p": 34.97e6, "xsph": 39.12e6}
 # masked one 24.9 M). The neighbour kernels are bound by instruction issue, and the issue roofline is
 # these instructions over the live launch time against 4 schedulers x SMs x the sampled SM clock.
 NCU_WARP_INST = {"lambda": 30.75e6, "delta_p": 21.59e6, "xsph": 18.60e6}
+
+# engines whose steps alternate in the end-to-end measurement (measured: 1 engine 0.608 ms per step with
+# synchronous copies, 2 engines 0.411, 3 engines 0.386, against 0.295 ms of device time)
+E2E_ENGINES = 3
 
 
 def peaks():
@@ -744,42 +748,50 @@ def run_gpe(args, rank, ws):
     e2e_seq = {"value": replica_value(n * args.steps, e2e_s, ws), "unit": "particle-steps/s",
                "how": "one engine on one stream: copy in, step, copy out (synchronous), per step"}
 
-    # two engines on two streams, step s on engine s % 2 with page-locked buffers (GPE_MEM_PINNED: the copies
-    # are asynchronous), so one step's copies overlap the other engine's step; every step still copies its
-    # 16 MB in and its 16 MB out inside the timed region. No L2 flush: the two engines' working sets
-    # (about 130 MB each) alternate through the 129 MB L2.
-    eng2 = gpe.Pbf(p, boxes, capacity=n)
-    eng2.set_tuning(cell=best.cell, block=best.block, persistent=int(best.persistent), skin=best.skin)
-    engines = [eng, eng2]
-    streams = [stream, torch.cuda.Stream()]
-    outs = [(o_pos, o_vel), (torch.empty((n, 2), dtype=torch.float32).pin_memory(),
-                             torch.empty((n, 2), dtype=torch.float32).pin_memory())]
-    for q in range(2):  # untimed: capture each engine's step graph
+    # E2E_ENGINES engines on as many streams, step s on engine s % E2E_ENGINES with page-locked buffers
+    # (GPE_MEM_PINNED: the copies are asynchronous), so one step's copies overlap the other engines' steps;
+    # every step still copies its 16 MB in and its 16 MB out inside the timed region. No L2 flush: the
+    # engines' working sets (about 130 MB each) alternate through the 129 MB L2.
+    engines = [eng] + [gpe.Pbf(p, boxes, capacity=n) for _ in range(E2E_ENGINES - 1)]
+    for e_ in engines[1:]:
+        e_.set_tuning(cell=best.cell, block=best.block, persistent=int(best.persistent), skin=best.skin)
+    streams = [stream] + [torch.cuda.Stream() for _ in range(E2E_ENGINES - 1)]
+    outs = [(o_pos, o_vel)] + [(torch.empty((n, 2), dtype=torch.float32).pin_memory(),
+                                torch.empty((n, 2), dtype=torch.float32).pin_memory())
+                               for _ in range(E2E_ENGINES - 1)]
+    for q in range(E2E_ENGINES):  # untimed: capture each engine's step graph
         engines[q].set_state(h_pos, h_vel, stream=streams[q].cuda_stream)
         engines[q].step(1, stream=streams[q].cuda_stream)
         engines[q].get_state(outs[q][0], outs[q][1], stream=streams[q].cuda_stream)
     torch.cuda.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
-    t0, t1, j1 = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-                  torch.cuda.Event())
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0.record(streams[0])
-    streams[1].wait_event(t0)
+    for st_ in streams[1:]:
+        st_.wait_event(t0)
+    h0 = time.perf_counter()
     for s_ in range(args.steps):
-        q, st_ = s_ % 2, streams[s_ % 2].cuda_stream
+        q = s_ % E2E_ENGINES
+        st_ = streams[q].cuda_stream
         engines[q].set_state(h_pos, h_vel, stream=st_)
         engines[q].step(1, stream=st_)
         engines[q].get_state(outs[q][0], outs[q][1], stream=st_)
-    j1.record(streams[1])
-    streams[0].wait_event(j1)
+    host_s = time.perf_counter() - h0  # the host's time to issue the steps (the calls return before the GPU)
+    for st_ in streams[1:]:
+        j_ = torch.cuda.Event()
+        j_.record(st_)
+        streams[0].wait_event(j_)
     t1.record(streams[0])
     torch.cuda.synchronize()
     e2e_pipe_s = t0.elapsed_time(t1) / 1e3
-    eng2.close()
+    for e_ in engines[1:]:
+        e_.close()
     e2e = {"value": replica_value(n * args.steps, e2e_pipe_s, ws), "unit": "particle-steps/s",
            "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
-           "how": "two engines on two streams, page-locked host buffers, asynchronous copies: one step's copies "
-                  "overlap the other engine's step", "sequential": e2e_seq}
+           "how": f"{E2E_ENGINES} engines on {E2E_ENGINES} streams, page-locked host buffers, asynchronous "
+                  "copies: one step's copies overlap the other engines' steps",
+           "host_issue_ms_per_step": 1e3 * host_s / args.steps, "sequential": e2e_seq}
 
     if rank != 0:
         return
