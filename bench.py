@@ -347,6 +347,80 @@ def reference_cuda_leg(args, stream, flush_l2):
            "how": "reference PBF.cu kernels (sm_103a cubin, 32x32 chunks) in a CUDA graph vs gpe_pbf_step, "
                   "same scene and constants, L2 flushed before each timed substep"}
     out["mpm"] = reference_mpm_leg(timed, stream, args.steps)
+    out["small"] = reference_small_leg(timed, stream, args.steps)
+    return out
+
+
+def reference_small_leg(timed, stream, steps):
+    """The small configurations against the reference's own kernels, reference units and constants: PBF with
+    16,384 atoms (a 128 x 128 block) in the reference's 12 x 6-chunk world (K = 2), and MLS-MPM with 65,536
+    J-EOS fluid particles (a 256 x 256 block) on its 196 x 100-node grid, the reference's MPM substep at its
+    36-block launch shape and at 8 blocks per SM. Per substep, graph-launched, L2 flushed before each."""
+    import torch
+
+    import gpe
+    from gpe import scenes
+    from oracle import refrun
+
+    pbf_cubin = ROOT / "oracle" / "_ref" / "PBF_ref_12x6_m320.cubin"
+    mpm_cubin = ROOT / "oracle" / "_ref" / "MPM_ref_12x6_n400000.cubin"
+    if not (pbf_cubin.exists() and mpm_cubin.exists()):
+        return {"unavailable": "reference kernels not built (oracle/build_ref.py needs the reference sources)"}
+    sh = stream.cuda_stream
+    out = {}
+
+    def graph_of(fn):
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            fn()
+
+        def replay():
+            with torch.cuda.stream(stream):
+                graph.replay()
+
+        return graph, replay
+
+    g = np.random.default_rng(5)
+    ix, iy = np.meshgrid(np.arange(128), np.arange(128), indexing="xy")
+    x = np.stack([20.0 + ix.ravel(), 20.0 + iy.ravel()], 1) + g.uniform(-0.05, 0.05, (128 * 128, 2))
+    v = g.uniform(-0.02, 0.02, x.shape)
+    x, v = x.astype(np.float32), v.astype(np.float32)
+    p = scenes.reference_pbf_params(iters=2)
+    ref = refrun.RefPBF((12, 6), 320, cubin=pbf_cubin)
+    ref.seed(x, v, float(p.gravity[1]))
+    graph, replay = graph_of(lambda: ref.substep(iters=p.iters, full=True, stream=sh))
+    ref_ms = 1e3 * timed(replay) / steps
+    del graph, ref
+    e = gpe.Pbf(p, [scenes.REFERENCE_BOX], capacity=len(x))
+    e.set_state(x, v, stream=sh)
+    eng_ms = 1e3 * timed(lambda: e.step(1, stream=sh)) / steps
+    e.close()
+    out["pbf_16k"] = {"reference_ms_per_step": ref_ms, "engine_ms_per_step": eng_ms, "speedup": ref_ms / eng_ms}
+
+    ix, iy = np.meshgrid(np.arange(256), np.arange(256), indexing="xy")
+    xm = np.stack([40.0 + ix.ravel() * 0.7, 5.0 + iy.ravel() * 0.7], 1) + g.uniform(-0.05, 0.05, (65536, 2))
+    vm = g.uniform(-5.0, 5.0, xm.shape)
+    Cm = np.zeros((65536, 4))
+    F = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), (65536, 1))
+    J = np.ones(65536)
+    xm, vm, Cm, F, J = (a.astype(np.float32) for a in (xm, vm, Cm, F, J))
+    ref = refrun.RefMPM(400 * 1000, (12, 6), cubin=mpm_cubin)
+    res = {}
+    for label, blocks in (("36_blocks", 36), ("full_gpu", 8 * torch.cuda.get_device_properties(0)
+                                                  .multi_processor_count)):
+        ref.seed(xm, vm, Cm, F, J)
+        graph, replay = graph_of(lambda: ref.substep(0, stream=sh, blocks=blocks))
+        res[label] = 1e3 * timed(replay) / steps
+        del graph
+    del ref
+    em = gpe.Mpm(scenes.reference_mpm_params(), capacity=65536)
+    em.set_state(xm, vm, Cm, F, J, stream=sh)
+    eng_ms = 1e3 * timed(lambda: em.step(1, stream=sh)) / steps
+    em.close()
+    out["mpm_65k"] = {"reference_ms_per_step_36_blocks": res["36_blocks"],
+                      "reference_ms_per_step_full_gpu": res["full_gpu"], "engine_ms_per_step": eng_ms,
+                      "speedup_vs_reference_launch_shape": res["36_blocks"] / eng_ms,
+                      "speedup_vs_reference_full_gpu": res["full_gpu"] / eng_ms}
     return out
 
 
