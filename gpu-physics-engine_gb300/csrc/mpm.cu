@@ -570,8 +570,10 @@ __global__ void k_grid(const MpmK k, float4* __restrict__ grid)
 }
 
 // G2P on a grid of velocities (RAW=false) or of raw momentum (RAW=true); writes the whole particle state
-template <int MODE, bool RAW, bool MS> // 5 blocks per SM in 48 registers (4 with the scene lookup)
-__global__ void __launch_bounds__(T_MPM, MS ? 4 : 5)
+// 5 blocks per SM in 48 registers (the scene-lookup variants spill a little there, and still run faster
+// than at 4 blocks)
+template <int MODE, bool RAW, bool MS>
+__global__ void __launch_bounds__(T_MPM, 5)
     k_g2p(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ x, float2* __restrict__ v,
           float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
           const int32_t* __restrict__ sid, float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
