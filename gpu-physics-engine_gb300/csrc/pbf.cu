@@ -963,6 +963,14 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
 // kernel instead (the omega-carrying pass inlined here differs from its own kernel in the last bit).
 // The Jacobi passes (and XSPH) of a step inside a persistent kernel; gen is the kernel's barrier count.
 // False when a barrier wait gave up (the caller returns).
+// one block at a barrier whose counter says another block has already arrived: the generation never
+// advances, so the wait runs out (gpe_selftest_barrier_timeout)
+__global__ void k_barrier_selftest(GridSync* g, uint32_t* status)
+{
+    unsigned int gen = 0u;
+    grid_barrier(g, gen, status);
+}
+
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
 __device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __restrict__ doms,
                                              const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
@@ -2551,6 +2559,32 @@ int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
     // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network
     const int32_t first = (warm && s->warm == GPE_WARM_PREV) ? -1 : ((warm && s->warm == GPE_WARM_MLP) ? 1 : 0);
     *launches = sorted + 2 * s->prm.iters + 1 + (vort ? 1 : 0) + first;
+    return GPE_OK;
+}
+
+int32_t gpe_selftest_barrier_timeout(uint32_t* status)
+{
+    gpe::clear_error();
+    if (!status) { return GPE_ERR_BAD_ARG; }
+    void* buf = nullptr;
+    GPE_TRY_CUDA(cudaMalloc(&buf, sizeof(GridSync) + sizeof(uint32_t)));
+    GridSync* g    = static_cast<GridSync*>(buf);
+    uint32_t* word = reinterpret_cast<uint32_t*>(g + 1);
+    GridSync init{};
+    init.count = 1u; // "another block has arrived": this one is not the last, so it waits for the generation
+    cudaError_t e = cudaMemcpy(g, &init, sizeof(GridSync), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) { e = cudaMemset(word, 0, sizeof(uint32_t)); }
+    if (e == cudaSuccess) {
+        k_barrier_selftest<<<1, 32>>>(g, word);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) { e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) { e = cudaMemcpy(status, word, sizeof(uint32_t), cudaMemcpyDeviceToHost); }
+    cudaFree(buf);
+    if (e != cudaSuccess) {
+        gpe::set_cuda_error(e, "gpe_selftest_barrier_timeout");
+        return GPE_ERR_CUDA;
+    }
     return GPE_OK;
 }
 

@@ -173,6 +173,7 @@ def lib() -> C.CDLL:
             "gpe_pbf_density_error": [vp, f32p, f32p, vp],
             "gpe_pbf_status": [vp, C.POINTER(C.c_uint32), vp],
             "gpe_pbf_launches_per_step": [vp, C.POINTER(i32)],
+            "gpe_selftest_barrier_timeout": [C.POINTER(C.c_uint32)],
             "gpe_mpm_create": [C.POINTER(MpmParams), i64, C.POINTER(vp)],
             "gpe_mpm_create_scenes": [C.POINTER(MpmParams), C.POINTER(MpmScene), i32, i64, C.POINTER(vp)],
             "gpe_mpm_set_scene_ids": [vp, vp, i64, i32, vp],
@@ -402,6 +403,13 @@ class Pbf:
         check(lib().gpe_pbf_set_warm_start(self.h, int(mode), None if mlp is None else mlp.h),
               "gpe_pbf_set_warm_start")
         self._mlp = mlp  # keep the network alive while the engine uses it
+
+
+def selftest_barrier_timeout() -> int:
+    """Runs gpe_selftest_barrier_timeout and returns the device status word it recorded."""
+    v = C.c_uint32()
+    check(lib().gpe_selftest_barrier_timeout(C.byref(v)), "gpe_selftest_barrier_timeout")
+    return int(v.value)
 
 
 # ----- MPM ----------------------------------------------------------------------------------------------

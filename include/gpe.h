@@ -160,6 +160,11 @@ int32_t gpe_pbf_density_error(gpe_pbf* pbf, float* max_err, float* mean_err, voi
 int32_t gpe_pbf_status(gpe_pbf* pbf, uint32_t* status, void* stream);
 /* Number of kernel launches the last gpe_pbf_step issued per step. */
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* pbf, int32_t* launches);
+/* Self-test of the bounded device waits (no counterpart in the reference): one block arrives at the
+ * persistent kernels' grid barrier set up to expect one more arrival than it will get, so its wait gives up
+ * after the barrier's time limit (100 ms), records GPE_STATUS_TIMEOUT and the kernel returns; *status
+ * receives the device status word. The device stays usable afterwards. */
+int32_t gpe_selftest_barrier_timeout(uint32_t* status);
 
 /* A "hose pipe" source (hosePipe, PBF.cu:1033-1065 and MPM.cu:439-473): rows of particles on a square lattice
  * behind a nozzle, moving with `velocity`, optionally jittered by a Gaussian of standard deviation `jitter`

@@ -293,3 +293,16 @@ def test_pinned_transfers_overlap_two_engines(gpe_mod, cuda_ok):
         np.testing.assert_array_equal(ov.numpy(), want[1])
         assert e.status() == 0
         e.close()
+
+
+def test_bounded_barrier_wait_times_out(gpe_mod, cuda_ok):
+    """The persistent kernels' grid barrier gives up after its time limit instead of hanging: a block that
+    waits for an arrival that never comes records GPE_STATUS_TIMEOUT and returns, and the device stays
+    usable."""
+    status = gpe_mod.selftest_barrier_timeout()
+    assert status & gpe_mod.STATUS_TIMEOUT
+    p, pos, vel, dom, boxes = _scene("dam")
+    e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+    e.step(1)
+    assert e.status() == 0
+    e.close()
