@@ -83,12 +83,15 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_bsum(uint32_t* __restrict__ bsu
 // exclusive scan of the totals.
 constexpr uint32_t FUSED_MAX_TILES = 2048;
 
-template <bool SUMS>
+// VEC: M is a multiple of 4 and the arrays are 16-byte aligned (zero8: 4-byte), so each thread moves four
+// cells per access; the per-thread runs of SCAN_I cells are then read from shared memory as 16-byte words
+// (2-way bank conflicts instead of 8-way).
+template <bool SUMS, bool VEC>
 __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ count, uint32_t M,
                                                       const uint32_t* __restrict__ bsum,
                                                       uint32_t* __restrict__ start, uint8_t* __restrict__ zero8)
 {
-    __shared__ uint32_t s_tile[SCAN_TILE];
+    __shared__ __align__(16) uint32_t s_tile[SCAN_TILE];
     const uint32_t base = blockIdx.x * SCAN_TILE;
     uint32_t prefix;
     if (SUMS) {
@@ -99,38 +102,74 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
         prefix = bsum[blockIdx.x];
     }
     // coalesced load, and zero the histogram for the next sort
+    if constexpr (VEC) {
 #pragma unroll
-    for (int t = 0; t < SCAN_I; ++t) {
-        const uint32_t li  = t * SCAN_T + threadIdx.x;
-        const uint32_t idx = base + li;
-        uint32_t c         = 0;
-        if (idx < M) {
-            c          = count[idx];
-            count[idx] = 0u;
-            if (zero8) { zero8[idx] = 0u; }
+        for (int t = 0; t < SCAN_I / 4; ++t) {
+            const uint32_t li  = 4u * (t * SCAN_T + threadIdx.x);
+            const uint32_t idx = base + li;
+            uint4 c            = make_uint4(0u, 0u, 0u, 0u);
+            if (idx < M) {
+                c                                        = *reinterpret_cast<const uint4*>(count + idx);
+                *reinterpret_cast<uint4*>(count + idx)   = make_uint4(0u, 0u, 0u, 0u);
+                if (zero8) { *reinterpret_cast<uint32_t*>(zero8 + idx) = 0u; }
+            }
+            *reinterpret_cast<uint4*>(s_tile + li) = c;
         }
-        s_tile[li] = c;
+    } else {
+#pragma unroll
+        for (int t = 0; t < SCAN_I; ++t) {
+            const uint32_t li  = t * SCAN_T + threadIdx.x;
+            const uint32_t idx = base + li;
+            uint32_t c         = 0;
+            if (idx < M) {
+                c          = count[idx];
+                count[idx] = 0u;
+                if (zero8) { zero8[idx] = 0u; }
+            }
+            s_tile[li] = c;
+        }
     }
     __syncthreads();
     // each thread owns SCAN_I consecutive cells
-    uint32_t loc[SCAN_I];
+    uint32_t v[SCAN_I];
+#pragma unroll
+    for (int q = 0; q < SCAN_I / 4; ++q) {
+        const uint4 w    = *reinterpret_cast<const uint4*>(s_tile + threadIdx.x * SCAN_I + 4 * q);
+        v[4 * q + 0]     = w.x;
+        v[4 * q + 1]     = w.y;
+        v[4 * q + 2]     = w.z;
+        v[4 * q + 3]     = w.w;
+    }
     uint32_t s = 0;
 #pragma unroll
     for (int t = 0; t < SCAN_I; ++t) {
-        loc[t] = s;
-        s += s_tile[threadIdx.x * SCAN_I + t];
+        const uint32_t c = v[t];
+        v[t]             = s;
+        s += c;
     }
     uint32_t total;
     const uint32_t ex  = block_excl_scan(s, &total);
     const uint32_t off = prefix + ex;
 #pragma unroll
-    for (int t = 0; t < SCAN_I; ++t) { s_tile[threadIdx.x * SCAN_I + t] = off + loc[t]; }
+    for (int q = 0; q < SCAN_I / 4; ++q) {
+        *reinterpret_cast<uint4*>(s_tile + threadIdx.x * SCAN_I + 4 * q) =
+            make_uint4(off + v[4 * q], off + v[4 * q + 1], off + v[4 * q + 2], off + v[4 * q + 3]);
+    }
     __syncthreads();
+    if constexpr (VEC) {
 #pragma unroll
-    for (int t = 0; t < SCAN_I; ++t) {
-        const uint32_t li  = t * SCAN_T + threadIdx.x;
-        const uint32_t idx = base + li;
-        if (idx < M) { start[idx] = s_tile[li]; }
+        for (int t = 0; t < SCAN_I / 4; ++t) {
+            const uint32_t li  = 4u * (t * SCAN_T + threadIdx.x);
+            const uint32_t idx = base + li;
+            if (idx < M) { *reinterpret_cast<uint4*>(start + idx) = *reinterpret_cast<const uint4*>(s_tile + li); }
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < SCAN_I; ++t) {
+            const uint32_t li  = t * SCAN_T + threadIdx.x;
+            const uint32_t idx = base + li;
+            if (idx < M) { start[idx] = s_tile[li]; }
+        }
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = prefix + total; }
 }
@@ -156,15 +195,17 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
     if (nb == 0) { return GPE_ERR_BAD_ARG; }
     k_scan_reduce<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
     GPE_CHECK_LAUNCH("k_scan_reduce");
-    if (nb <= FUSED_MAX_TILES) {
-        k_scan_down<true><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start, zero_bytes);
-        GPE_CHECK_LAUNCH("k_scan_down");
-    } else {
+    const bool vec = n_keys % 4 == 0 && reinterpret_cast<uintptr_t>(count) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(start) % 16 == 0 && reinterpret_cast<uintptr_t>(zero_bytes) % 4 == 0;
+    const bool sums = nb <= FUSED_MAX_TILES;
+    if (!sums) {
         k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
         GPE_CHECK_LAUNCH("k_scan_bsum");
-        k_scan_down<false><<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start, zero_bytes);
-        GPE_CHECK_LAUNCH("k_scan_down");
     }
+    auto down = sums ? (vec ? k_scan_down<true, true> : k_scan_down<true, false>)
+                     : (vec ? k_scan_down<false, true> : k_scan_down<false, false>);
+    down<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum, start, zero_bytes);
+    GPE_CHECK_LAUNCH("k_scan_down");
     return GPE_OK;
 }
 
