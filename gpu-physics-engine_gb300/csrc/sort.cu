@@ -49,15 +49,28 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total)
     return before + inc - v;
 }
 
+// VEC: M is a multiple of 4 and count is 16-byte aligned (four cells per load)
+template <bool VEC>
 __global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t* __restrict__ count, uint32_t M,
                                                         uint32_t* __restrict__ bsum)
 {
     const uint32_t base = blockIdx.x * SCAN_TILE;
     uint32_t s          = 0;
+    if constexpr (VEC) {
 #pragma unroll
-    for (int t = 0; t < SCAN_I; ++t) {
-        const uint32_t idx = base + t * SCAN_T + threadIdx.x;
-        if (idx < M) { s += count[idx]; }
+        for (int t = 0; t < SCAN_I / 4; ++t) {
+            const uint32_t idx = base + 4u * (t * SCAN_T + threadIdx.x);
+            if (idx < M) {
+                const uint4 c = *reinterpret_cast<const uint4*>(count + idx);
+                s += (c.x + c.y) + (c.z + c.w);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < SCAN_I; ++t) {
+            const uint32_t idx = base + t * SCAN_T + threadIdx.x;
+            if (idx < M) { s += count[idx]; }
+        }
     }
     uint32_t total;
     block_excl_scan(s, &total);
@@ -193,10 +206,10 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
 {
     const uint32_t nb = (uint32_t)scan_blocks(n_keys);
     if (nb == 0) { return GPE_ERR_BAD_ARG; }
-    k_scan_reduce<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
-    GPE_CHECK_LAUNCH("k_scan_reduce");
     const bool vec = n_keys % 4 == 0 && reinterpret_cast<uintptr_t>(count) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(start) % 16 == 0 && reinterpret_cast<uintptr_t>(zero_bytes) % 4 == 0;
+    (vec ? k_scan_reduce<true> : k_scan_reduce<false>)<<<nb, SCAN_T, 0, st>>>(count, n_keys, bsum);
+    GPE_CHECK_LAUNCH("k_scan_reduce");
     const bool sums = nb <= FUSED_MAX_TILES;
     if (!sums) {
         k_scan_bsum<<<1, SCAN_T, 0, st>>>(bsum, nb);
