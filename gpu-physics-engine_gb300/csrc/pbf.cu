@@ -257,14 +257,16 @@ __device__ __forceinline__ bool scan(const DomDev& d, const PbfK& k, const uint3
 
 // A delta p pass moved particle i (sort cell key) by at least skin / (2 iters): the particles of the 3 x 3
 // cells around its sort cell scan in full for the rest of the step.
-__device__ __noinline__ void mark_mover(const DomDev& d, const PbfK& k, uint32_t key)
+// Arguments by value: the call keeps them in registers (a reference would put the scene's DomDev on the stack).
+__device__ __noinline__ void mark_mover(uint8_t* __restrict__ mflag, uint32_t coff, int32_t ncx, int32_t ncy,
+                                        uint32_t key)
 {
-    const uint32_t local = key - d.coff;
-    const int32_t cy     = (int32_t)(local / (uint32_t)d.ncx);
-    const int32_t cx     = (int32_t)(local - (uint32_t)cy * (uint32_t)d.ncx);
-    for (int32_t y = max(cy - 1, 0); y <= min(cy + 1, d.ncy - 1); ++y) {
-        for (int32_t x = max(cx - 1, 0); x <= min(cx + 1, d.ncx - 1); ++x) {
-            k.mflag[d.coff + (uint32_t)y * (uint32_t)d.ncx + (uint32_t)x] = 1u;
+    const uint32_t local = key - coff;
+    const int32_t cy     = (int32_t)(local / (uint32_t)ncx);
+    const int32_t cx     = (int32_t)(local - (uint32_t)cy * (uint32_t)ncx);
+    for (int32_t y = max(cy - 1, 0); y <= min(cy + 1, ncy - 1); ++y) {
+        for (int32_t x = max(cx - 1, 0); x <= min(cx + 1, ncx - 1); ++x) {
+            mflag[coff + (uint32_t)y * (uint32_t)ncx + (uint32_t)x] = 1u;
         }
     }
 }
@@ -542,7 +544,7 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     xs_out[i] = make_float2(ox, oy);
     if constexpr (MASK == MASK_USE) {
         const float mx = ox - p.x, my = oy - p.y;
-        if (!(fmaf(mx, mx, my * my) < k.move2)) { mark_mover(d, k, __ldg(&k.keys[i])); }
+        if (!(fmaf(mx, mx, my * my) < k.move2)) { mark_mover(k.mflag, d.coff, d.ncx, d.ncy, __ldg(&k.keys[i])); }
     }
 }
 
