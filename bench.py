@@ -157,15 +157,10 @@ def replica_value(units_per_rank: float, local_s: float, ws: int) -> float:
     return ws * units_per_rank / allmax(local_s, ws)
 
 
-DT = 1.0 / 2000.0  # the step at which the plain 4-iteration solver is stable on this 10 m deep scene
-
-
 def workload(iters: int = 4):
     from gpe import scenes
 
-    p = scenes.dam_params(iters=iters)
-    p.dt = DT
-    pos, vel, boxes = scenes.million()
+    p, pos, vel, boxes = scenes.million_workload(iters=iters)
     cfg = {"workload": "pbf_1m_plain_k4", "particles": int(len(pos)), "iters": iters, "h": 0.02,
            "dt": "1/2000", "domain": "20.48 x 20.48 (4 x 4 chunks of 5.12)", "cells": 1024 * 1024,
            "scene": "960x1024 lattice block + 256x256 splash |v|~U(0,2), seed 2",
@@ -537,9 +532,7 @@ def batched_leg(args, stream, flush_l2):
     from gpe import scenes
 
     sh = stream.cuda_stream
-    p = scenes.dam_params(iters=4)
-    p.dt = 1.0 / 480.0
-    pos, vel, dom, boxes = scenes.batched_scenes(n_scenes=256, seed=3, lo=2048, hi=65536)
+    p, pos, vel, dom, boxes = scenes.batched_workload(iters=4)
     n = len(pos)
     e = gpe.Pbf(p, boxes, capacity=n)
 
@@ -579,7 +572,8 @@ def mpm_leg(args, stream, flush_l2):
            material and plastic state read and written once) plus 64 per grid node;
     library: the same grid and particle count with a fifth each of water, jelly, snow, Neo-Hookean and
            Drucker-Prager sand (two discs each);
-    elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid, dt = 1e-4 (launch-bound);
+    elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid (32 per cell), dt = 1e-4,
+           re-sorted every 16 steps (launch-bound);
     batched_32: 32 mixed scenes of 64k-512k particles in one engine (batched_mpm)."""
     import torch
 
@@ -621,8 +615,7 @@ def mpm_leg(args, stream, flush_l2):
     lib = (gpe.MPM_MAT_FLUID, gpe.MPM_MAT_COROTATED, gpe.MPM_MAT_SNOW, gpe.MPM_MAT_NEOHOOKEAN, gpe.MPM_MAT_SAND)
     pos, mat = scenes.mixed_discs(n, seed=5, discs_per_material=2, materials=lib)
     out["library_4m"] = timed(p, pos, np.zeros_like(pos), mat, 136.0 * n + 64.0 * p.nx * p.ny)
-    pe = scenes.elastic_params()
-    pos, vel = scenes.two_squares()
+    pe, pos, vel = scenes.elastic_workload()
     out["elastic_65k"] = timed(pe, pos, vel, None, 120.0 * len(pos) + 64.0 * pe.nx * pe.ny)
     out["batched_32"] = batched_mpm(timed, sh, stream)
     return out

@@ -9,6 +9,7 @@
 #include <curand_kernel.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include "gpe_internal.h"
@@ -25,12 +26,18 @@ struct HoseK {
     unsigned long long seed;
 };
 
-// Host: the hose's geometry; returns the requested count (width x rows), 0 for a degenerate hose.
+// Host: the hose's geometry; returns the requested count (width x rows), or -1 when width, rows or their
+// product is not finite or exceeds INT32_MAX (the emitters then refuse the call with GPE_ERR_CAPACITY).
 inline int32_t make_hose(const gpe_hose& h, float dt, uint64_t seed, HoseK* k)
 {
     const float speed = std::sqrt(h.velocity[0] * h.velocity[0] + h.velocity[1] * h.velocity[1]);
-    const int32_t w   = std::max(1, (int32_t)std::lround(h.nozzle_width / h.spacing));
-    const int32_t r   = std::max(1, (int32_t)std::lround(speed * dt * (float)h.steps_per_call / h.spacing));
+    // width and rows as the reference rounds them (lround of the float quotients), range-checked in double
+    const double wq = std::nearbyint((double)(h.nozzle_width / h.spacing));
+    const double rq = std::nearbyint((double)(speed * dt * (float)h.steps_per_call / h.spacing));
+    if (!(wq < 2147483647.0) || !(rq < 2147483647.0)) { return -1; } // also refuses NaN
+    const int64_t w = std::max<int64_t>(1, (int64_t)std::lround(h.nozzle_width / h.spacing));
+    const int64_t r = std::max<int64_t>(1, (int64_t)std::lround(speed * dt * (float)h.steps_per_call / h.spacing));
+    if (w * r > (int64_t)INT32_MAX) { return -1; }
     const float inv   = speed > 1e-6f ? 1.f / speed : 0.f;
     k->ox             = h.origin[0];
     k->oy             = h.origin[1];
@@ -42,8 +49,8 @@ inline int32_t make_hose(const gpe_hose& h, float dt, uint64_t seed, HoseK* k)
     k->vy             = h.velocity[1];
     k->spacing        = h.spacing;
     k->jitter         = h.jitter;
-    k->width          = w;
-    k->count          = w * r;
+    k->width          = (int32_t)w;
+    k->count          = (int32_t)(w * r);
     k->seed           = (unsigned long long)seed;
     return k->count;
 }

@@ -428,9 +428,10 @@ __device__ __forceinline__ BlockBox block_box(const MpmK& k, const MpmScene& sc,
 
 // Scatter of one block's particles through a shared-memory tile (particleToGrid, MPM.cu:116-126). All threads
 // of the block must call it; `valid` marks threads that carry a particle.
+// wide_warps counts the warps that need the 5-round reduction (a run longer than 16 lanes).
 template <bool MS>
 __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s,
-                                          float2 v, float4 Q, float4* __restrict__ grid)
+                                          float2 v, float4 Q, float4* __restrict__ grid, uint32_t* wide_warps)
 {
     __shared__ float s_x[TILE_CAP], s_y[TILE_CAP], s_m[TILE_CAP];
     const BlockBox bb = block_box<MS>(k, sc, valid, s);
@@ -504,6 +505,7 @@ __device__ __forceinline__ void p2g_block(const MpmK& k, const MpmScene& sc, boo
     if (longest <= 16u) {
         scatter(std::integral_constant<int, 4>{});
     } else {
+        if (lane == 0u) { atomicAdd(wide_warps, 1u); } // warp-uniform branch: one count per warp
         scatter(std::integral_constant<int, 5>{});
     }
     if (tiled) {
@@ -550,7 +552,7 @@ __global__ void __launch_bounds__(T_MPM, MS ? 6 : 8)
         vv              = v[i];
         s               = stencil(k, sc, x[i], status);
     }
-    p2g_block<MS>(k, sc, valid, s, vv, Q, grid);
+    p2g_block<MS>(k, sc, valid, s, vv, Q, grid, status + 2);
 }
 
 // gridKernel, MPM.cu:131-177 (in place)
@@ -1411,6 +1413,16 @@ int32_t gpe_mpm_get_grid(gpe_mpm* s, float* dst, int64_t n_nodes, int32_t mem, v
     return GPE_OK;
 }
 
+int32_t gpe_mpm_p2g_wide_warps(gpe_mpm* s, uint32_t* count, void* stream)
+{
+    if (!s || !count) { return GPE_ERR_BAD_ARG; }
+    cudaStream_t st = as_stream(stream);
+    GPE_TRY_CUDA(cudaMemcpyAsync(count, s->status + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GPE_TRY_CUDA(cudaMemsetAsync(s->status + 2, 0, sizeof(uint32_t), st));
+    GPE_TRY_CUDA(cudaStreamSynchronize(st));
+    return GPE_OK;
+}
+
 int32_t gpe_mpm_status(gpe_mpm* s, uint32_t* status, void* stream)
 {
     if (!s || !status) { return GPE_ERR_BAD_ARG; }
@@ -1443,6 +1455,11 @@ int32_t gpe_mpm_emit(gpe_mpm* s, const gpe_hose* hose, uint64_t seed, int32_t* r
     HoseK h{};
     const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
     if (requested) { *requested = cnt; }
+    if (cnt < 0 || (int64_t)cnt > s->cap) {
+        gpe::set_error(GPE_ERR_CAPACITY, "emit: the hose asks for %s particles, more than the engine's capacity "
+                       "of %lld", cnt < 0 ? "2^31 or more" : std::to_string(cnt).c_str(), (long long)s->cap);
+        return GPE_ERR_CAPACITY;
+    }
     cudaStream_t st = as_stream(stream);
     if (cnt > 0) {
         const int c = s->cur;

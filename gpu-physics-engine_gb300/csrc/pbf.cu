@@ -926,11 +926,17 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p)
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-constexpr uint64_t GRID_WAIT_NS = 100ull * 1000ull * 1000ull; // a barrier wait gives up after 100 ms
+// A barrier wait of the persistent solve gives up after 2 s. A barrier normally completes within a few
+// microseconds; the limit is far above that so that a context the GPU merely time-slices with other
+// processes (which can stall it for tens of milliseconds) is not reported as hung. The self-test of the
+// bounded wait uses 100 ms.
+constexpr uint64_t GRID_WAIT_NS     = 2000ull * 1000ull * 1000ull;
+constexpr uint64_t GRID_SELFTEST_NS = 100ull * 1000ull * 1000ull;
 
 // All threads of every block. False when this block gave up waiting (GPE_STATUS_TIMEOUT is set); the
 // caller then returns, and the other blocks time out at their next barrier in turn.
-__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uint32_t* status)
+__device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uint32_t* status,
+                                             uint64_t limit_ns = GRID_WAIT_NS)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -945,7 +951,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
         } else {
             const uint64_t t0 = tc::globaltimer();
             while (ld_acquire(&g->gen) != target) {
-                if (tc::globaltimer() - t0 > GRID_WAIT_NS) {
+                if (tc::globaltimer() - t0 > limit_ns) {
                     ok = 0;
                     atomicOr(status, GPE_STATUS_TIMEOUT);
                     break;
@@ -970,7 +976,7 @@ __device__ __forceinline__ bool grid_barrier(GridSync* g, unsigned int& gen, uin
 __global__ void k_barrier_selftest(GridSync* g, uint32_t* status)
 {
     unsigned int gen = 0u;
-    grid_barrier(g, gen, status);
+    grid_barrier(g, gen, status, GRID_SELFTEST_NS);
 }
 
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
@@ -1529,10 +1535,14 @@ void bind_k(gpe_pbf* s)
 // masks in this engine's configuration: cell h (3 x 3 scan), a skin, at least one iteration
 bool masks_on(const gpe_pbf* s) { return s->skin > 0.f && s->k.R == 1 && s->prm.iters > 0; }
 
+// Cells along one edge of a scene; -1 when extent / cell is not finite or reaches 2^30 (the cast to int32
+// would be undefined there). Scene extents are checked to be > 0 before this is called.
+constexpr double MAX_CELLS_ALONG = (double)(1u << 30);
 int32_t cells_along(float extent, float cell)
 {
-    const int32_t c = (int32_t)std::ceil(extent / cell);
-    return c < 1 ? 1 : c;
+    const double c = std::ceil((double)(extent / cell));
+    if (!(c < MAX_CELLS_ALONG)) { return -1; } // also false for NaN
+    return c < 1.0 ? 1 : (int32_t)c;
 }
 
 void build_domains(gpe_pbf* s)
@@ -1575,12 +1585,17 @@ int32_t sync_count(gpe_pbf* s, cudaStream_t st)
     return GPE_OK;
 }
 
+// Total sort cells of the scenes; CELLS_INVALID when a scene's extent / cell is not finite or too large.
+constexpr uint64_t CELLS_INVALID = ~(uint64_t)0;
 uint64_t count_cells(const gpe_pbf_params* p, const gpe_domain* doms, int32_t nd)
 {
     const float cell = p->cell > 0.f ? p->cell : p->h;
     uint64_t off     = 0;
     for (int32_t d = 0; d < nd; ++d) {
-        off += (uint64_t)cells_along(doms[d].extent[0], cell) * (uint64_t)cells_along(doms[d].extent[1], cell);
+        const int32_t cx = cells_along(doms[d].extent[0], cell);
+        const int32_t cy = cells_along(doms[d].extent[1], cell);
+        if (cx < 0 || cy < 0) { return CELLS_INVALID; }
+        off += (uint64_t)cx * (uint64_t)cy;
     }
     return off;
 }
@@ -2134,6 +2149,10 @@ int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, 
         }
     }
     const uint64_t cells = count_cells(params, domains, n_domains);
+    if (cells == CELLS_INVALID) {
+        gpe::set_error(GPE_ERR_CAPACITY, "gpe_pbf_create: a scene extent is not finite or spans 2^30 cells or more");
+        return GPE_ERR_CAPACITY;
+    }
     if (cells == 0 || cells > (uint64_t)1 << 30) {
         gpe::set_error(GPE_ERR_CAPACITY, "gpe_pbf_create: %llu cells exceed the 2^30 limit",
                        (unsigned long long)cells);
@@ -2608,6 +2627,11 @@ extern "C" int32_t gpe_pbf_emit(gpe_pbf* s, const gpe_hose* hose, uint64_t seed,
     HoseK h{};
     const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
     if (requested) { *requested = cnt; }
+    if (cnt < 0 || (int64_t)cnt > s->cap) {
+        gpe::set_error(GPE_ERR_CAPACITY, "emit: the hose asks for %s particles, more than the engine's capacity "
+                       "of %lld", cnt < 0 ? "2^31 or more" : std::to_string(cnt).c_str(), (long long)s->cap);
+        return GPE_ERR_CAPACITY;
+    }
     cudaStream_t st = as_stream(stream);
     if (cnt > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
@@ -3015,6 +3039,11 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
         return GPE_ERR_BAD_ARG;
     }
     const uint64_t cells = count_cells(params, domain, 1);
+    if (cells == CELLS_INVALID) {
+        gpe::set_error(GPE_ERR_CAPACITY,
+                       "gpe_pbf_predict_sort_noalloc: the scene extent is not finite or spans 2^30 cells or more");
+        return GPE_ERR_CAPACITY;
+    }
     if ((int64_t)cells != n_cells) {
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_predict_sort_noalloc: the scene has %llu cells, not %lld",
                        (unsigned long long)cells, (long long)n_cells);
@@ -3026,6 +3055,18 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
                        "limits of %d particles / %d cells",
                        (long long)n, (unsigned long long)cells, GPE_NOALLOC_MAX_PARTICLES, GPE_NOALLOC_MAX_CELLS);
         return GPE_ERR_CAPACITY;
+    }
+    // The kernels access pos, vel, pos_sorted and pred_sorted as float2 and the index arrays as 32-bit words:
+    // a misaligned caller pointer (a view offset by one float, say) would fault the whole context, so it is
+    // refused here, before any device work.
+    const auto misaligned = [](const void* ptr, uintptr_t a) { return (reinterpret_cast<uintptr_t>(ptr) & (a - 1)) != 0; };
+    if (misaligned(cell_start, 4) ||
+        (n > 0 && (misaligned(pos, 8) || misaligned(vel, 8) || misaligned(pos_sorted, 8) ||
+                   misaligned(pred_sorted, 8) || misaligned(key_sorted, 4) || misaligned(perm, 4)))) {
+        gpe::set_error(GPE_ERR_BAD_ARG,
+                       "gpe_pbf_predict_sort_noalloc: pos, vel, pos_sorted and pred_sorted must be 8-byte aligned, "
+                       "key_sorted, perm and cell_start 4-byte aligned");
+        return GPE_ERR_BAD_ARG;
     }
     uint8_t* scratch = nullptr;
     rc               = noalloc_scratch(&scratch);

@@ -581,6 +581,12 @@ class Mpm:
         check(lib().gpe_mpm_status(self.h, C.byref(v), stream), "gpe_mpm_status")
         return v.value
 
+    def p2g_wide_warps(self, stream=None) -> int:
+        """Warps whose P2G needed the 5-round run reduction since the last call (read and cleared)."""
+        v = C.c_uint32()
+        check(lib().gpe_mpm_p2g_wide_warps(self.h, C.byref(v), stream), "gpe_mpm_p2g_wide_warps")
+        return v.value
+
     def emit(self, hose: Hose, seed: int = 0, stream=None) -> int:
         req = C.c_int32()
         check(lib().gpe_mpm_emit(self.h, C.byref(hose), int(seed), C.byref(req), stream), "gpe_mpm_emit")

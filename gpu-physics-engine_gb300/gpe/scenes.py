@@ -70,6 +70,34 @@ def reference_pbf_block(nx: int = 48, ny: int = 40, spacing: float = 1.05, seed:
     return pos.astype(F32), vel.astype(F32), [box]
 
 
+def reference_border_band(chunk=(5, 2), speed: float = 1.0, seed: int = 31, box=REFERENCE_BOX):
+    """Atoms converging on one 32 x 32 chunk of the reference's world from the 2 x 2 cells that border it in its
+    eight neighbour chunks (reference units, velocities per substep): 8 atoms per cell, placed so that their
+    first prediction x + v + g lies in that cell, every atom moving towards the chunk's centre at `speed`.
+    After one substep 258 of them queue for the centre chunk, most of the reference's 320 migration slots
+    (kMaxMigrants, constants.h:51), while no border cell holds more atoms than the 8 halo slots the reference
+    exports per cell (kCellSlots, constants.h:47; a denser border cell loses neighbours across the chunk
+    border in the reference, haloKernel PBF.cu:66-137)."""
+    g = rng(seed)
+    g_step = reference_pbf_params().gravity[1]
+    x0, y0 = chunk[0] * 32.0, chunk[1] * 32.0
+    cells = []
+    for k in range(16):
+        cells += [(x0 - 2.0, y0 + 2 * k, True), (x0 + 32.0, y0 + 2 * k, True),
+                  (x0 + 2 * k, y0 - 2.0, False), (x0 + 2 * k, y0 + 32.0, False)]
+    cells += [(x0 - 2.0, y0 - 2.0, True), (x0 + 32.0, y0 - 2.0, True), (x0 - 2.0, y0 + 32.0, True),
+              (x0 + 32.0, y0 + 32.0, True)]
+    across = [(ox, oy) for ox in (0.5, 1.5) for oy in (0.25, 0.75, 1.25, 1.75)]
+    along = [(ox, oy) for ox in (0.25, 0.75, 1.25, 1.75) for oy in (0.5, 1.5)]
+    pts = [(cx + ox, cy + oy) for cx, cy, side in cells for ox, oy in (across if side else along)]
+    xs1 = np.array(pts) + g.uniform(-0.05, 0.05, (len(pts), 2))  # first predictions
+    d = np.array([x0 + 16.0, y0 + 16.0]) - xs1
+    vel = speed * d / np.linalg.norm(d, axis=1, keepdims=True) + g.uniform(-0.02, 0.02, xs1.shape)
+    pos = xs1 - vel
+    pos[:, 1] -= g_step
+    return pos.astype(F32), vel.astype(F32), [box]
+
+
 def reference_million(seed: int = 12, side: int = 1024):
     """1,048,576 atoms on a 1024 x 1024 lattice (spacing 1, the atom diameter) filling a 32 x 32-chunk world
     of the reference (1024 x 1024 units, 1024 atoms per chunk of capacity 1536), small random
@@ -155,6 +183,30 @@ def million(seed: int = 2, spacing: float = 0.01, h: float = 0.02):
     vel[block.shape[0]:, 0] = sp * np.cos(ang)
     vel[block.shape[0]:, 1] = sp * np.sin(ang)
     return pos.astype(F32), vel.astype(F32), [(0.0, 0.0, side, side)]
+
+
+MILLION_DT = 1.0 / 2000.0  # the 10 m deep block needs an effective sound speed K dx / dt well above sqrt(g H)
+
+
+def million_workload(iters: int = 4):
+    """The 1M-particle PBF workload: million() with the dam-break physics at dt = 1/2000 (the plain 4-iteration
+    form diverges at 1/240 and above on this 10 m deep block). Returns (params, pos, vel, boxes)."""
+    p = dam_params(iters=iters)
+    p.dt = MILLION_DT
+    pos, vel, boxes = million()
+    return p, pos, vel, boxes
+
+
+BATCHED_DT = 1.0 / 480.0  # the dam-break physics is stable at 1/480, not at 1/120 (4 Jacobi iterations)
+
+
+def batched_workload(iters: int = 4, n_scenes: int = 256):
+    """256 independent dam-break scenes (batched_scenes, seed 3, 2,048-65,536 particles each) with the
+    dam-break physics at dt = 1/480. Returns (params, pos, vel, dom, boxes)."""
+    p = dam_params(iters=iters)
+    p.dt = BATCHED_DT
+    pos, vel, dom, boxes = batched_scenes(n_scenes=n_scenes, seed=3, lo=2048, hi=65536)
+    return p, pos, vel, dom, boxes
 
 
 def batched_scenes(n_scenes: int = 256, seed: int = 3, lo: int = 2048, hi: int = 65536, spacing: float = 0.01):
@@ -281,6 +333,16 @@ def two_squares(n: int = 65536, seed: int = 1):
     vel[:h, 0] = 0.5
     vel[h:, 0] = -0.5
     return pos, vel
+
+
+def elastic_workload(sort_interval: int = 16):
+    """The plain MLS-MPM workload: 65,536 fixed-corotated particles in two squares on a 128^2 grid
+    (elastic_params, two_squares), 32 particles per cell, re-sorted by cell every sort_interval steps so that
+    the particles of a cell are consecutive. Returns (params, pos, vel)."""
+    p = elastic_params()
+    p.sort_interval = sort_interval
+    pos, vel = two_squares()
+    return p, pos, vel
 
 
 def mixed_params(n: int, grid: int = 1024) -> MpmParams:

@@ -162,8 +162,10 @@ int32_t gpe_pbf_status(gpe_pbf* pbf, uint32_t* status, void* stream);
 int32_t gpe_pbf_launches_per_step(const gpe_pbf* pbf, int32_t* launches);
 /* Self-test of the bounded device waits (no counterpart in the reference): one block arrives at the
  * persistent kernels' grid barrier set up to expect one more arrival than it will get, so its wait gives up
- * after the barrier's time limit (100 ms), records GPE_STATUS_TIMEOUT and the kernel returns; *status
- * receives the device status word. The device stays usable afterwards. */
+ * after a 100 ms limit, records GPE_STATUS_TIMEOUT and the kernel returns; *status receives the device
+ * status word. The device stays usable afterwards. (Inside the persistent solve the same wait gives up after
+ * 2 s, far above a barrier's microseconds, so that a context that the GPU time-slices with other processes
+ * is not reported as hung.) */
 int32_t gpe_selftest_barrier_timeout(uint32_t* status);
 
 /* A "hose pipe" source (hosePipe, PBF.cu:1033-1065 and MPM.cu:439-473): rows of particles on a square lattice
@@ -364,7 +366,10 @@ int32_t gpe_pbf_autotune(gpe_pbf* pbf, int32_t trial_steps, gpe_pbf_tuning* best
  *        (n_cells from the scene extent and the sort-cell size, as gpe_pbf_num_cells reports).
  * Limits: n <= GPE_NOALLOC_MAX_PARTICLES and n_cells <= GPE_NOALLOC_MAX_CELLS, else GPE_ERR_CAPACITY.
  * The first call on a device looks up the scratch array's device address (cudaGetSymbolAddress) and should
- * come before any stream capture. All calls share the one array: calls that overlap on the GPU (on
+ * come before any stream capture. Under lazy module loading the array itself is created when the library's
+ * device code is first used on the device, which can be this first call; make it early, before device memory
+ * runs short. pos, vel, pos_sorted and pred_sorted must be 8-byte aligned and key_sorted, perm and cell_start
+ * 4-byte aligned, else GPE_ERR_BAD_ARG before any device work. All calls share the one array: calls that overlap on the GPU (on
  * different streams, or from several host threads) race, so serialise them. */
 #define GPE_NOALLOC_MAX_PARTICLES (1 << 18)
 #define GPE_NOALLOC_MAX_CELLS (1 << 20)
@@ -463,6 +468,11 @@ int32_t gpe_mpm_stage(gpe_mpm* mpm, int32_t stage, void* stream);
 /* Node grid of the current step: nx*ny float4 (momentum or velocity x, y; mass; unused). */
 int32_t gpe_mpm_get_grid(gpe_mpm* mpm, float* dst, int64_t n_nodes, int32_t mem, void* stream);
 int32_t gpe_mpm_status(gpe_mpm* mpm, uint32_t* status, void* stream);
+/* Diagnostic without a counterpart in the reference (whose P2G, MPM.cu:116-126, issues one global atomic per
+ * node and particle): reads and clears the number of warps whose P2G summed their particles' node
+ * contributions with the 5-round segmented reduction, i.e. held a run of more than 16 consecutive particles
+ * sharing one stencil base node (scenes at about 30 particles per cell), since the last call. */
+int32_t gpe_mpm_p2g_wide_warps(gpe_mpm* mpm, uint32_t* count, void* stream);
 int32_t gpe_mpm_launches_per_step(const gpe_mpm* mpm, int32_t* launches);
 /* Appends the hose's particles at the live count (MPMEmitterKernel, MPM.cu:380-438): C = 0, F = I, J = 1
  * and the engine's material; needs GPE_MPM_FLAG_DYNAMIC_COUNT. *requested receives width x rows. */

@@ -209,14 +209,53 @@ class RefPBF:
                 _p(self.halo_vel), _p(self.num_atoms)], stream)
         if not full:
             return
+        self.migrate(stream)
+        self.prep(stream)
+
+    def migrate(self, stream=0):
+        """The migration half of a substep's tail (PBF.cu:947-950): halo offsets cleared, then atoms whose next
+        prediction leaves their chunk queued for the destination chunk."""
         _chk(cu().cuMemsetD32Async(C.c_void_p(_p(self.halo_offsets)), 0, self.halo_offsets.numel(),
                                    C.c_void_p(stream)), "memset halo_offsets")
-        launch(k["migrationKernel"], (sx, sy), (512,),
+        launch(self.k["migrationKernel"], (self.sx, self.sy), (512,),
                [_p(self.pos[1]), _p(self.vel), _p(self.num_atoms), _p(self.mig_pos), _p(self.mig_vel),
                 _p(self.mig_count)], stream)
-        launch(k["prepNextSubstepKernel"], (sx, sy), (256,),
+
+    def prep(self, stream=0):
+        """prepNextSubstepKernel (PBF.cu:951-954): queues drained, next prediction, per-chunk cell sort."""
+        launch(self.k["prepNextSubstepKernel"], (self.sx, self.sy), (256,),
                [_p(self.offsets), _p(self.pos[0]), _p(self.pos[1]), _p(self.vel), _p(self.num_atoms),
                 _p(self.mig_pos), _p(self.mig_vel), _p(self.mig_count)], stream)
+
+    def read_sorted(self):
+        """Every atom after prepNextSubstepKernel, chunk by chunk in the reference's (atomic-order) sorted
+        order: (global cell index in the scene's row-major grid of 16 x 16-cell chunks, x, x*), absolute."""
+        import torch
+
+        torch.cuda.synchronize()
+        num = self.num_atoms.cpu().numpy()
+        offs = self.offsets.cpu().numpy().view(np.uint32).reshape(self.sx * self.sy, 256)
+        P0 = self.pos[0].cpu().numpy().reshape(self.sx * self.sy, self.MAX_ATOMS, 2)
+        P1 = self.pos[1].cpu().numpy().reshape(self.sx * self.sy, self.MAX_ATOMS, 2)
+        cells, xs_, x_ = [], [], []
+        ncx = self.sx * self.GRID
+        for c in range(self.sx * self.sy):
+            n = int(num[c])
+            if n == 0:
+                continue
+            start = offs[c] & 0xFFFF
+            end = offs[c] >> 16
+            if int(end[-1]) != n:
+                raise RuntimeError(f"chunk {c}: cell offsets end at {int(end[-1])}, not at its {n} atoms")
+            local = np.repeat(np.arange(256), (end - start).astype(np.int64))
+            gx = (c % self.sx) * self.GRID + local % self.GRID
+            gy = (c // self.sx) * self.GRID + local // self.GRID
+            org = np.array([(c % self.sx) * self.CHUNK, (c // self.sx) * self.CHUNK], np.float32)
+            cells.append(gy * ncx + gx)
+            x_.append(P0[c, :n] + org)
+            xs_.append(P1[c, :n] + org)
+        return (np.concatenate(cells).astype(np.uint32), np.concatenate(x_).astype(np.float32),
+                np.concatenate(xs_).astype(np.float32))
 
     def output(self, stream=0):
         launch(self.k["PBFOutputKernel"], (self.sx, self.sy), (256,),

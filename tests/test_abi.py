@@ -72,3 +72,47 @@ def test_no_device_reports_device_error(gpe_mod, monkeypatch):
     rc = lib.gpe_pbf_create(C.byref(p), gpe_mod.make_domains([(0, 0, 1, 1)]), 1, 10, C.byref(h))
     assert rc == gpe_mod.ERR_DEVICE
     assert b"cuda" in lib.gpe_last_error_message().lower()
+
+
+def test_extents_beyond_the_cell_range_are_refused(gpe_mod):
+    """A scene whose extent / cell is not finite or reaches 2^30 cells along an edge is refused with
+    GPE_ERR_CAPACITY before the cell count is cast to int32 (and before the device is touched)."""
+    lib = gpe_mod.lib()
+    from gpe import scenes
+
+    p = scenes.dam_params()
+    h = C.c_void_p()
+    for ext in ((1e30, 1.0), (1.0, float("inf")), (float(2 ** 31) * 0.02, 1.0)):
+        doms = gpe_mod.make_domains([(0.0, 0.0, ext[0], ext[1])])
+        assert lib.gpe_pbf_create(C.byref(p), doms, 1, 10, C.byref(h)) == gpe_mod.ERR_CAPACITY, ext
+        fn = lib.gpe_pbf_predict_sort_noalloc
+        fn.restype = C.c_int32
+        fn.argtypes = [C.POINTER(gpe_mod.PbfParams), C.POINTER(gpe_mod.Domain), C.c_void_p, C.c_void_p, C.c_int64,
+                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        base = 0x10000
+        rc = fn(C.byref(p), doms, base, base, 4, base, base, base, base, base, 16, None)
+        assert rc == gpe_mod.ERR_CAPACITY, ext
+
+
+def test_noalloc_refuses_misaligned_buffers_before_any_launch(gpe_mod):
+    """The allocation-free sort reads and writes caller memory as float2 and 32-bit words; a pointer that is
+    not aligned for that (here one float past an aligned base) is refused with GPE_ERR_BAD_ARG before any
+    device work, so the call is safe to make without a GPU."""
+    lib = gpe_mod.lib()
+    from gpe import scenes
+
+    p = scenes.dam_params()
+    fn = lib.gpe_pbf_predict_sort_noalloc
+    fn.restype = C.c_int32
+    fn.argtypes = [C.POINTER(gpe_mod.PbfParams), C.POINTER(gpe_mod.Domain), C.c_void_p, C.c_void_p, C.c_int64,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    doms = gpe_mod.make_domains([(0.0, 0.0, 0.32, 0.32)])
+    cells = 16 * 16
+    base = 0x100000
+    good = [base] * 7
+    for slot, off in ((0, 4), (1, 4), (2, 4), (3, 4), (4, 2), (5, 2), (6, 2)):
+        args = list(good)
+        args[slot] = base + off
+        rc = fn(C.byref(p), doms, args[0], args[1], 64, args[2], args[3], args[4], args[5], args[6], cells, None)
+        assert rc == gpe_mod.ERR_BAD_ARG, slot
+        assert b"aligned" in lib.gpe_last_error_message()

@@ -110,6 +110,28 @@ def test_pbf_emit_respects_capacity(gpe_mod, cuda_ok):
     assert e.status() & gpe_mod.STATUS_CAPACITY
 
 
+def test_emit_refuses_a_hose_beyond_int32_or_capacity(gpe_mod, cuda_ok):
+    """Width x rows is computed in 64-bit: a hose whose count overflows int32 (or exceeds the engine's
+    capacity) is refused with GPE_ERR_CAPACITY instead of wrapping to a wrong count."""
+    from gpe import scenes
+
+    e, _, pos, _, _ = _pbf(gpe_mod, capacity=5000)
+    n0 = e.n
+    for nozzle, spacing in ((1e9, 1e-3), (8.0, 1e-5), (4e5, 1.05)):
+        with pytest.raises(gpe_mod.GpeError) as ei:
+            e.emit(gpe_mod.make_hose((50.0, 150.0), (1.0, -0.3), nozzle, spacing, 0.0, 20))
+        assert ei.value.status == gpe_mod.ERR_CAPACITY
+    assert e.n == n0 and e.status() == 0
+    mp = scenes.elastic_params(2048, 64)
+    mp.flags |= gpe_mod.MPM_FLAG_DYNAMIC_COUNT
+    m = gpe_mod.Mpm(mp, capacity=4096)
+    m.set_state(np.full((16, 2), 0.5, np.float32))
+    with pytest.raises(gpe_mod.GpeError) as ei:
+        m.emit(gpe_mod.make_hose((0.5, 0.5), (1.0, 0.0), 1e9, 1e-4, 0.0, 10))
+    assert ei.value.status == gpe_mod.ERR_CAPACITY
+    m.close()
+
+
 def test_pbf_emit_needs_dynamic_count(gpe_mod, cuda_ok):
     e, _, _, _, _ = _pbf(gpe_mod, dynamic=False)
     with pytest.raises(gpe_mod.GpeError) as ei:

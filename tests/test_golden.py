@@ -59,3 +59,24 @@ def test_oracle_reproduces_reference_mpm_substep(gpe_mod, oracle):
         if nm == "C":
             tol = 1e-4 * np.abs(b).max()
         _assert_close(a, b, tol, f"MPM {nm}")
+
+
+def test_oracle_reproduces_reference_migration_and_sort(gpe_mod, oracle):
+    """A complete reference substep, migration and the per-chunk cell sort included, on the border band:
+    258 atoms queue for one chunk (of its 320 slots). After the oracle's step and the next predict + sort,
+    every cell holds as many atoms as in the reference and the same atoms (x and the next prediction x*)."""
+    from gpe import scenes
+    from refcompare import compare_with_reference_sort
+
+    g = _load("pbf_reference_migration.npz")
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_border_band()
+    assert np.array_equal(pos, g["x"]) and np.array_equal(vel, g["v"]), "fixture inputs changed"
+    mig = g["mig_count"]
+    assert 240 <= mig.max() < 320, f"the fullest migration queue holds {mig.max()} atoms"
+    assert int(mig.sum()) > 250
+    o = oracle.PbfOracle(p, boxes)
+    r = o.step(pos, vel, None, 1, pair_id=g["slot"])
+    s = o.predict_sort(r["x"], r["v"])
+    compare_with_reference_sort(g["out_cell"], g["out_x"], g["out_xs"], s["key"], s["x"], s["xs"])
+

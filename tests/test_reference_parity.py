@@ -4,7 +4,9 @@ driver API by oracle/refrun.py) on the same inputs.
 PBF: one substep stopped after XSPHKernel, so no atomic-order sort intervenes; the engine and the oracle seed
 the self pair's pseudo-random gradient direction with the reference's chunk slots (GPE_PBF_PAIR_IDS), so
 every term matches. The reference works in chunk-local coordinates, the engine in scene coordinates, so
-positions differ by the rounding of that change of frame (a few ulp of the scene coordinate).
+positions differ by the rounding of that change of frame (a few ulp of the scene coordinate). A complete
+substep — migration across chunk borders and the reference's per-chunk cell sort — is compared cell by cell
+(tests/refcompare.py): the reference's order within a cell follows shared-memory atomics.
 """
 import numpy as np
 import pytest
@@ -74,19 +76,51 @@ def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok)
     _check_pbf(xs0, ox, ov, ol, rx, rv, rl, "oracle")
 
 
-def test_pbf_full_substeps_run(gpe_mod, cuda_ok):
-    """Several complete reference substeps (with migration and the atomic-order sort) keep every atom and
-    stay inside the box; the engine's steps from the same state keep the same atom count."""
+def _engine_substep_then_sort(gpe_mod, p, pos, vel, slot, boxes):
+    """The engine's step seeded like the reference (pair directions from the reference's chunk slots), then the
+    next step's predict + sort: (cell key, x, x*) in sorted order."""
+    q = p.copy()
+    q.flags |= gpe_mod.PBF_PAIR_IDS
+    e = gpe_mod.Pbf(q, boxes, capacity=len(pos))
+    e.set_state(pos, vel)
+    e.set_field(gpe_mod.PBF_FIELD_ID, np.asarray(slot, np.uint32))
+    e.step(1)
+    assert e.status() == 0
+    e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+    out = (e.field(gpe_mod.PBF_FIELD_KEY), e.field(gpe_mod.PBF_FIELD_POS), e.field(gpe_mod.PBF_FIELD_PRED))
+    e.close()
+    return out
+
+
+def test_pbf_complete_substep_with_migration_matches_reference(gpe_mod, cuda_ok):
+    """A complete reference substep on the border band — migration of 258 atoms into one chunk (of its 320
+    queue slots) and the per-chunk cell sort included — against the engine's step and next predict + sort:
+    per-cell counts bit for bit and the same atoms in every cell, both against the reference run here and
+    against the committed fixture."""
     import torch
     from oracle import refrun
+    from refcompare import compare_with_reference_sort
 
-    p, pos, vel, boxes = _pbf_case()
+    from gpe import scenes
+
+    p = scenes.reference_pbf_params(iters=2)
+    pos, vel, boxes = scenes.reference_border_band()
     ref = refrun.RefPBF((12, 6), 320)
-    ref.seed(pos, vel, float(p.gravity[1]))
-    for _ in range(5):
-        ref.substep(iters=p.iters, full=True)
+    _, slot = ref.seed(pos, vel, float(p.gravity[1]))
+    ref.substep(iters=p.iters, full=False)
+    ref.migrate()
     torch.cuda.synchronize()
-    assert int(ref.num_atoms.sum().item()) == len(pos)
+    mig = ref.mig_count.cpu().numpy()
+    assert 240 <= mig.max() < 320
+    ref.prep()
+    cell, rx, rxs = ref.read_sorted()
+    assert len(cell) == len(pos)
+    key, x, xs = _engine_substep_then_sort(gpe_mod, p, pos, vel, slot, boxes)
+    compare_with_reference_sort(cell, rx, rxs, key, x, xs)
+    from pathlib import Path
+
+    g = dict(np.load(Path(__file__).resolve().parent / "golden" / "pbf_reference_migration.npz"))
+    compare_with_reference_sort(g["out_cell"], g["out_x"], g["out_xs"], key, x, xs)
 
 
 def test_mpm_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok):
