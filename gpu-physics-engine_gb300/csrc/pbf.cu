@@ -10,7 +10,10 @@
 //   vorticity confinement       k_vorticity      (Macklin & Mueller 2013; absent in the reference)
 //
 // Layout: structure-of-arrays in HBM, particles of all scenes in one array sorted by global cell key
-// (scene-major, then row-major cells), so a row of neighbour cells is one contiguous index range. The
+// (scene-major, then row-major cells), so a row of neighbour cells is one contiguous index range. Within a
+// step each particle is held as its start position x and its displacement d = x* - x (one float4): the
+// neighbour offset x*_i - x*_j = (x_i - x_j) + (d_i - d_j) and the velocity d / dt then keep FP32 precision
+// relative to themselves, whatever the magnitude of the scene coordinates. The
 // reference's per-chunk shared-memory pools, 1-cell halo copies and migration queues exist because a block
 // of its design must hold a whole chunk; with a device-wide sort every scene is one domain, neighbours
 // across what were chunk borders are read in place from L2, and a particle that crosses a border simply
@@ -102,6 +105,23 @@ __device__ __forceinline__ T ldn(const T* p)
         return __ldg(p);
     }
 }
+
+// A particle of the step: start position x (.x, .y) and displacement d = x* - x (.z, .w).
+__device__ __forceinline__ float2 xy_of(const float4 a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ float2 d_of(const float4 a) { return make_float2(a.z, a.w); }
+// The offset x*_i - x*_j from the start positions and displacements. For neighbours x_i - x_j is exact (the
+// two lie within a factor two of each other, Sterbenz), so the offset's only rounding is relative to itself,
+// not to the coordinates; x* itself (x + d, rounded) is needed only to find a particle's cell.
+__device__ __forceinline__ float2 offset(const float2 pi, const float2 di, const float4 b)
+{
+    return add2(sub2(pi, xy_of(b)), sub2(di, d_of(b)));
+}
+
+// a neighbour's (x, d) record and one more value of it (lambda, omega or the multiplier memory)
+struct Nbr {
+    float4 q;
+    float a;
+};
 
 // Visits every particle index in the cells within R of the base cell of (px, py) (the reference scans the
 // 3x3 cells around clamp(floorf(x)/kCellDim), PBF.cu:252-263). Each row of cells is one contiguous range.
@@ -345,12 +365,16 @@ __global__ void __launch_bounds__(T_PART)
 // The atomic ranks are unique but depend on warp scheduling; the stable slot of particle i is the number of
 // entries of its cell's bucket with a smaller pre-sort index.
 // CG: start and bucket were written earlier in the same (persistent) kernel, so they are read from L2
+// Output: the step's (x, d) records (xd_out, the engine), or x and x* as two float2 arrays (x_out, xs_out, the
+// allocation-free sort). d = x* - x is computed from the FP32 x* that decided the cell key, so x + d gives that
+// x* back (exactly while x and x* lie within a factor two of each other).
 template <bool CG = false>
 __device__ __forceinline__ void place_one(const PbfK& k, const uint2* __restrict__ keyrank,
                                           const uint32_t* __restrict__ start, const uint32_t* __restrict__ bucket,
-                                          const float2* __restrict__ x_in, const float2* __restrict__ v_in,
-                                          float2* __restrict__ x_out, float2* __restrict__ xs_out,
-                                          uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out,
+                                          const float2* x_in, const float2* __restrict__ v_in,
+                                          float4* __restrict__ xd_out, float2* __restrict__ x_out,
+                                          float2* __restrict__ xs_out, uint32_t* __restrict__ perm,
+                                          uint32_t* __restrict__ key_out,
                                           const uint32_t* __restrict__ id_in, uint32_t* __restrict__ id_out,
                                           const float* __restrict__ acc_in, float* __restrict__ prev_out,
                                           float* __restrict__ lam_out, int32_t i)
@@ -362,8 +386,13 @@ __device__ __forceinline__ void place_one(const PbfK& k, const uint2* __restrict
     for (uint32_t t = s; t < e; ++t) { rank += (ldn<CG>(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
     const uint32_t dst = s + rank;
     const float2 p     = x_in[i];
-    x_out[dst]         = p;
-    xs_out[dst]        = predict(k, p, v_in[i]);
+    const float2 ps    = predict(k, p, v_in[i]);
+    if (xd_out) {
+        xd_out[dst] = make_float4(p.x, p.y, __fsub_rn(ps.x, p.x), __fsub_rn(ps.y, p.y));
+    } else {
+        x_out[dst]  = p;
+        xs_out[dst] = ps;
+    }
     perm[dst]          = (uint32_t)i;
     key_out[dst]       = kr.x;
     if (id_in) { id_out[dst] = id_in[i]; }
@@ -378,15 +407,15 @@ __device__ __forceinline__ void place_one(const PbfK& k, const uint2* __restrict
 __global__ void __launch_bounds__(T_PART)
     k_place(const PbfK k, const uint2* __restrict__ keyrank, const uint32_t* __restrict__ start,
             const uint32_t* __restrict__ bucket, const float2* __restrict__ x_in,
-            const float2* __restrict__ v_in, float2* __restrict__ x_out, float2* __restrict__ xs_out,
-            uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out, const uint32_t* __restrict__ id_in,
-            uint32_t* __restrict__ id_out, const float* __restrict__ acc_in, float* __restrict__ prev_out,
-            float* __restrict__ lam_out)
+            const float2* __restrict__ v_in, float4* __restrict__ xd_out, float2* __restrict__ x_out,
+            float2* __restrict__ xs_out, uint32_t* __restrict__ perm, uint32_t* __restrict__ key_out,
+            const uint32_t* __restrict__ id_in, uint32_t* __restrict__ id_out, const float* __restrict__ acc_in,
+            float* __restrict__ prev_out, float* __restrict__ lam_out)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count_of(k)) { return; }
-    place_one(k, keyrank, start, bucket, x_in, v_in, x_out, xs_out, perm, key_out, id_in, id_out, acc_in, prev_out,
-              lam_out, i);
+    place_one(k, keyrank, start, bucket, x_in, v_in, xd_out, x_out, xs_out, perm, key_out, id_in, id_out, acc_in,
+              prev_out, lam_out, i);
 }
 
 // ----- lambda (PBF.cu:243-294) --------------------------------------------------------------------------
@@ -400,12 +429,14 @@ enum { ACC_NONE = 0, ACC_SUM = 1, ACC_PROJ = 2 };
 template <bool MULTI, bool SELFG, int ACC, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restrict__ doms,
                                            const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
-                                           const float2* __restrict__ xs, float* __restrict__ lam,
+                                           const float4* __restrict__ xd, float* __restrict__ lam,
                                            const uint32_t* __restrict__ pair_id, float* __restrict__ acc, int32_t i)
 {
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
-    const float2 p       = xs[i];
+    const float4 p4      = xd[i];
+    const float2 px = xy_of(p4), pd = d_of(p4);
+    const float2 p       = add2(px, pd); // x*, for the cell lookup
     // The reference accumulates per pair sv = -cs m (h-r)^2 r/|r|, |sv|^2 / m and m W6 (PBF.cu:264-286).
     // Constants are hoisted: sx, sy = sum (h-r)^2 r/|r|, s4 = sum (h-r)^4 (= |sv|^2 / (cs m)^2 since r/|r| is a
     // unit vector), s6 = sum (h^2 - r^2)^3. The self pair (r = 0) is added after the loop: it contributes
@@ -417,8 +448,8 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     // pairs beyond h (and of the self pair) are masked to zero; a data-dependent accept branch here would
     // make each warp execute both paths on almost every iteration.
     // ME: the candidate may be the particle itself (full scans); masked scans never visit it
-    auto body = [&](uint32_t j, const float2 q, auto me) -> bool {
-        const float2 r  = sub2(p, q);
+    auto body = [&](uint32_t j, const float4 q, auto me) -> bool {
+        const float2 r  = offset(px, pd, q);
         const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool self = decltype(me)::value && j == (uint32_t)i;
         self_seen       = self_seen || self;
@@ -432,7 +463,7 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         const float w   = d2 * inv;
         sg              = fma2(make_float2(w, w), r, sg);
         s4              = fmaf(d2, d2, s4);
-        if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
+        if (SELFG && in && !dir && r.x == 0.f && r.y == 0.f) {
             // a distinct atom at the same position: the reference's pseudo-random pair direction
             float nx, ny;
             if (pair_id) {
@@ -447,9 +478,9 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         return r2 < k.skin2;
     };
     const bool self_masked = scan_ld2<MASK, CG>(
-        d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xs[j]); },
-        [&](uint32_t j, const float2 q) -> bool { return body(j, q, std::true_type{}); },
-        [&](uint32_t j, const float2 q) -> bool { return body(j, q, std::false_type{}); });
+        d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xd[j]); },
+        [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::true_type{}); },
+        [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::false_type{}); });
     self_seen = self_seen || self_masked;
     if (self_seen) {
         s6 = fmaf(k.h2 * k.h2, k.h2, s6);
@@ -486,12 +517,12 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
 template <bool MULTI, bool SELFG, int ACC, int MASK>
 __global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (MASK == MASK_USE ? 4 : 1))
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-             const uint32_t* __restrict__ start, const float2* __restrict__ xs, float* __restrict__ lam,
+             const uint32_t* __restrict__ start, const float4* __restrict__ xd, float* __restrict__ lam,
              const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < count_of(k)) {
-        lambda_one<MULTI, SELFG, ACC, false, MASK>(k, doms, dom, start, xs, lam, pair_id, acc, i);
+        lambda_one<MULTI, SELFG, ACC, false, MASK>(k, doms, dom, start, xd, lam, pair_id, acc, i);
     }
 }
 
@@ -500,11 +531,13 @@ __global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (M
 template <bool MULTI, bool SCORR, bool ACCINIT, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restrict__ doms,
                                             const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
-                                            const float2* __restrict__ xs, const float* __restrict__ lam,
-                                            float2* __restrict__ xs_out, float* __restrict__ acc, int32_t i)
+                                            const float4* __restrict__ xd, const float* __restrict__ lam,
+                                            float4* __restrict__ xd_out, float* __restrict__ acc, int32_t i)
 {
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
-    const float2 p  = xs[i];
+    const float4 p4 = xd[i];
+    const float2 px = xy_of(p4), pd = d_of(p4);
+    const float2 p  = add2(px, pd); // x*, for the cell lookup
     const float li  = lam[i];
     if (ACCINIT) { acc[i] = li; }
     const float mli = li * k.mass;
@@ -513,14 +546,10 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
     const float c6w = k.c6 * k.inv_w_dq;
     float2 sg = make_float2(0.f, 0.f); // (sx, sy)
     scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
-                      [&](uint32_t j) {
-                          const float2 q = ldn<CG>(&xs[j]);
-                          return make_float3(q.x, q.y, ldn<CG>(&lam[j]));
-                      },
-                      [&](uint32_t, const float3 ql) -> bool {
-        const float2 q  = make_float2(ql.x, ql.y);
-        const float lj  = ql.z;
-        const float2 r  = sub2(p, q);
+                      [&](uint32_t j) { return Nbr{ldn<CG>(&xd[j]), ldn<CG>(&lam[j])}; },
+                      [&](uint32_t, const Nbr ql) -> bool {
+        const float lj  = ql.a;
+        const float2 r  = offset(px, pd, ql.q);
         const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool ok   = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
         const float inv = rsqrtf(ok ? r2 : 1.f);
@@ -537,13 +566,15 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
         return false;
     });
     const float s = -k.cs * k.dp_scale;
-    float ox = fmaf(s, sg.x, p.x), oy = fmaf(s, sg.y, p.y);
-    // clamp<float>(v, lb, ub), PBF.cu:496-497
-    oy = (oy > d.hiy) ? d.hiy : ((oy < d.loy) ? d.loy : oy);
-    ox = (ox > d.hix) ? d.hix : ((ox < d.lox) ? d.lox : ox);
-    xs_out[i] = make_float2(ox, oy);
+    // the correction moves the displacement; the position x + d is clamped to the walls (clamp<float>(v, lb,
+    // ub), PBF.cu:496-497) by setting d = wall - x, exact next to the wall, so that x + d lands on it
+    float dx = fmaf(s, sg.x, pd.x), dy = fmaf(s, sg.y, pd.y);
+    const float ox = px.x + dx, oy = px.y + dy;
+    dy = (oy > d.hiy) ? __fsub_rn(d.hiy, px.y) : ((oy < d.loy) ? __fsub_rn(d.loy, px.y) : dy);
+    dx = (ox > d.hix) ? __fsub_rn(d.hix, px.x) : ((ox < d.lox) ? __fsub_rn(d.lox, px.x) : dx);
+    xd_out[i] = make_float4(px.x, px.y, dx, dy);
     if constexpr (MASK == MASK_USE) {
-        const float mx = ox - p.x, my = oy - p.y;
+        const float mx = dx - pd.x, my = dy - pd.y;
         if (!(fmaf(mx, mx, my * my) < k.move2)) { mark_mover(k.mflag, d.coff, d.ncx, d.ncy, __ldg(&k.keys[i])); }
     }
 }
@@ -551,12 +582,12 @@ __device__ __forceinline__ void delta_p_one(const PbfK& k, const DomDev* __restr
 template <bool MULTI, bool SCORR, bool ACCINIT, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_delta_p(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-              const uint32_t* __restrict__ start, const float2* __restrict__ xs, const float* __restrict__ lam,
-              float2* __restrict__ xs_out, float* __restrict__ acc)
+              const uint32_t* __restrict__ start, const float4* __restrict__ xd, const float* __restrict__ lam,
+              float4* __restrict__ xd_out, float* __restrict__ acc)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < count_of(k)) {
-        delta_p_one<MULTI, SCORR, ACCINIT, false, MASK>(k, doms, dom, start, xs, lam, xs_out, acc, i);
+        delta_p_one<MULTI, SCORR, ACCINIT, false, MASK>(k, doms, dom, start, xd, lam, xd_out, acc, i);
     }
 }
 
@@ -566,19 +597,21 @@ __global__ void __launch_bounds__(T_MAX)
 // the one documented with gpe_pbf_set_warm_start).
 template <bool MULTI, bool SELFG, int MASK = MASK_OFF>
 __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, const uint32_t* __restrict__ start,
-                                               const float2* __restrict__ xs, const float2* __restrict__ xsorted,
-                                               const float* __restrict__ prev, const uint32_t* __restrict__ pair_id,
-                                               int32_t i, uint32_t pbase, float (&f)[MLP_F])
+                                               const float4* __restrict__ xd, const float* __restrict__ prev,
+                                               const uint32_t* __restrict__ pair_id, int32_t i, uint32_t pbase,
+                                               float (&f)[MLP_F])
 {
-    const float2 p = xs[i];
+    const float4 p4 = xd[i];
+    const float2 px = xy_of(p4), pd = d_of(p4);
+    const float2 p  = add2(px, pd); // x*
     float2 sg = make_float2(0.f, 0.f); // (sx, sy)
     float s4 = 0.f, s6 = 0.f, swl = 0.f;
     int32_t nn     = 0;
     bool self_seen = false;
     scan<MASK, false>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float2 q  = __ldg(&xs[j]);
+        const float4 q  = __ldg(&xd[j]);
         const float lp  = __ldg(&prev[j]);
-        const float2 r  = sub2(p, q);
+        const float2 r  = offset(px, pd, q);
         const float r2  = fmaf(r.x, r.x, r.y * r.y);
         const bool self = j == (uint32_t)i;
         self_seen       = self_seen || self;
@@ -594,7 +627,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
         const float w   = d2 * inv;
         sg              = fma2(make_float2(w, w), r, sg);
         s4              = fmaf(d2, d2, s4);
-        if (SELFG && in && !dir && p.x == q.x && p.y == q.y) {
+        if (SELFG && in && !dir && r.x == 0.f && r.y == 0.f) {
             float nx, ny;
             if (pair_id) {
                 pair_direction(__ldg(&pair_id[i]), __ldg(&pair_id[j]), nx, ny);
@@ -628,8 +661,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
     const float self = k.inv_mass * (gx * gx + gy * gy);
     const float grad = k.inv_rho0 * k.inv_rho0 * (self + gsq);
     const float lam  = -C / (grad + k.eps);
-    const float2 po  = xsorted[i];
-    const float ddx = p.x - po.x, ddy = p.y - po.y;
+    const float ddx = pd.x, ddy = pd.y; // x* - x
     const float inv_h = 1.f / k.h;
     const float wall  = fminf(fminf(p.x - d.lox, d.hix - p.x), fminf(p.y - d.loy, d.hiy - p.y)) * inv_h;
     f[0]  = (float)nn;
@@ -656,8 +688,7 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
 template <bool MULTI, bool SELFG, int MASK>
 __global__ void __launch_bounds__(T_PART)
     k_lambda_feat(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                  const uint32_t* __restrict__ start, const float2* __restrict__ xs,
-                  const float2* __restrict__ xsorted, const float* __restrict__ prev,
+                  const uint32_t* __restrict__ start, const float4* __restrict__ xd, const float* __restrict__ prev,
                   const uint32_t* __restrict__ pair_id, const MlpDev* __restrict__ mlp, uint16_t* __restrict__ feat)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -665,7 +696,7 @@ __global__ void __launch_bounds__(T_PART)
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     float f[MLP_F];
-    (void)warm_features<MULTI, SELFG, MASK>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    (void)warm_features<MULTI, SELFG, MASK>(k, d, start, xd, prev, pair_id, i, pbase, f);
     float mu[MLP_FP], isd[MLP_FP];
 #pragma unroll
     for (int q = 0; q < MLP_FP; ++q) {
@@ -730,16 +761,16 @@ struct CollectK {
 template <bool MULTI, bool SELFG>
 __global__ void __launch_bounds__(T_PART)
     k_lambda_collect(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                     const uint32_t* __restrict__ start, const float2* __restrict__ xs,
-                     const float2* __restrict__ xsorted, const float* __restrict__ prev, float* __restrict__ lam,
-                     const uint32_t* __restrict__ pair_id, const CollectK col)
+                     const uint32_t* __restrict__ start, const float4* __restrict__ xd,
+                     const float* __restrict__ prev, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
+                     const CollectK col)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count_of(k)) { return; }
     const DomDev d       = load_dom<MULTI>(k, doms, dom, i);
     const uint32_t pbase = MULTI ? __ldg(&start[d.coff]) : 0u;
     float f[MLP_F];
-    lam[i] = warm_features<MULTI, SELFG>(k, d, start, xs, xsorted, prev, pair_id, i, pbase, f);
+    lam[i] = warm_features<MULTI, SELFG>(k, d, start, xd, prev, pair_id, i, pbase, f);
     if (col.stride != 0u && mix32((uint32_t)i * 0x9E3779B9u ^ col.salt) % col.stride == 0u) {
         const int32_t slot = atomicAdd(&col.cnt[0], 1);
         if (slot < col.cap) {
@@ -784,23 +815,23 @@ __device__ __forceinline__ void velocity_clamp(const PbfK& k, float& vx, float& 
 template <bool MULTI, bool VORT, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict__ doms,
                                          const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
-                                         const float2* __restrict__ x, const float2* __restrict__ xs,
+                                         const float4* __restrict__ xd, float2* __restrict__ x_out,
                                          float2* __restrict__ v_out, float* __restrict__ omega,
                                          uint32_t* __restrict__ status, int32_t i)
 {
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
-    const float2 p  = xs[i];
-    const float2 po = x[i];
-    const float vax = (p.x - po.x) * k.inv_dt, vay = (p.y - po.y) * k.inv_dt;
+    const float4 p4 = xd[i];
+    const float2 px = xy_of(p4), pd = d_of(p4);
+    const float2 p  = add2(px, pd); // x*: the step's end position
+    // v = (x* - x) / dt = d / dt (PBF.cu:538): no cancellation of two large coordinates
+    const float vax = pd.x * k.inv_dt, vay = pd.y * k.inv_dt;
     // dv = c sum (v_j - v_i) W6 (PBF.cu:602-615) with the poly6 coefficient hoisted; the self pair adds 0.
     // omega = sum (v_j - v_i) x grad_j W with grad_j W = +cs (h-r)^2 r/|r| (cs hoisted as well).
     float2 dvs = make_float2(0.f, 0.f); // (dvx, dvy)
     float w    = 0.f;
     // ME: the candidate may be the particle itself (full scans); masked scans never visit it
-    auto xbody = [&](uint32_t j, const float4 qq4, auto me) -> bool {
-        const float2 q  = make_float2(qq4.x, qq4.y);
-        const float2 qo = make_float2(qq4.z, qq4.w);
-        const float2 r  = sub2(p, q);
+    auto xbody = [&](uint32_t j, const float4 q, auto me) -> bool {
+        const float2 r  = offset(px, pd, q);
         const float rx = r.x, ry = r.y;
         // explicit fused forms: the result must not depend on how the compiler contracts this body in the
         // kernel it is inlined into (separate launches and the persistent solve are compared bit for bit)
@@ -808,7 +839,7 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
         // masked, branch-free (see k_lambda); the self pair adds nothing in exact arithmetic (v_i - v_i) and is
         // left out (masked scans skip the particle's own slot)
         const bool in   = (r2 <= k.h2) && !(decltype(me)::value && j == (uint32_t)i);
-        const float2 dv = fma2(sub2(q, qo), make_float2(k.inv_dt, k.inv_dt), make_float2(-vax, -vay));
+        const float2 dv = fma2(d_of(q), make_float2(k.inv_dt, k.inv_dt), make_float2(-vax, -vay));
         const float dx = dv.x, dy = dv.y;
         const float qq  = in ? k.h2 - r2 : 0.f;
         const float p6  = qq * qq * qq;
@@ -822,14 +853,9 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
         }
         return false;
     };
-    scan_ld2<MASK, CG>(d, k, start, p.x, p.y, i,
-                       [&](uint32_t j) {
-                          const float2 q  = ldn<CG>(&xs[j]);
-                          const float2 qo = ldn<CG>(&x[j]);
-                          return make_float4(q.x, q.y, qo.x, qo.y);
-                      },
-                       [&](uint32_t j, const float4 qq4) -> bool { return xbody(j, qq4, std::true_type{}); },
-                       [&](uint32_t j, const float4 qq4) -> bool { return xbody(j, qq4, std::false_type{}); });
+    scan_ld2<MASK, CG>(d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xd[j]); },
+                       [&](uint32_t j, const float4 q) -> bool { return xbody(j, q, std::true_type{}); },
+                       [&](uint32_t j, const float4 q) -> bool { return xbody(j, q, std::false_type{}); });
     w *= k.cs;
     const float cx = k.xsph_c * k.c6;
     float vx       = fmaf(dvs.x, cx, vax);
@@ -839,40 +865,39 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
         atomicOr(status, GPE_STATUS_NONFINITE);
     }
     v_out[i] = make_float2(vx, vy);
+    x_out[i] = p; // the step's end position, in this step's sorted order
     if (VORT) { omega[i] = w; }
 }
 
 template <bool MULTI, bool VORT, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_xsph(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-           const uint32_t* __restrict__ start, const float2* __restrict__ x, const float2* __restrict__ xs,
+           const uint32_t* __restrict__ start, const float4* __restrict__ xd, float2* __restrict__ x_out,
            float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, x, xs, v_out, omega, status, i); }
+    if (i < count_of(k)) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, xd, x_out, v_out, omega, status, i); }
 }
 
 // ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
 template <bool MULTI, bool CG = false, int MASK = MASK_OFF>
 __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __restrict__ doms,
                                               const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
-                                              const float2* __restrict__ xs, const float* __restrict__ omega,
+                                              const float4* __restrict__ xd, const float* __restrict__ omega,
                                               float2* __restrict__ v, int32_t i)
 {
-    const DomDev d = load_dom<MULTI>(k, doms, dom, i);
-    const float2 p = xs[i];
+    const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
+    const float4 p4 = xd[i];
+    const float2 px = xy_of(p4), pd = d_of(p4);
+    const float2 p  = add2(px, pd); // x*, for the cell lookup
     const float wi = omega[i];
     const float aw = fabsf(wi);
     float2 eg = make_float2(0.f, 0.f); // (ex, ey)
     scan_ld<MASK, CG>(d, k, start, p.x, p.y, i,
-                      [&](uint32_t j) {
-                          const float2 q = ldn<CG>(&xs[j]);
-                          return make_float3(q.x, q.y, ldn<CG>(&omega[j]));
-                      },
-                      [&](uint32_t, const float3 qw) -> bool {
-        const float2 q   = make_float2(qw.x, qw.y);
-        const float wj   = qw.z;
-        const float2 r   = sub2(p, q);
+                      [&](uint32_t j) { return Nbr{ldn<CG>(&xd[j]), ldn<CG>(&omega[j])}; },
+                      [&](uint32_t, const Nbr qw) -> bool {
+        const float wj   = qw.a;
+        const float2 r   = offset(px, pd, qw.q);
         const float rx = r.x, ry = r.y;
         const float r2   = fmaf(rx, rx, ry * ry); // explicit fused forms, as in xsph_one
         const bool ok    = (r2 <= k.h2) && (r2 > 1e-12f); // masked, branch-free (see k_lambda)
@@ -899,11 +924,11 @@ __device__ __forceinline__ void vorticity_one(const PbfK& k, const DomDev* __res
 template <bool MULTI, int MASK>
 __global__ void __launch_bounds__(T_MAX)
     k_vorticity(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                const uint32_t* __restrict__ start, const float2* __restrict__ xs,
+                const uint32_t* __restrict__ start, const float4* __restrict__ xd,
                 const float* __restrict__ omega, float2* __restrict__ v)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { vorticity_one<MULTI, false, MASK>(k, doms, dom, start, xs, omega, v, i); }
+    if (i < count_of(k)) { vorticity_one<MULTI, false, MASK>(k, doms, dom, start, xd, omega, v, i); }
 }
 
 // ----- the persistent solve: every Jacobi pass (and XSPH) of a step in one launch -----------------------
@@ -982,8 +1007,8 @@ __global__ void k_barrier_selftest(GridSync* g, uint32_t* status)
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
 __device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __restrict__ doms,
                                              const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
-                                             float2* __restrict__ xs_a, float2* __restrict__ xs_b,
-                                             const float2* __restrict__ x, float* __restrict__ lam,
+                                             float4* __restrict__ xd_a, float4* __restrict__ xd_b,
+                                             float2* x_out, float* __restrict__ lam,
                                              const uint32_t* __restrict__ pair_id, float2* __restrict__ v,
                                              float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
                                              unsigned int& gen, uint32_t* __restrict__ status)
@@ -991,8 +1016,8 @@ __device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __rest
     const int32_t n      = count_of(k);
     const int32_t stride = (int32_t)(gridDim.x * blockDim.x);
     const int32_t i0     = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
-    float2* cur          = xs_a;
-    float2* nxt          = xs_b;
+    float4* cur          = xd_a;
+    float4* nxt          = xd_b;
     constexpr int MU = MASKS ? MASK_USE : MASK_OFF;
     for (int32_t it = 0; it < iters; ++it) {
         if (MASKS && it == 0) {
@@ -1009,13 +1034,13 @@ __device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __rest
             delta_p_one<MULTI, SCORR, false, true, MU>(k, doms, dom, start, cur, lam, nxt, nullptr, i);
         }
         if (!grid_barrier(gs, gen, status)) { return false; }
-        float2* t = cur;
+        float4* t = cur;
         cur       = nxt;
         nxt       = t;
     }
     if (XSPH) {
         for (int32_t i = i0; i < n; i += stride) {
-            xsph_one<MULTI, false, true, MU>(k, doms, dom, start, x, cur, v, omega, status, i);
+            xsph_one<MULTI, false, true, MU>(k, doms, dom, start, cur, x_out, v, omega, status, i);
         }
     }
     return true;
@@ -1024,14 +1049,14 @@ __device__ __forceinline__ bool solve_phases(const PbfK& k, const DomDev* __rest
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
 __global__ void __launch_bounds__(T_MAX)
     k_solve_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                       const uint32_t* __restrict__ start, float2* __restrict__ xs_a, float2* __restrict__ xs_b,
-                       const float2* __restrict__ x, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
+                       const uint32_t* __restrict__ start, float4* __restrict__ xd_a, float4* __restrict__ xd_b,
+                       float2* __restrict__ x_out, float* __restrict__ lam, const uint32_t* __restrict__ pair_id,
                        float2* __restrict__ v, float* __restrict__ omega, int32_t iters, GridSync* __restrict__ gs,
                        uint32_t* __restrict__ status)
 {
     unsigned int gen = 0u; // the barrier word is zeroed before every launch
-    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, start, xs_a, xs_b, x, lam, pair_id, v, omega, iters,
-                                                   gs, gen, status);
+    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, start, xd_a, xd_b, x_out, lam, pair_id, v, omega,
+                                                   iters, gs, gen, status);
 }
 
 // ----- the whole step in one persistent launch ------------------------------------------------------------
@@ -1073,15 +1098,14 @@ __device__ __forceinline__ uint32_t block_excl_scan_any(uint32_t v, uint32_t* to
 }
 
 struct SortBufs {
-    const float2* x;         // current positions (unsorted order)
+    float2* x;               // current positions (unsorted order); the step's end positions (sorted) replace them
     const float2* v;         // velocities (unsorted order)
     uint2* keyrank;
     uint32_t* count;         // histogram, zero on entry and on exit
     uint32_t* bsum;          // tile totals
     uint32_t* start;         // cell starts (ncells + 1)
     uint32_t* bucket;
-    float2* x_sorted;        // placed x
-    float2* xs_sorted;       // placed x* (the solve's first input)
+    float4* xd_sorted;       // placed (x, d) records (the solve's first input)
     uint32_t* perm;
     uint32_t* keys;
     const uint32_t* id_in;   // ids to carry (or null)
@@ -1093,7 +1117,7 @@ struct SortBufs {
 template <bool MULTI, bool SELFG, bool SCORR, bool XSPH, bool MASKS>
 __global__ void __launch_bounds__(T_MAX)
     k_step_persistent(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
-                      const SortBufs sb, float2* __restrict__ xs_b, float* __restrict__ lam,
+                      const SortBufs sb, float4* __restrict__ xd_b, float* __restrict__ lam,
                       const uint32_t* __restrict__ pair_id, float2* __restrict__ v_out, float* __restrict__ omega,
                       int32_t iters, GridSync* __restrict__ gs, uint32_t* __restrict__ status)
 {
@@ -1167,12 +1191,13 @@ __global__ void __launch_bounds__(T_MAX)
     if (!grid_barrier(gs, gen, status)) { return; }
     // stable placement and gather
     for (int32_t i = i0; i < n; i += stride) {
-        place_one<true>(k, sb.keyrank, sb.start, sb.bucket, sb.x, sb.v, sb.x_sorted, sb.xs_sorted, sb.perm, sb.keys,
-                        sb.id_in, sb.id_out, nullptr, nullptr, nullptr, i);
+        place_one<true>(k, sb.keyrank, sb.start, sb.bucket, sb.x, sb.v, sb.xd_sorted, nullptr, nullptr, sb.perm,
+                        sb.keys, sb.id_in, sb.id_out, nullptr, nullptr, nullptr, i);
     }
+    // (every block has read its unsorted positions before this barrier; XSPH overwrites them later)
     if (!grid_barrier(gs, gen, status)) { return; }
-    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, sb.start, sb.xs_sorted, xs_b, sb.x_sorted, lam,
-                                                   pair_id, v_out, omega, iters, gs, gen, status);
+    solve_phases<MULTI, SELFG, SCORR, XSPH, MASKS>(k, doms, dom, sb.start, sb.xd_sorted, xd_b, sb.x, lam, pair_id,
+                                                   v_out, omega, iters, gs, gen, status);
 }
 
 // ----- density for the density-error metric --------------------------------------------------------------
@@ -1382,7 +1407,7 @@ using namespace gpe;
 
 struct PbfGraph {
     cudaGraphExec_t exec = nullptr;
-    int X_end, id_end;
+    int id_end;
 };
 
 struct gpe_pbf {
@@ -1398,7 +1423,8 @@ struct gpe_pbf {
 
     void* base        = nullptr;
     DomDev* d_doms    = nullptr;
-    float2* pos[4]    = {};
+    float2* pos       = nullptr; // positions between steps (after a step: that step's sorted order)
+    float4* xd[2]     = {};      // within a step: sorted (x, d) records, the current and the next
     float2* vel       = nullptr;
     float* lam        = nullptr;
     float* omega      = nullptr;
@@ -1439,8 +1465,8 @@ struct gpe_pbf {
     int32_t dp_since_build = 0;   // delta p passes since they were made
     int32_t mask_passes = 1;      // delta p passes the move threshold k.move2 allows for
 
-    // buffer roles: X = current x; after PREDICT_SORT: SX = sorted x, XS = current x*, XO = the other x*
-    int X = 0, SX = -1, XS = -1, XO = -1;
+    // within a step (after PREDICT_SORT): XS = the current (x, d) records, XO = the other buffer; -1 between steps
+    int XS = -1, XO = -1;
     int id_cur        = 0;
     bool have_state   = false;
     bool have_sort    = false;
@@ -1610,22 +1636,16 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 {
     s->masks_valid  = false;
     const int32_t n = (int32_t)lsize(s);
-    // roles for this step: the three buffers other than X, in order
-    int fr[3], c = 0;
-    for (int b = 0; b < 4; ++b) {
-        if (b != s->X) { fr[c++] = b; }
-    }
-    s->SX = fr[0];
-    s->XS = fr[1];
-    s->XO = fr[2];
+    s->XS           = 0;
+    s->XO           = 1;
     s->k.n = (int32_t)s->n;
     if (n > 0) {
         if (multi(s)) {
-            k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X], s->vel,
+            k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos, s->vel,
                                                                    s->keyrank, s->count);
         } else {
-            k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos[s->X],
-                                                                    s->vel, s->keyrank, s->count);
+            k_predict_hist<false><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos, s->vel,
+                                                                    s->keyrank, s->count);
         }
         GPE_CHECK_LAUNCH("k_predict_hist");
     }
@@ -1636,8 +1656,8 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     if (rc) { return rc; }
     if (n > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
-        k_place<<<blocks_for(n), T_PART, 0, st>>>(s->k, s->keyrank, s->start, s->bucket, s->pos[s->X], s->vel,
-                                                  s->pos[s->SX], s->pos[s->XS], s->perm, s->keys,
+        k_place<<<blocks_for(n), T_PART, 0, st>>>(s->k, s->keyrank, s->start, s->bucket, s->pos, s->vel,
+                                                  s->xd[s->XS], nullptr, nullptr, s->perm, s->keys,
                                                   ids ? s->ids[s->id_cur] : nullptr,
                                                   ids ? s->ids[s->id_cur ^ 1] : nullptr,
                                                   accumulating(s) ? s->acc : nullptr, s->prev,
@@ -1652,10 +1672,10 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 
 // Template dispatch tables: [multi scene][flag][accumulation mode]
 using LamFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                       const float2*, float*, const uint32_t*, float*, int);
+                       const float4*, float*, const uint32_t*, float*, int);
 template <bool M, bool S, int A>
 cudaError_t lam_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                const uint32_t* start, const float2* xs, float* lam, const uint32_t* pid, float* acc, int mask)
+                const uint32_t* start, const float4* xs, float* lam, const uint32_t* pid, float* acc, int mask)
 {
     if constexpr (A == ACC_PROJ) { // the projected-increment ablation keeps full scans
         k_lambda<M, S, A, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, pid, acc);
@@ -1677,10 +1697,10 @@ const LamFn kLam[2][2][3] = {{GPE_LAM3(false, false), GPE_LAM3(false, true)},
 #undef GPE_LAM3
 
 using DpFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                      const float2*, const float*, float2*, float*, int);
+                      const float4*, const float*, float4*, float*, int);
 template <bool M, bool S, bool A>
 cudaError_t dp_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-               const uint32_t* start, const float2* xs, const float* lam, float2* out, float* acc, int mask)
+               const uint32_t* start, const float4* xs, const float* lam, float4* out, float* acc, int mask)
 {
     if (mask == MASK_USE) {
         k_delta_p<M, S, A, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xs, lam, out, acc);
@@ -1696,45 +1716,45 @@ const DpFn kDp[2][2][2] = {{{dp_launch<false, false, false>, dp_launch<false, fa
                             {dp_launch<true, true, false>, dp_launch<true, true, true>}}};
 
 using FeatFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                        const float2*, const float2*, const float*, const uint32_t*, const MlpDev*, uint16_t*, int);
+                        const float4*, const float*, const uint32_t*, const MlpDev*, uint16_t*, int);
 template <bool M, bool S>
 void feat_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                 const uint32_t* start, const float2* xs, const float2* xo, const float* prev, const uint32_t* pid,
-                 const MlpDev* mlp, uint16_t* feat, int mask)
+                 const uint32_t* start, const float4* xd, const float* prev, const uint32_t* pid, const MlpDev* mlp,
+                 uint16_t* feat, int mask)
 {
     if (mask == MASK_BUILD) {
-        k_lambda_feat<M, S, MASK_BUILD><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+        k_lambda_feat<M, S, MASK_BUILD><<<g, blk, 0, st>>>(k, doms, dom, start, xd, prev, pid, mlp, feat);
     } else {
-        k_lambda_feat<M, S, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, pid, mlp, feat);
+        k_lambda_feat<M, S, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xd, prev, pid, mlp, feat);
     }
 }
 const FeatFn kFeat[2][2] = {{feat_launch<false, false>, feat_launch<false, true>},
                             {feat_launch<true, false>, feat_launch<true, true>}};
 
 using ColFn = void (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                       const float2*, const float2*, const float*, float*, const uint32_t*, const CollectK&);
+                       const float4*, const float*, float*, const uint32_t*, const CollectK&);
 template <bool M, bool S>
 void col_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-                const uint32_t* start, const float2* xs, const float2* xo, const float* prev, float* lam,
-                const uint32_t* pid, const CollectK& col)
+                const uint32_t* start, const float4* xd, const float* prev, float* lam, const uint32_t* pid,
+                const CollectK& col)
 {
-    k_lambda_collect<M, S><<<g, blk, 0, st>>>(k, doms, dom, start, xs, xo, prev, lam, pid, col);
+    k_lambda_collect<M, S><<<g, blk, 0, st>>>(k, doms, dom, start, xd, prev, lam, pid, col);
 }
 const ColFn kCol[2][2] = {{col_launch<false, false>, col_launch<false, true>},
                           {col_launch<true, false>, col_launch<true, true>}};
 
 using XsFn = cudaError_t (*)(unsigned, unsigned, cudaStream_t, const PbfK&, const DomDev*, const int32_t*, const uint32_t*,
-                      const float2*, const float2*, float2*, float*, uint32_t*, int);
+                      const float4*, float2*, float2*, float*, uint32_t*, int);
 template <bool M, bool V>
 cudaError_t xs_launch(unsigned g, unsigned blk, cudaStream_t st, const PbfK& k, const DomDev* doms, const int32_t* dom,
-               const uint32_t* start, const float2* x, const float2* xs, float2* v, float* om, uint32_t* status,
+               const uint32_t* start, const float4* xd, float2* x_out, float2* v, float* om, uint32_t* status,
                int mask)
 {
     if (mask == MASK_USE) {
-        k_xsph<M, V, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+        k_xsph<M, V, MASK_USE><<<g, blk, 0, st>>>(k, doms, dom, start, xd, x_out, v, om, status);
         return cudaGetLastError();
     } else {
-        k_xsph<M, V, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, x, xs, v, om, status);
+        k_xsph<M, V, MASK_OFF><<<g, blk, 0, st>>>(k, doms, dom, start, xd, x_out, v, om, status);
         return cudaGetLastError();
     }
 }
@@ -1762,7 +1782,7 @@ int32_t stage_lambda(gpe_pbf* s, cudaStream_t st, int acc)
         mask = s->masks_valid ? MASK_USE : MASK_BUILD;
     }
     GPE_TRY_CUDA(kLam[multi(s) ? 1 : 0][sg][acc](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
-                                                 s->pos[s->XS], s->lam, pid, s->acc, mask));
+                                                 s->xd[s->XS], s->lam, pid, s->acc, mask));
     if (mask == MASK_BUILD) {
         s->masks_valid    = true;
         s->dp_since_build = 0;
@@ -1785,8 +1805,8 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
         const gpe::MlpDev* md = gpe::mlp_device(s->mlp);
         // the feature pass scans every neighbour on the sorted positions: it makes the step's masks
         const int mask = masks_on(s) ? MASK_BUILD : MASK_OFF;
-        kFeat[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
-                      s->prev, pid, md, s->feat, mask);
+        kFeat[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->xd[s->XS], s->prev, pid,
+                      md, s->feat, mask);
         GPE_CHECK_LAUNCH("k_lambda_feat");
         if (mask == MASK_BUILD) {
             s->masks_valid    = true;
@@ -1798,8 +1818,8 @@ int32_t stage_lambda_warm(gpe_pbf* s, cudaStream_t st)
         GPE_CHECK_LAUNCH("k_mlp_apply");
         s->launches += 1;
     } else {
-        kCol[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->pos[s->XS], s->pos[s->SX],
-                     s->prev, s->lam, pid, s->col);
+        kCol[mi][sg](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start, s->xd[s->XS], s->prev,
+                     s->lam, pid, s->col);
         GPE_CHECK_LAUNCH("k_lambda_collect");
     }
     s->launches += 1;
@@ -1816,8 +1836,8 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
         const int mask = s->masks_valid ? MASK_USE : MASK_OFF;
         s->dp_since_build += 1;
         GPE_TRY_CUDA(kDp[multi(s) ? 1 : 0][sc][accinit ? 1 : 0](nblk(s), (unsigned)s->block, st, s->k, s->d_doms,
-                                                                s->dom, s->start, s->pos[s->XS], s->lam,
-                                                                s->pos[s->XO], s->acc, mask));
+                                                                s->dom, s->start, s->xd[s->XS], s->lam,
+                                                                s->xd[s->XO], s->acc, mask));
         s->launches += 1;
     }
     std::swap(s->XS, s->XO);
@@ -1829,7 +1849,7 @@ int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
     if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
     GPE_TRY_CUDA(kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
-                                             s->pos[s->SX], s->pos[s->XS], s->vel, s->omega, s->status,
+                                             s->xd[s->XS], s->pos, s->vel, s->omega, s->status,
                                              s->masks_valid ? MASK_USE : MASK_OFF));
     s->launches += 1;
     return GPE_OK;
@@ -1843,18 +1863,18 @@ int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
     if (multi(s)) {
         if (mu) {
             k_vorticity<true, MASK_USE><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                         s->pos[s->XS], s->omega, s->vel);
+                                                                         s->xd[s->XS], s->omega, s->vel);
         } else {
             k_vorticity<true, MASK_OFF><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                         s->pos[s->XS], s->omega, s->vel);
+                                                                         s->xd[s->XS], s->omega, s->vel);
         }
     } else {
         if (mu) {
             k_vorticity<false, MASK_USE><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                          s->pos[s->XS], s->omega, s->vel);
+                                                                          s->xd[s->XS], s->omega, s->vel);
         } else {
             k_vorticity<false, MASK_OFF><<<g, (unsigned)s->block, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                          s->pos[s->XS], s->omega, s->vel);
+                                                                          s->xd[s->XS], s->omega, s->vel);
         }
     }
     GPE_CHECK_LAUNCH("k_vorticity");
@@ -1864,9 +1884,9 @@ int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 
 int32_t stage_finish(gpe_pbf* s)
 {
+    // XSPH wrote the step's end positions (sorted) into pos
     s->masks_valid = false;
-    s->X  = s->XS;
-    s->SX = s->XS = s->XO = -1;
+    s->XS = s->XO = -1;
     return GPE_OK;
 }
 
@@ -1917,11 +1937,11 @@ int32_t stage_solve_persistent(gpe_pbf* s, cudaStream_t st)
         }
         const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? s->ids[s->id_cur] : nullptr;
         PbfK k              = s->k;
-        float2* xa          = s->pos[s->XS];
-        float2* xb          = s->pos[s->XO];
-        const float2* xsort = s->pos[s->SX];
+        float4* xa          = s->xd[s->XS];
+        float4* xb          = s->xd[s->XO];
+        float2* xo          = s->pos;
         int32_t iters       = s->prm.iters;
-        void* args[]        = {&k,  &s->d_doms, &s->dom, &s->start, &xa,   &xb,        &xsort,
+        void* args[]        = {&k,  &s->d_doms, &s->dom, &s->start, &xa,   &xb,        &xo,
                                &s->lam, &pid, &s->vel, &s->omega, &iters, &s->gsync, &s->status};
         GPE_TRY_CUDA(cudaMemsetAsync(s->gsync, 0, sizeof(GridSync), st));
         if (masks_on(s)) { GPE_TRY_CUDA(cudaMemsetAsync(s->mflag, 0, (size_t)s->ncells, st)); }
@@ -1957,13 +1977,8 @@ const void* step_kernel_k(bool m, bool sg, bool sc, bool v)
 int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
 {
     s->masks_valid = false;
-    int fr[3], c = 0;
-    for (int b = 0; b < 4; ++b) {
-        if (b != s->X) { fr[c++] = b; }
-    }
-    s->SX  = fr[0];
-    s->XS  = fr[1];
-    s->XO  = fr[2];
+    s->XS  = 0;
+    s->XO  = 1;
     s->k.n = (int32_t)s->n;
     const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
     if (lsize(s) > 0) {
@@ -1977,15 +1992,14 @@ int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
             s->coop_grid = std::max(1, per_sm) * gpe::sm_count();
         }
         SortBufs sb{};
-        sb.x         = s->pos[s->X];
+        sb.x         = s->pos;
         sb.v         = s->vel;
         sb.keyrank   = s->keyrank;
         sb.count     = s->count;
         sb.bsum      = s->bsum;
         sb.start     = s->start;
         sb.bucket    = s->bucket;
-        sb.x_sorted  = s->pos[s->SX];
-        sb.xs_sorted = s->pos[s->XS];
+        sb.xd_sorted = s->xd[s->XS];
         sb.perm      = s->perm;
         sb.keys      = s->keys;
         sb.id_in     = ids ? s->ids[s->id_cur] : nullptr;
@@ -1994,7 +2008,7 @@ int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
         sb.ncells    = (uint32_t)s->ncells;
         const uint32_t* pid = (s->prm.flags & GPE_PBF_PAIR_IDS) ? sb.id_out : nullptr;
         PbfK k              = s->k;
-        float2* xb          = s->pos[s->XO];
+        float4* xb          = s->xd[s->XO];
         int32_t iters       = s->prm.iters;
         void* args[]        = {&k, &s->d_doms, &s->dom, &sb, &xb, &s->lam, &pid, &s->vel, &s->omega, &iters,
                                &s->gsync, &s->status};
@@ -2064,8 +2078,9 @@ int32_t alloc_buffers(gpe_pbf* s)
     const size_t M = (size_t)s->cells_cap; // room for the finest sort grid the tuning may select
     Carver c;
     const size_t o_doms = c.take<DomDev>((size_t)s->nd);
-    size_t o_pos[4];
-    for (int b = 0; b < 4; ++b) { o_pos[b] = c.take<float2>(N); }
+    const size_t o_pos   = c.take<float2>(N);
+    const size_t o_xd0   = c.take<float4>(N);
+    const size_t o_xd1   = c.take<float4>(N);
     const size_t o_vel   = c.take<float2>(N);
     const size_t o_lam   = c.take<float>(N);
     const size_t o_om    = c.take<float>(N);
@@ -2092,7 +2107,9 @@ int32_t alloc_buffers(gpe_pbf* s)
     GPE_TRY_CUDA(cudaMemset(s->base, 0, c.off));
     uint8_t* b = static_cast<uint8_t*>(s->base);
     s->d_doms  = reinterpret_cast<DomDev*>(b + o_doms);
-    for (int q = 0; q < 4; ++q) { s->pos[q] = reinterpret_cast<float2*>(b + o_pos[q]); }
+    s->pos     = reinterpret_cast<float2*>(b + o_pos);
+    s->xd[0]   = reinterpret_cast<float4*>(b + o_xd0);
+    s->xd[1]   = reinterpret_cast<float4*>(b + o_xd1);
     s->vel     = reinterpret_cast<float2*>(b + o_vel);
     s->lam     = reinterpret_cast<float*>(b + o_lam);
     s->omega   = reinterpret_cast<float*>(b + o_om);
@@ -2250,11 +2267,10 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
         }
     }
     cudaStream_t st = as_stream(stream);
-    s->X            = 0;
-    s->SX = s->XS = s->XO = -1;
+    s->XS = s->XO   = -1;
     s->id_cur     = 0;
     if (n > 0) {
-        GPE_TRY_CUDA(cudaMemcpyAsync(s->pos[0], pos, sizeof(float2) * (size_t)n, kind_in(mem), st));
+        GPE_TRY_CUDA(cudaMemcpyAsync(s->pos, pos, sizeof(float2) * (size_t)n, kind_in(mem), st));
         if (vel) {
             GPE_TRY_CUDA(cudaMemcpyAsync(s->vel, vel, sizeof(float2) * (size_t)n, kind_in(mem), st));
         } else {
@@ -2305,7 +2321,7 @@ int32_t gpe_pbf_get_state(gpe_pbf* s, float* pos, float* vel, int32_t* domain_id
     }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
     if (n > 0) {
-        if (pos) { GPE_TRY_CUDA(cudaMemcpyAsync(pos, s->pos[s->X], sizeof(float2) * (size_t)n, kind_out(mem), st)); }
+        if (pos) { GPE_TRY_CUDA(cudaMemcpyAsync(pos, s->pos, sizeof(float2) * (size_t)n, kind_out(mem), st)); }
         if (vel) { GPE_TRY_CUDA(cudaMemcpyAsync(vel, s->vel, sizeof(float2) * (size_t)n, kind_out(mem), st)); }
         if (domain_id) {
             if (s->nd > 1) {
@@ -2363,7 +2379,7 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
         if (--n_steps == 0) { return GPE_OK; }
     }
     // the step sequence is captured once per (steps, starting buffer roles) and replayed as one graph
-    const auto key = std::make_tuple(n_steps, s->X, s->id_cur);
+    const auto key = std::make_tuple(n_steps, 0, s->id_cur);
     auto it        = s->graphs.find(key);
     if (it == s->graphs.end()) {
         cudaStream_t cap_st = st;
@@ -2372,7 +2388,7 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
             GPE_TRY_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
             own = true;
         }
-        const int X0 = s->X, id0 = s->id_cur;
+        const int id0 = s->id_cur;
         GPE_TRY_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
         s->launches = 0;
         int32_t rc  = GPE_OK;
@@ -2380,9 +2396,7 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(cap_st, &graph);
         PbfGraph pg;
-        pg.X_end  = s->X;
         pg.id_end = s->id_cur;
-        s->X      = X0;
         s->id_cur = id0;
         if (rc == GPE_OK && ce != cudaSuccess) {
             gpe::set_cuda_error(ce, "cudaStreamEndCapture");
@@ -2402,7 +2416,6 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
         it = s->graphs.emplace(key, pg).first;
     }
     GPE_TRY_CUDA(cudaGraphLaunch(it->second.exec, st));
-    s->X         = it->second.X_end;
     s->id_cur    = it->second.id_end;
     s->have_sort = true;
     return GPE_OK;
@@ -2414,7 +2427,7 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
     if (!s) { return GPE_ERR_BAD_ARG; }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
     cudaStream_t st = as_stream(stream);
-    const bool in_step = s->SX >= 0;
+    const bool in_step = s->XS >= 0;
     switch (stage) {
         case GPE_PBF_STAGE_PREDICT_SORT:
             if (in_step) { break; }
@@ -2448,10 +2461,10 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
                 s->k.n = (int32_t)s->n;
                 if (multi(s)) {
                     k_density<true><<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                         s->pos[s->X], s->rho, s->red);
+                                                                         s->pos, s->rho, s->red);
                 } else {
                     k_density<false><<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->start,
-                                                                          s->pos[s->X], s->rho, s->red);
+                                                                          s->pos, s->rho, s->red);
                 }
                 GPE_CHECK_LAUNCH("k_density");
             }
@@ -2483,20 +2496,71 @@ int32_t gpe_pbf_density_error(gpe_pbf* s, float* max_err, float* mean_err, void*
     return GPE_OK;
 }
 
-static int32_t field_ptr(gpe_pbf* s, int32_t field, void** p, size_t* esize, int64_t* count)
+// x* = x + d of every record, rounded once (field GPE_PBF_FIELD_PRED)
+__global__ void k_xd_pred(const float4* __restrict__ xd, float2* __restrict__ out, int32_t n)
 {
-    const bool in_step = s->SX >= 0;
-    *count             = s->n;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 a = xd[i];
+        out[i]         = make_float2(__fadd_rn(a.x, a.z), __fadd_rn(a.y, a.w));
+    }
+}
+// a written x*: d = x* - x
+__global__ void k_xd_set_pred(float4* __restrict__ xd, const float2* __restrict__ xs, int32_t n)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 a = xd[i];
+        const float2 q = xs[i];
+        xd[i]          = make_float4(a.x, a.y, __fsub_rn(q.x, a.x), __fsub_rn(q.y, a.y));
+    }
+}
+
+// Within a step, x (POS) and d (DISP) are the halves of the (x, d) records and x* (PRED) is computed from
+// them; field_ptr reports those as their record array with a byte offset and a 16-byte stride.
+struct FieldLoc {
+    void* p;
+    size_t esize;
+    int64_t count;
+    size_t stride; // 0: contiguous
+    int kind;      // 0: plain memory, 1: x* computed from the records
+};
+
+static int32_t field_ptr(gpe_pbf* s, int32_t field, FieldLoc* f)
+{
+    const bool in_step = s->XS >= 0;
+    f->count           = s->n;
+    f->stride          = 0;
+    f->kind            = 0;
+    void** p           = &f->p;
+    size_t* esize      = &f->esize;
     switch (field) {
-        case GPE_PBF_FIELD_POS: *p = s->pos[in_step ? s->SX : s->X]; *esize = 8; break;
+        case GPE_PBF_FIELD_POS:
+            if (in_step) {
+                *p        = s->xd[s->XS];
+                f->stride = sizeof(float4);
+            } else {
+                *p = s->pos;
+            }
+            *esize = 8;
+            break;
+        case GPE_PBF_FIELD_DISP:
+            if (!in_step) { return GPE_ERR_NOT_READY; }
+            *p        = reinterpret_cast<uint8_t*>(s->xd[s->XS]) + sizeof(float2);
+            f->stride = sizeof(float4);
+            *esize    = 8;
+            break;
         case GPE_PBF_FIELD_VEL: *p = s->vel; *esize = 8; break;
         case GPE_PBF_FIELD_PRED:
             if (!in_step) { return GPE_ERR_NOT_READY; }
-            *p = s->pos[s->XS]; *esize = 8; break;
+            *p      = s->xd[s->XS];
+            *esize  = 8;
+            f->kind = 1;
+            break;
         case GPE_PBF_FIELD_LAMBDA: *p = s->lam; *esize = 4; break;
         case GPE_PBF_FIELD_KEY: *p = s->keys; *esize = 4; break;
         case GPE_PBF_FIELD_PERM: *p = s->perm; *esize = 4; break;
-        case GPE_PBF_FIELD_CELL_START: *p = s->start; *esize = 4; *count = (int64_t)s->ncells + 1; break;
+        case GPE_PBF_FIELD_CELL_START: *p = s->start; *esize = 4; f->count = (int64_t)s->ncells + 1; break;
         case GPE_PBF_FIELD_DOMAIN: *p = s->dom; *esize = 4; break;
         case GPE_PBF_FIELD_DENSITY: *p = s->rho; *esize = 4; break;
         case GPE_PBF_FIELD_ID: *p = s->ids[s->id_cur]; *esize = 4; break;
@@ -2514,20 +2578,31 @@ int32_t gpe_pbf_get_field(gpe_pbf* s, int32_t field, void* dst, int64_t n_elems,
     if (!s || !dst || (mem != GPE_MEM_HOST && mem != GPE_MEM_DEVICE)) { return GPE_ERR_BAD_ARG; }
     const int32_t rcn = sync_count(s, as_stream(stream));
     if (rcn) { return rcn; }
-    void* p;
-    size_t es;
-    int64_t cnt;
-    int32_t rc = field_ptr(s, field, &p, &es, &cnt);
+    FieldLoc f{};
+    int32_t rc = field_ptr(s, field, &f);
     if (rc) {
         gpe::set_error(rc, "gpe_pbf_get_field: field %d unavailable", field);
         return rc;
     }
-    if (n_elems != cnt) {
-        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_field: field %d has %lld elements", field, (long long)cnt);
+    if (n_elems != f.count) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_get_field: field %d has %lld elements", field, (long long)f.count);
         return GPE_ERR_BAD_ARG;
     }
     cudaStream_t st = as_stream(stream);
-    if (cnt > 0) { GPE_TRY_CUDA(cudaMemcpyAsync(dst, p, es * (size_t)cnt, kind_out(mem), st)); }
+    const size_t n  = (size_t)f.count;
+    if (n > 0) {
+        if (f.kind == 1) {
+            // x* = x + d into the sort's (key, rank) scratch, which is free within a step, then out
+            float2* tmp = reinterpret_cast<float2*>(s->keyrank);
+            k_xd_pred<<<blocks_for((int64_t)n), T_PART, 0, st>>>(static_cast<const float4*>(f.p), tmp, (int32_t)n);
+            GPE_CHECK_LAUNCH("k_xd_pred");
+            GPE_TRY_CUDA(cudaMemcpyAsync(dst, tmp, sizeof(float2) * n, kind_out(mem), st));
+        } else if (f.stride) {
+            GPE_TRY_CUDA(cudaMemcpy2DAsync(dst, f.esize, f.p, f.stride, f.esize, n, kind_out(mem), st));
+        } else {
+            GPE_TRY_CUDA(cudaMemcpyAsync(dst, f.p, f.esize * n, kind_out(mem), st));
+        }
+    }
     if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
     return GPE_OK;
 }
@@ -2542,14 +2617,25 @@ int32_t gpe_pbf_set_field(gpe_pbf* s, int32_t field, const void* src, int64_t n_
         return GPE_ERR_BAD_ARG;
     }
     s->masks_valid = false; // a written position (or anything else) may move a particle past its masks
-    void* p;
-    size_t es;
-    int64_t cnt;
-    int32_t rc = field_ptr(s, field, &p, &es, &cnt);
+    FieldLoc f{};
+    int32_t rc = field_ptr(s, field, &f);
     if (rc) { return rc; }
-    if (n_elems != cnt) { return GPE_ERR_BAD_ARG; }
+    if (n_elems != f.count) { return GPE_ERR_BAD_ARG; }
     cudaStream_t st = as_stream(stream);
-    if (cnt > 0) { GPE_TRY_CUDA(cudaMemcpyAsync(p, src, es * (size_t)cnt, kind_in(mem), st)); }
+    const size_t n  = (size_t)f.count;
+    if (n > 0) {
+        if (f.kind == 1) {
+            // a new x* keeps x and sets d = x* - x
+            float2* tmp = reinterpret_cast<float2*>(s->keyrank);
+            GPE_TRY_CUDA(cudaMemcpyAsync(tmp, src, sizeof(float2) * n, kind_in(mem), st));
+            k_xd_set_pred<<<blocks_for((int64_t)n), T_PART, 0, st>>>(static_cast<float4*>(f.p), tmp, (int32_t)n);
+            GPE_CHECK_LAUNCH("k_xd_set_pred");
+        } else if (f.stride) {
+            GPE_TRY_CUDA(cudaMemcpy2DAsync(f.p, f.stride, src, f.esize, f.esize, n, kind_in(mem), st));
+        } else {
+            GPE_TRY_CUDA(cudaMemcpyAsync(f.p, src, f.esize * n, kind_in(mem), st));
+        }
+    }
     if (mem == GPE_MEM_HOST) { GPE_TRY_CUDA(cudaStreamSynchronize(st)); }
     if (field == GPE_PBF_FIELD_LAMBDA_SUM) { s->mem_valid = true; } // the caller supplied the memory
     return GPE_OK;
@@ -2620,7 +2706,7 @@ extern "C" int32_t gpe_pbf_emit(gpe_pbf* s, const gpe_hose* hose, uint64_t seed,
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_emit: needs GPE_PBF_DYNAMIC_COUNT and a single scene");
         return GPE_ERR_NOT_READY;
     }
-    if (s->SX >= 0) {
+    if (s->XS >= 0) {
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_emit: a step is in progress (stage API)");
         return GPE_ERR_NOT_READY;
     }
@@ -2635,7 +2721,7 @@ extern "C" int32_t gpe_pbf_emit(gpe_pbf* s, const gpe_hose* hose, uint64_t seed,
     cudaStream_t st = as_stream(stream);
     if (cnt > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
-        k_pbf_emit<<<blocks_for(cnt), T_PART, 0, st>>>(s->k, h, s->pos[s->X], s->vel, s->d_count, (int32_t)s->cap,
+        k_pbf_emit<<<blocks_for(cnt), T_PART, 0, st>>>(s->k, h, s->pos, s->vel, s->d_count, (int32_t)s->cap,
                                                        ids ? s->ids[s->id_cur] : nullptr, s->status);
         GPE_CHECK_LAUNCH("k_pbf_emit");
     }
@@ -2651,7 +2737,7 @@ extern "C" int32_t gpe_pbf_publish(gpe_pbf* s, const gpe_view* view, int32_t vie
                                      view->chunks_y <= 0 || !(view->chunk_dim > 0.f) || view->chunk_capacity <= 0)) {
         return GPE_ERR_BAD_ARG;
     }
-    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (s->XS >= 0) { return GPE_ERR_NOT_READY; }
     cudaStream_t st = as_stream(stream);
     const gpe_view* vp = nullptr;
     gpe_view vv{};
@@ -2665,7 +2751,7 @@ extern "C" int32_t gpe_pbf_publish(gpe_pbf* s, const gpe_view* view, int32_t vie
     }
     if (lsize(s) > 0) {
         k_pbf_publish<<<(unsigned)((lsize(s) + PUB_PER_BLOCK - 1) / PUB_PER_BLOCK), T_PART, 0, st>>>(
-            s->k, vv, vp, s->pos[s->X], s->vel, s->status);
+            s->k, vv, vp, s->pos, s->vel, s->status);
         GPE_CHECK_LAUNCH("k_pbf_publish");
     }
     return GPE_OK;
@@ -2676,27 +2762,23 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
     gpe::clear_error();
     if (!s || n_steps < 0) { return GPE_ERR_BAD_ARG; }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
-    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (s->XS >= 0) { return GPE_ERR_NOT_READY; }
     if (s->warm == GPE_WARM_MLP && !s->mem_valid) {
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_enqueue: run one gpe_pbf_step first to start the multiplier memory");
         return GPE_ERR_NOT_READY;
     }
     cudaStream_t st   = as_stream(stream);
-    const int X0      = s->X;
     const int id0     = s->id_cur;
     int32_t rc        = GPE_OK;
     for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, st); }
     if (rc) { return rc; }
-    // return the buffer roles to where they started, so the recorded sequence can be replayed
+    // return the id buffer role to where it started, so the recorded sequence can be replayed (positions stay
+    // in one buffer: every step writes its end positions where it read its start positions)
     const size_t n = (size_t)lsize(s);
-    if (s->X != X0 && n > 0) {
-        GPE_TRY_CUDA(cudaMemcpyAsync(s->pos[X0], s->pos[s->X], sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
-    }
     if (s->id_cur != id0 && n > 0) {
         GPE_TRY_CUDA(cudaMemcpyAsync(s->ids[id0], s->ids[s->id_cur], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
                                      st));
     }
-    s->X         = X0;
     s->id_cur    = id0;
     s->have_sort = true;
     return GPE_OK;
@@ -2773,7 +2855,7 @@ extern "C" int32_t gpe_pbf_set_tuning(gpe_pbf* s, const gpe_pbf_tuning* t)
 {
     gpe::clear_error();
     if (!s || !t) { return GPE_ERR_BAD_ARG; }
-    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (s->XS >= 0) { return GPE_ERR_NOT_READY; }
     return apply_tuning(s, *t);
 }
 
@@ -2782,7 +2864,7 @@ extern "C" int32_t gpe_pbf_autotune(gpe_pbf* s, int32_t trial_steps, gpe_pbf_tun
 {
     gpe::clear_error();
     if (!s || trial_steps < 1) { return GPE_ERR_BAD_ARG; }
-    if (!s->have_state || s->SX >= 0 || s->warm != GPE_WARM_NONE || s->dynamic) {
+    if (!s->have_state || s->XS >= 0 || s->warm != GPE_WARM_NONE || s->dynamic) {
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_autotune: needs a state, GPE_WARM_NONE and a host particle count");
         return GPE_ERR_NOT_READY;
     }
@@ -2904,7 +2986,7 @@ extern "C" int32_t gpe_pbf_set_warm_start(gpe_pbf* s, int32_t mode, const gpe_ml
     if (!s || mode < GPE_WARM_NONE || mode > GPE_WARM_MLP || (mode == GPE_WARM_MLP && !mlp)) {
         return GPE_ERR_BAD_ARG;
     }
-    if (s->SX >= 0) { return GPE_ERR_NOT_READY; }
+    if (s->XS >= 0) { return GPE_ERR_NOT_READY; }
     if (mode == GPE_WARM_MLP) {
         // the network kernel's tiles live in shared memory: prefer the largest carveout so that 6 CTAs fit
         GPE_TRY_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k_mlp_apply),
@@ -2934,7 +3016,7 @@ extern "C" int32_t gpe_mlp_collect(gpe_mlp* m, gpe_pbf* s, int32_t n_steps, int3
     gpe::clear_error();
     if (!m || !s || n_steps < 0 || stride < 1) { return GPE_ERR_BAD_ARG; }
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
-    if (s->warm != GPE_WARM_NONE || s->SX >= 0) {
+    if (s->warm != GPE_WARM_NONE || s->XS >= 0) {
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_mlp_collect: the engine must be in GPE_WARM_NONE between steps");
         return GPE_ERR_NOT_READY;
     }
@@ -3109,7 +3191,7 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
         if (rc) { return rc; }
         k_place<<<blocks_for(n), T_PART, 0, st>>>(k, keyrank, cell_start, bucket,
                                                   reinterpret_cast<const float2*>(pos),
-                                                  reinterpret_cast<const float2*>(vel),
+                                                  reinterpret_cast<const float2*>(vel), nullptr,
                                                   reinterpret_cast<float2*>(pos_sorted),
                                                   reinterpret_cast<float2*>(pred_sorted), perm, key_sorted, nullptr,
                                                   nullptr, nullptr, nullptr, nullptr);

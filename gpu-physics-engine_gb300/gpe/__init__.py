@@ -24,7 +24,7 @@ PBF_SELF_GRAD, PBF_VEL_CLAMP, PBF_TRACK_IDS, PBF_PAIR_IDS, PBF_DYNAMIC_COUNT = 0
  PBF_STAGE_FINISH, PBF_STAGE_DENSITY, PBF_STAGE_WARM_LAMBDA) = range(8)
 (PBF_FIELD_POS, PBF_FIELD_VEL, PBF_FIELD_PRED, PBF_FIELD_LAMBDA, PBF_FIELD_KEY, PBF_FIELD_PERM,
  PBF_FIELD_CELL_START, PBF_FIELD_DOMAIN, PBF_FIELD_DENSITY, PBF_FIELD_ID, PBF_FIELD_OMEGA,
- PBF_FIELD_LAMBDA_PREV, PBF_FIELD_LAMBDA_SUM) = range(13)
+ PBF_FIELD_LAMBDA_PREV, PBF_FIELD_LAMBDA_SUM, PBF_FIELD_DISP) = range(14)
 WARM_NONE, WARM_PREV, WARM_MLP = 0, 1, 2
 MLP_FEATURES, MLP_HIDDEN, MLP_NUM_WEIGHTS, MLP_BLOB_FLOATS = 12, 64, 5057, 5083
 
@@ -266,7 +266,8 @@ _FIELD_DT = {PBF_FIELD_POS: (np.float32, 2), PBF_FIELD_VEL: (np.float32, 2), PBF
              PBF_FIELD_LAMBDA: (np.float32, 1), PBF_FIELD_KEY: (np.uint32, 1), PBF_FIELD_PERM: (np.uint32, 1),
              PBF_FIELD_CELL_START: (np.uint32, 1), PBF_FIELD_DOMAIN: (np.int32, 1),
              PBF_FIELD_DENSITY: (np.float32, 1), PBF_FIELD_ID: (np.uint32, 1), PBF_FIELD_OMEGA: (np.float32, 1),
-             PBF_FIELD_LAMBDA_PREV: (np.float32, 1), PBF_FIELD_LAMBDA_SUM: (np.float32, 1)}
+             PBF_FIELD_LAMBDA_PREV: (np.float32, 1), PBF_FIELD_LAMBDA_SUM: (np.float32, 1),
+             PBF_FIELD_DISP: (np.float32, 2)}
 
 
 class Pbf:

@@ -135,6 +135,10 @@ typedef struct gpe_pbf gpe_pbf;
 #define GPE_PBF_FIELD_OMEGA 10     /* vorticity from the last XSPH stage [float]           */
 #define GPE_PBF_FIELD_LAMBDA_PREV 11 /* previous step's summed multiplier, sorted [float]   */
 #define GPE_PBF_FIELD_LAMBDA_SUM 12  /* this step's summed multiplier so far [float]        */
+#define GPE_PBF_FIELD_DISP 13      /* d = x* - x within a step [float2]: a step holds each particle as its start
+                                      position x (POS) and its displacement d, so that neighbour offsets and
+                                      velocities d / dt keep FP32 precision at any coordinate magnitude; PRED
+                                      is x + d rounded once                                                      */
 
 int32_t gpe_pbf_create(const gpe_pbf_params* params, const gpe_domain* domains, int32_t n_domains,
                        int64_t capacity, gpe_pbf** out);

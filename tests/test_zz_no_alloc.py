@@ -28,7 +28,7 @@ def _engine_stage(gpe_mod, p, pos, vel, box):
     e = gpe_mod.Pbf(p, [box], capacity=len(pos))
     e.set_state(pos, vel)
     e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
-    out = {"pos": e.field(gpe_mod.PBF_FIELD_POS), "pred": e.field(gpe_mod.PBF_FIELD_PRED),
+    out = {"pos": e.field(gpe_mod.PBF_FIELD_POS), "disp": e.field(gpe_mod.PBF_FIELD_DISP),
            "key": e.field(gpe_mod.PBF_FIELD_KEY), "perm": e.field(gpe_mod.PBF_FIELD_PERM),
            "cell_start": e.field(gpe_mod.PBF_FIELD_CELL_START)}
     n_cells = e.num_cells
@@ -73,8 +73,10 @@ def test_noalloc_sort_matches_stage_twice(gpe_mod, cuda_ok):
         got = _noalloc(gpe_mod, p, pos, vel, box, n_cells)
         for k in ("key", "perm", "cell_start"):
             assert np.array_equal(got[k], want[k]), f"{k} differs (scene {seed})"
-        for k in ("pos", "pred"):
-            assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), f"{k} differs (scene {seed})"
+        assert np.array_equal(got["pos"].view(np.uint32), want["pos"].view(np.uint32)), f"pos differs (scene {seed})"
+        # the engine's step holds x and d = x* - x: the FP32 difference of the no-alloc sort's x* and x
+        disp = (got["pred"] - got["pos"]).astype(np.float32)
+        assert np.array_equal(disp.view(np.uint32), want["disp"].view(np.uint32)), f"x* differs (scene {seed})"
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpe_mod, cuda_ok):
