@@ -477,11 +477,35 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         }
         return r2 < k.skin2;
     };
-    const bool self_masked = scan_ld2<MASK, CG>(
-        d, k, start, p.x, p.y, i, [&](uint32_t j) { return ldn<CG>(&xd[j]); },
-        [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::true_type{}); },
-        [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::false_type{}); });
-    self_seen = self_seen || self_masked;
+    auto ld   = [&](uint32_t j) { return ldn<CG>(&xd[j]); };
+    auto full = [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::true_type{}); };
+    auto near = [&](uint32_t j, const float4 q) -> bool { return body(j, q, std::false_type{}); };
+    if constexpr (MASK == MASK_BUILD) {
+        // Record the masks with a distance-only scan of the 3 x 3 cells, then apply the lambda terms to the
+        // recorded candidates alone (their loads hit L1): the same terms in the same order as the full
+        // scan, whose other candidates (beyond h, or the particle itself) add exact zeros.
+        const int32_t bx   = cell_coord(p.x, d.ox, k.inv_cell, d.ncx);
+        const int32_t by   = cell_coord(p.y, d.oy, k.inv_cell, d.ncy);
+        const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
+        bool seen          = false;
+        uint4 m            = scan_build(d, start, bx, by, i, [&](uint32_t j) -> bool {
+            const float2 r = offset(px, pd, ld(j));
+            seen           = seen || (j == (uint32_t)i);
+            return fmaf(r.x, r.x, r.y * r.y) < k.skin2;
+        });
+        const bool fits = !(m.x & MASK_BAD); // no row held more candidates than a mask word
+        if (key != __ldg(&k.keys[i])) { m.x |= MASK_BAD; } // built around another cell than the sort cell
+        k.nmask[i] = m;
+        if (fits) {
+            scan_masked(d, start, bx, by, m, ld, near);
+            self_seen = seen;
+        } else {
+            for_neighbours_at(d, k, start, bx, by, [&](uint32_t j) { full(j, ld(j)); });
+        }
+    } else {
+        const bool self_masked = scan_ld2<MASK, CG>(d, k, start, p.x, p.y, i, ld, full, near);
+        self_seen              = self_seen || self_masked;
+    }
     if (self_seen) {
         s6 = fmaf(k.h2 * k.h2, k.h2, s6);
         if (SELFG) {
@@ -513,9 +537,9 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
     }
 }
 
-// the mask pass in 32 registers, the masked passes in 40
+// the mask-recording pass in 40 registers (3 blocks of 512 per SM), the masked passes in 32
 template <bool MULTI, bool SELFG, int ACC, int MASK>
-__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 4 : (MASK == MASK_USE ? 4 : 1))
+__global__ void __launch_bounds__(T_MAX, (MASK == MASK_BUILD && !SELFG) ? 3 : (MASK == MASK_USE ? 4 : 1))
     k_lambda(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
              const uint32_t* __restrict__ start, const float4* __restrict__ xd, float* __restrict__ lam,
              const uint32_t* __restrict__ pair_id, float* __restrict__ acc)
