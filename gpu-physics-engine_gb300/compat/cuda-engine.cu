@@ -262,7 +262,8 @@ void MPMTickStaging::torusUpload(cudaStream_t stream)
 
 PBFArena::PBFArena()
 {
-    // the reference's arena (cuda-engine.cpp:102-139), kept for code that touches its members
+    // the reference's arena (cuda-engine.cpp:102-139): the chunk-major state is written at the end of every
+    // tick; the migration queues and halos are allocated for code that touches them (the engine has neither)
     const size_t offs   = align128((size_t)kNumChunks * kCellsPerChunk * sizeof(uint32_t));
     const size_t inner2 = align128((size_t)kNumChunks * kMaxAtoms * sizeof(float2));
     const size_t inner1 = align128((size_t)kNumChunks * kMaxAtoms * sizeof(float));
@@ -312,9 +313,24 @@ void instantiatePBFGraph(GraphEnv& g, PBFArena& pbf)
     make_tick_env(g);
     gpe_view* target = nullptr;
     CUDACHECK(cudaGetSymbolAddress((void**)&target, g_pbf_view));
+    // the arena's chunk-major members mirror the engine's state at the end of every tick, as the reference's
+    // arena holds it after its last substep's prepNextSubstepKernel (PBF.cu:786-833)
+    gpe_chunk_state arena{};
+    arena.pos            = reinterpret_cast<float*>(pbf.pos[0]);
+    arena.pred           = reinterpret_cast<float*>(pbf.pos[1]);
+    arena.vel            = reinterpret_cast<float*>(pbf.vel);
+    arena.lambda         = pbf.lambda;
+    arena.counts         = pbf.num_atoms;
+    arena.offsets        = pbf.offsets;
+    arena.chunks_x       = kSceneDimX;
+    arena.chunks_y       = kSceneDimY;
+    arena.chunk_cells    = kGridDim;
+    arena.chunk_dim      = kChunkDim;
+    arena.chunk_capacity = kMaxAtoms;
     CUDACHECK(cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal));
     must(gpe_pbf_enqueue(pbf.engine(), kNumSteps, g.stream), "gpe_pbf_enqueue");
     must(gpe_pbf_publish(pbf.engine(), target, GPE_MEM_DEVICE, g.stream), "gpe_pbf_publish");
+    must(gpe_pbf_publish_chunks(pbf.engine(), &arena, g.stream), "gpe_pbf_publish_chunks");
     CUDACHECK(cudaStreamEndCapture(g.stream, &g.graph));
     CUDACHECK(cudaGraphInstantiate(&g.exec, g.graph, 0));
 }

@@ -6,10 +6,14 @@
 // Types, members and function signatures are the reference's, because drivers use them directly
 // (pbf.halo_offsets, g.stream, g.exec, ...). What differs is behind them:
 //   * PBFArena / MPMArena own a gpe_pbf / gpe_mpm engine. The live particle state is the engine's
-//     (scene-wide sorted arrays for PBF, flat arrays for MPM); the chunk-major PBF arrays of the reference
-//     (offsets, pos, vel, lambda, num_atoms, migration queues, halos) are allocated with the reference's
-//     sizes so that drivers can keep touching them, but the engine neither reads nor writes them.
-//     MPMArena's pos/vel/C/F/J/num_points point at the engine's own arrays.
+//     (scene-wide sorted arrays for PBF, flat arrays for MPM). PBFArena's chunk-major members offsets,
+//     pos[0], pos[1], vel, lambda and num_atoms are written at the end of every tick with the state in the
+//     reference's layout (gpe_pbf_publish_chunks): each atom in the chunk of its next prediction, chunk-local
+//     coordinates, cells packed as (end << 16) | start. The migration queues and halos are allocated with the
+//     reference's sizes for code that touches them; the engine has neither (one scene-wide sort replaces
+//     them). MPMArena's pos/vel/C/F/J/num_points point at the engine's own arrays; num_points[0] is the live
+//     count and num_points[1] the count at the last publish, set by the publish as MPMOutputKernel does
+//     (MPM.cu:317).
 //   * instantiate*Graph records one tick — kNumSteps PBF substeps (kSubsteps MPM substeps) and the publish
 //     into the current output target — into g.graph, and instantiates g.exec, as the reference does.
 //   * hosePipe appends particles on the device (gpe_*_emit) instead of going through migration queues.

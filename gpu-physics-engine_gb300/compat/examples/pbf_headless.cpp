@@ -1,12 +1,14 @@
 // pbf_headless — the reference's PBF driver loop (main/PBF-master.cpp:33-122) without the window thread,
 // written against cuda-engine.h: emit with the hose pipe until TARGET_COUNT atoms, launch one tick graph per
 // iteration, roll the triple-buffered output and report the tick times. Ends by checking that the last
-// published output holds every atom of the engine, inside the scene. Exit status 0 on success.
+// published output holds every atom of the engine, inside the scene, and that the arena's own chunk-major
+// members hold them too, each in the chunk and cell of its prediction. Exit status 0 on success.
 //   usage: pbf_headless [ticks]
 #include <cuda_runtime_api.h>
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
 #include <vector>
 
@@ -74,12 +76,42 @@ int main(int argc, char** argv)
             outside += ok ? 0 : 1;
         }
     }
+    // the arena's own members after the last tick: every atom in the chunk and cell of its prediction pos[1]
+    // (chunk-local), per cell the packed range (end << 16) | start, and x* - x the displacement vel + gravity
+    std::vector<int32_t> na(kNumChunks);
+    std::vector<uint32_t> offs((size_t)kNumChunks * kCellsPerChunk);
+    std::vector<float2> p0((size_t)kNumChunks * kMaxAtoms), p1(p0.size()), v0(p0.size());
+    CUDACHECK(cudaMemcpy(na.data(), pbf.num_atoms, sizeof(int32_t) * na.size(), cudaMemcpyDeviceToHost));
+    CUDACHECK(cudaMemcpy(offs.data(), pbf.offsets, sizeof(uint32_t) * offs.size(), cudaMemcpyDeviceToHost));
+    CUDACHECK(cudaMemcpy(p0.data(), pbf.pos[0], sizeof(float2) * p0.size(), cudaMemcpyDeviceToHost));
+    CUDACHECK(cudaMemcpy(p1.data(), pbf.pos[1], sizeof(float2) * p1.size(), cudaMemcpyDeviceToHost));
+    CUDACHECK(cudaMemcpy(v0.data(), pbf.vel, sizeof(float2) * v0.size(), cudaMemcpyDeviceToHost));
+    int64_t arena_atoms = 0, arena_bad = 0;
+    for (int c = 0; c < kNumChunks; ++c) {
+        arena_atoms += na[(size_t)c];
+        uint32_t expect = 0;
+        for (int cell = 0; cell < kCellsPerChunk; ++cell) {
+            const uint32_t o = offs[(size_t)c * kCellsPerChunk + cell], st = o & 0xFFFFu, en = o >> 16;
+            arena_bad += (st != expect || en < st) ? 1 : 0;
+            expect = en;
+            for (uint32_t a = st; a < en && a < (uint32_t)kMaxAtoms; ++a) {
+                const size_t q = (size_t)c * kMaxAtoms + a;
+                const int gx   = std::min(std::max((int)std::floor(p1[q].x) / kCellDim, 0), kGridDim - 1);
+                const int gy   = std::min(std::max((int)std::floor(p1[q].y) / kCellDim, 0), kGridDim - 1);
+                const float dx = p1[q].x - p0[q].x - v0[q].x, dy = p1[q].y - p0[q].y - v0[q].y;
+                arena_bad += (gx + gy * kGridDim != cell || std::fabs(dx) > 1e-3f || std::fabs(dy) > 1e-2f) ? 1 : 0;
+            }
+        }
+        arena_bad += expect != (uint32_t)na[(size_t)c] ? 1 : 0;
+    }
     uint32_t status = 0;
     gpe_pbf_status(pbf.engine(), &status, nullptr);
     std::printf("{\"ticks\": %d, \"requested\": %d, \"engine_atoms\": %lld, \"published\": %lld, \"misplaced\": %lld, "
+                "\"arena_atoms\": %lld, \"arena_inconsistent\": %lld, "
                 "\"status\": %u, \"avg_tick_ms\": %.4f, \"longest_tick_ms\": %.4f}\n",
-                ticks, atoms, (long long)engine_n, (long long)published, (long long)outside, status,
-                ticks > 1 ? total_ms / (float)(ticks - 1) : 0.f, longest);
-    const bool ok = engine_n > 0 && published == engine_n && outside == 0 && engine_n <= atoms && status == 0;
+                ticks, atoms, (long long)engine_n, (long long)published, (long long)outside, (long long)arena_atoms,
+                (long long)arena_bad, status, ticks > 1 ? total_ms / (float)(ticks - 1) : 0.f, longest);
+    const bool ok = engine_n > 0 && published == engine_n && outside == 0 && engine_n <= atoms && status == 0 &&
+                    arena_atoms == engine_n && arena_bad == 0;
     return ok ? 0 : 1;
 }

@@ -1413,6 +1413,107 @@ __global__ void __launch_bounds__(T_PART)
     }
 }
 
+// ----- chunk-major state, the reference's PBFArena layout (gpe_pbf_publish_chunks) ---------------------
+// After a step the reference's arena holds, per chunk of the scene, its atoms sorted by the cell of their
+// next prediction (prepNextSubstepKernel, PBF.cu:786-833): x and x* in chunk-local coordinates, the
+// displacement, and per cell the packed range (end << 16) | start (PBF.cu:814-817). An atom belongs to the
+// chunk of its prediction (migration, PBF.cu:639-737); within a cell the order follows atomics, as there.
+// The cell histogram is accumulated in the caller's offsets array, which the scan then overwrites.
+__device__ __forceinline__ int32_t chunk_cell_key(const PbfK& k, const gpe_chunk_state& c, float2 xs, int32_t* chunk,
+                                                  float2* org)
+{
+    const float inv  = 1.f / c.chunk_dim;
+    const int32_t cx = min(max((int32_t)floorf((xs.x - k.d0.ox) * inv), 0), c.chunks_x - 1);
+    const int32_t cy = min(max((int32_t)floorf((xs.y - k.d0.oy) * inv), 0), c.chunks_y - 1);
+    *org             = make_float2(k.d0.ox + (float)cx * c.chunk_dim, k.d0.oy + (float)cy * c.chunk_dim);
+    const float cell = c.chunk_dim / (float)c.chunk_cells;
+    const int32_t gx = min(max((int32_t)floorf((xs.x - org->x) / cell), 0), c.chunk_cells - 1);
+    const int32_t gy = min(max((int32_t)floorf((xs.y - org->y) / cell), 0), c.chunk_cells - 1);
+    *chunk           = cx + cy * c.chunks_x;
+    return *chunk * c.chunk_cells * c.chunk_cells + gx + gy * c.chunk_cells;
+}
+
+__global__ void __launch_bounds__(T_PART)
+    k_chunk_hist(const PbfK k, const gpe_chunk_state c, const float2* __restrict__ x, const float2* __restrict__ v,
+                 uint2* __restrict__ keyrank)
+{
+    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < count_of(k);
+    int32_t key      = -1;
+    if (valid) {
+        int32_t ch;
+        float2 org;
+        key = chunk_cell_key(k, c, predict(k, x[i], v[i]), &ch, &org);
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const int32_t leader = __ffs(peers) - 1;
+    const int32_t lane   = threadIdx.x & 31;
+    uint32_t base        = 0;
+    if (valid && lane == leader) { base = atomicAdd(&c.offsets[key], (uint32_t)__popc(peers)); }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) { keyrank[i] = make_uint2((uint32_t)key, base + (uint32_t)__popc(peers & ((1u << lane) - 1u))); }
+}
+
+// one block of 1024 threads per chunk: the cell counts become packed (end << 16) | start, capped at the
+// chunk capacity
+__global__ void __launch_bounds__(1024) k_chunk_scan(const gpe_chunk_state c, uint32_t* __restrict__ status)
+{
+    const int32_t cells = c.chunk_cells * c.chunk_cells;
+    __shared__ uint32_t s_warp[32];
+    uint32_t* off    = c.offsets + (size_t)blockIdx.x * (size_t)cells;
+    const uint32_t v = (int32_t)threadIdx.x < cells ? off[threadIdx.x] : 0u;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) { inc += t; }
+    }
+    if (lane == 31) { s_warp[warp] = inc; }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) { w += t; }
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t end   = inc + (warp ? s_warp[warp - 1] : 0u);
+    const uint32_t start = end - v;
+    const uint32_t cap   = (uint32_t)c.chunk_capacity;
+    if ((int32_t)threadIdx.x < cells) { off[threadIdx.x] = (min(end, cap) << 16) | min(start, cap); }
+    if ((int32_t)threadIdx.x == cells - 1) {
+        c.counts[blockIdx.x] = (int32_t)min(end, cap);
+        if (end > cap) { atomicOr(status, GPE_STATUS_CAPACITY); }
+    }
+}
+
+__global__ void __launch_bounds__(T_PART)
+    k_chunk_place(const PbfK k, const gpe_chunk_state c, const float2* __restrict__ x, const float2* __restrict__ v,
+                  const float* __restrict__ lam, const uint2* __restrict__ keyrank)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count_of(k)) { return; }
+    const float2 p  = x[i];
+    const float2 w  = v[i];
+    const float2 xs = predict(k, p, w);
+    int32_t ch;
+    float2 org;
+    (void)chunk_cell_key(k, c, xs, &ch, &org);
+    const uint2 kr     = keyrank[i];
+    const uint32_t o   = c.offsets[kr.x];
+    const uint32_t sl  = (o & 0xFFFFu) + kr.y;
+    if (sl >= (o >> 16)) { return; } // past the chunk's capacity (reported by the scan)
+    const size_t q                        = (size_t)ch * (size_t)c.chunk_capacity + sl;
+    reinterpret_cast<float2*>(c.pos)[q]   = make_float2(p.x - org.x, p.y - org.y);
+    reinterpret_cast<float2*>(c.pred)[q]  = make_float2(xs.x - org.x, xs.y - org.y);
+    reinterpret_cast<float2*>(c.vel)[q]   = w;
+    if (c.lambda) { c.lambda[q] = lam[i]; }
+}
+
 __global__ void k_iota(uint32_t* __restrict__ a, int32_t n)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2777,6 +2878,39 @@ extern "C" int32_t gpe_pbf_publish(gpe_pbf* s, const gpe_view* view, int32_t vie
         k_pbf_publish<<<(unsigned)((lsize(s) + PUB_PER_BLOCK - 1) / PUB_PER_BLOCK), T_PART, 0, st>>>(
             s->k, vv, vp, s->pos, s->vel, s->status);
         GPE_CHECK_LAUNCH("k_pbf_publish");
+    }
+    return GPE_OK;
+}
+
+extern "C" int32_t gpe_pbf_publish_chunks(gpe_pbf* s, const gpe_chunk_state* state, void* stream)
+{
+    gpe::clear_error();
+    if (!s || !state) { return GPE_ERR_BAD_ARG; }
+    if (s->nd != 1 || s->XS >= 0) {
+        gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_publish_chunks: needs one scene, between steps");
+        return GPE_ERR_NOT_READY;
+    }
+    const gpe_chunk_state c = *state;
+    if (!c.pos || !c.pred || !c.vel || !c.counts || !c.offsets || c.chunks_x < 1 || c.chunks_y < 1 ||
+        c.chunk_cells < 1 || c.chunk_cells > 32 || !(c.chunk_dim > 0.f) || c.chunk_capacity < 1 ||
+        c.chunk_capacity > 0xFFFF) {
+        gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_publish_chunks: bad chunk state (null array, more than 32 x 32 "
+                                        "cells or 65535 slots per chunk)");
+        return GPE_ERR_BAD_ARG;
+    }
+    cudaStream_t st     = as_stream(stream);
+    const size_t chunks = (size_t)c.chunks_x * (size_t)c.chunks_y;
+    GPE_TRY_CUDA(cudaMemsetAsync(c.offsets, 0, sizeof(uint32_t) * chunks * (size_t)(c.chunk_cells * c.chunk_cells), st));
+    const int64_t n = lsize(s);
+    if (n > 0) {
+        k_chunk_hist<<<blocks_for(n), T_PART, 0, st>>>(s->k, c, s->pos, s->vel, s->keyrank);
+        GPE_CHECK_LAUNCH("k_chunk_hist");
+    }
+    k_chunk_scan<<<(unsigned)chunks, 1024, 0, st>>>(c, s->status);
+    GPE_CHECK_LAUNCH("k_chunk_scan");
+    if (n > 0) {
+        k_chunk_place<<<blocks_for(n), T_PART, 0, st>>>(s->k, c, s->pos, s->vel, s->lam, s->keyrank);
+        GPE_CHECK_LAUNCH("k_chunk_place");
     }
     return GPE_OK;
 }

@@ -207,6 +207,30 @@ int32_t gpe_pbf_emit(gpe_pbf* pbf, const gpe_hose* hose, uint64_t seed, int32_t*
  * when they run, so a captured graph follows later updates of the struct, as the reference's __constant__
  * c_output does, PBF.cu:29 and TickStaging::outputTargetUpload, PBF.cu:50-55). */
 int32_t gpe_pbf_publish(gpe_pbf* pbf, const gpe_view* view, int32_t view_mem, void* stream);
+/* The engine's state in the reference's chunk-major arena layout (PBFArena, cuda-engine.h:124-161, as
+ * prepNextSubstepKernel leaves it, PBF.cu:786-833): every particle in the chunk of its next prediction
+ * x* = x + dt v + dt^2 g, chunk-local x (pos, the arena's pos[0]) and x* (pred, pos[1]), v (vel; the per-step
+ * displacement when dt = 1), the last Jacobi multiplier (lambda, may be NULL), particles per chunk (counts,
+ * num_atoms) and per cell of a chunk's chunk_cells x chunk_cells grid the packed slot range
+ * (end << 16) | start of the particles whose prediction lies in it (offsets, chunk-major, row-major cells).
+ * Within a cell the order follows atomics, as in the reference; particles beyond a chunk's capacity are left
+ * out and GPE_STATUS_CAPACITY is set. */
+typedef struct gpe_chunk_state {
+    float* pos;         /* float2[chunks * chunk_capacity]  */
+    float* pred;        /* float2[chunks * chunk_capacity]  */
+    float* vel;         /* float2[chunks * chunk_capacity]  */
+    float* lambda;      /* float[chunks * chunk_capacity]   */
+    int32_t* counts;    /* int32[chunks]                    */
+    uint32_t* offsets;  /* uint32[chunks * chunk_cells^2]   */
+    int32_t chunks_x, chunks_y;
+    int32_t chunk_cells;    /* cells along a chunk edge, at most 32 (kGridDim, constants.h:45) */
+    float chunk_dim;        /* chunk edge (kChunkDim, constants.h:48)                          */
+    int32_t chunk_capacity; /* slots per chunk, at most 65535 (kMaxAtoms, constants.h:50)      */
+} gpe_chunk_state;
+/* Writes the state between steps (one scene). The struct is read when the call is made; its arrays are device
+ * memory (the reference's arena members), written when the work runs, so the call can be recorded into a
+ * graph. */
+int32_t gpe_pbf_publish_chunks(gpe_pbf* pbf, const gpe_chunk_state* state, void* stream);
 /* Issues n_steps steps on the stream without an engine-owned graph, so that they can be recorded into the
  * caller's own stream capture (the reference's instantiatePBFGraph builds one graph per tick, PBF.cu:901-961).
  * Buffer roles are returned to their starting state at the end, so a captured sequence can be replayed. */

@@ -342,3 +342,5 @@ def test_compat_headless_loop(gpe_mod, cuda_ok, prog):
     assert r.returncode == 0, r.stdout + r.stderr
     out = json.loads(r.stdout.strip().splitlines()[-1])
     assert out["published"] > 0 and out["misplaced"] == 0
+    if prog == "pbf_headless":  # the arena's chunk-major members are live
+        assert out["arena_atoms"] == out["engine_atoms"] and out["arena_inconsistent"] == 0
