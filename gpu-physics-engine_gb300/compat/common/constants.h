@@ -58,6 +58,11 @@ constexpr int32_t kCellsPerChunk = kGridDim * kGridDim;
 constexpr int32_t kHaloCells     = 4 * kGridDim + 4;
 constexpr int32_t kHaloAtoms     = kHaloCells * kCellSlots;
 
+// Renderer (the splat rasteriser's image: kSimScale pixels per scene unit)
+constexpr float kSimScale    = 5.f;
+constexpr size_t kDispWidth  = (size_t)((float)kSceneDimX * kChunkDim * kSimScale);
+constexpr size_t kDispHeight = (size_t)((float)kSceneDimY * kChunkDim * kSimScale);
+
 // MLS-MPM
 constexpr int32_t kSubsteps   = 20;
 constexpr size_t kSimWidth    = (size_t)(kSceneDimX * (int32_t)kChunkDim);

@@ -98,6 +98,34 @@ def reference_border_band(chunk=(5, 2), speed: float = 1.0, seed: int = 31, box=
     return pos.astype(F32), vel.astype(F32), [box]
 
 
+def reference_render_view(seed: int = 41, chunks_x: int = 12, chunks_y: int = 6, capacity: int = 1536,
+                          visible=(3, 2), stack: int = 6):
+    """A chunk-major view (the reference's View: chunks_x x chunks_y chunks of `capacity` slots, absolute
+    coordinates, reference units) whose image the reference's own drawKernel (cuda-render.cu:259-310) draws
+    deterministically: every pixel is written by one thread only. In each of the first visible[0] x visible[1]
+    chunks, atoms 0..195 sit on a 14 x 14 lattice 2 units (10 pixels at scale 5) apart, 28 more on the chunk's
+    left and bottom edges (their splats cover the black chunk lines), and atom a + 256 k (k < stack) on top of
+    atom a, a little offset: drawKernel's thread a draws those in order, so stacked splats blend sequentially.
+    Splats of different lattice points never overlap; slots 224..255 of every 256 hold atoms outside the
+    image, which draw nothing. Chunk counts are seeded; the other chunks are empty.
+    Returns (pos [chunks, capacity, 2] float32, counts [chunks] int32)."""
+    g = rng(seed)
+    pos = np.full((chunks_x * chunks_y, capacity, 2), -50.0, F32)
+    counts = np.zeros(chunks_x * chunks_y, np.int32)
+    base = [(3.0 + 2 * i, 3.0 + 2 * j) for j in range(14) for i in range(14)]
+    base += [(0.2, 3.0 + 2 * j) for j in range(14)] + [(3.0 + 2 * i, 0.2) for i in range(14)]
+    base = np.array(base)  # 224 points, chunk-local
+    for cy in range(visible[1]):
+        for cx in range(visible[0]):
+            c = cx + cy * chunks_x
+            org = np.array([cx * 32.0, cy * 32.0])
+            for k in range(stack):
+                jit = g.uniform(-0.1, 0.1, base.shape) if k == 0 else g.uniform(-0.3, 0.3, base.shape)
+                pos[c, 256 * k:256 * k + len(base)] = org + base + jit
+            counts[c] = int(g.integers(200, min(capacity, 256 * stack) + 1))
+    return pos, counts
+
+
 def reference_million(seed: int = 12, side: int = 1024):
     """1,048,576 atoms on a 1024 x 1024 lattice (spacing 1, the atom diameter) filling a 32 x 32-chunk world
     of the reference (1024 x 1024 units, 1024 atoms per chunk of capacity 1536), small random

@@ -328,3 +328,34 @@ class RefMPM:
         n = self.n
         return (self.pos[:n].cpu().numpy(), self.vel[:n].cpu().numpy(), self.C[:n].cpu().numpy(),
                 self.F[:n].cpu().numpy(), self.J[:n].cpu().numpy())
+
+
+# ===================================================================================================== render
+class RefRender:
+    """The reference's splat renderer (libs/render/source/cuda-render.cu: backgroundKernel and drawKernel, as
+    launchFill issues them, :189-211) drawing a chunk-major view into a pitched RGBA8 device buffer instead of
+    its D3D12 surface."""
+
+    def __init__(self, cubin=None, scene=(12, 6)):
+        self.sx, self.sy = scene
+        self.m = Module(cubin or REF_DIR / f"render_ref_{self.sx}x{self.sy}.cubin")
+        self.k = {n: self.m.fn(n) for n in ("backgroundKernel", "drawKernel")}
+
+    def render(self, pos, counts, width, height, stream=0):
+        import torch
+
+        cap = pos.shape[1]
+        d_pos = torch.from_numpy(np.ascontiguousarray(pos, np.float32).reshape(-1, 2)).cuda()
+        d_vel = torch.zeros_like(d_pos)
+        d_cnt = torch.from_numpy(np.ascontiguousarray(counts, np.int32)).cuda()
+        pitch = 4 * width
+        img = torch.zeros(height * pitch, dtype=torch.uint8, device="cuda")
+        del cap
+        sz = C.c_size_t
+        launch(self.k["backgroundKernel"], ((width + 31) // 32, (height + 15) // 16), (32, 16),
+               [_p(img), sz(pitch), sz(width), sz(height)], stream)
+        launch(self.k["drawKernel"], (self.sx, self.sy), (256,),
+               [_p(d_pos), _p(d_vel), _p(d_cnt), _p(img), sz(pitch), sz(width), sz(height)], stream)
+        torch.cuda.synchronize()
+        return img.cpu().numpy().reshape(height, width, 4)
+

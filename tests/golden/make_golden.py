@@ -17,6 +17,11 @@ oracle/build_ref.py) on a GPU:
                              absolute. The reference's intra-cell order follows shared-memory atomics, so only
                              per-cell counts and per-cell atom sets are comparable.
 
+  render_reference_frame.npz  the reference's splat renderer (backgroundKernel + drawKernel,
+                             cuda-render.cu:214-310) on gpe.scenes.reference_render_view into a 470 x 300
+                             image: the view (pos, counts), the size and the RGBA8 image. The view is drawn
+                             deterministically by the reference (no pixel is written by two threads).
+
 Usage (on a machine with a GPU): python tests/golden/make_golden.py OUT_DIR [fixture stem ...]
 """
 from __future__ import annotations
@@ -63,6 +68,16 @@ def make_pbf_migration():
     return dict(x=pos, v=vel, slot=slot.astype(np.uint32), mig_count=mig, out_cell=cell, out_x=x, out_xs=xs)
 
 
+def make_render():
+    from gpe import scenes
+    from oracle import refrun
+
+    pos, counts = scenes.reference_render_view()
+    w, h = 470, 300
+    img = refrun.RefRender().render(pos, counts, w, h)
+    return dict(pos=pos, counts=counts, width=np.int32(w), height=np.int32(h), image=img)
+
+
 def make_mpm():
     from gpe import scenes
     from oracle import refrun
@@ -76,7 +91,7 @@ def make_mpm():
 
 
 FIXTURES = {"pbf_reference_substep": make_pbf, "mpm_reference_substep": make_mpm,
-            "pbf_reference_migration": make_pbf_migration}
+            "pbf_reference_migration": make_pbf_migration, "render_reference_frame": make_render}
 
 if __name__ == "__main__":
     out = Path(sys.argv[1] if len(sys.argv) > 1 else Path(__file__).parent)

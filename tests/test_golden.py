@@ -80,3 +80,18 @@ def test_oracle_reproduces_reference_migration_and_sort(gpe_mod, oracle):
     s = o.predict_sort(r["x"], r["v"])
     compare_with_reference_sort(g["out_cell"], g["out_x"], g["out_xs"], s["key"], s["x"], s["xs"])
 
+
+def test_oracle_reproduces_reference_render_frame(oracle):
+    """The reference's own backgroundKernel and drawKernel drew this view (every pixel by one thread, up to six
+    stacked splats blended in order, splats over the chunk lines, clipping at the image edge): the oracle's
+    sequential restatement gives the same image byte for byte."""
+    from gpe import scenes
+
+    g = _load("render_reference_frame.npz")
+    pos, counts = scenes.reference_render_view()
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(counts, g["counts"]), "fixture inputs changed"
+    w, h = int(g["width"]), int(g["height"])
+    img = oracle.render_frame(w, h, 5.0, 32.0, pos, counts)
+    diff = np.argwhere(img != g["image"])
+    assert len(diff) == 0, (len(diff), diff[:5])
+

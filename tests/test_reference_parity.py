@@ -6,7 +6,9 @@ the self pair's pseudo-random gradient direction with the reference's chunk slot
 every term matches. The reference works in chunk-local coordinates, the engine in scene coordinates, so
 positions differ by the rounding of that change of frame (a few ulp of the scene coordinate). A complete
 substep — migration across chunk borders and the reference's per-chunk cell sort — is compared cell by cell
-(tests/refcompare.py): the reference's order within a cell follows shared-memory atomics.
+(tests/refcompare.py): the reference's order within a cell follows shared-memory atomics. The splat renderer
+is compared with the reference's backgroundKernel and drawKernel byte for byte on a view they draw
+deterministically.
 """
 import numpy as np
 import pytest
@@ -146,3 +148,34 @@ def test_mpm_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok)
             if nm in ("C",):
                 tol = 1e-4 * np.abs(b64).max()
             _assert_close(a, b, tol, f"{who} MPM {nm}")
+
+
+def test_render_engine_matches_reference_kernels(gpe_mod, cuda_ok):
+    """gpe_render_frame against the reference's backgroundKernel + drawKernel (cuda-render.cu:214-310), run
+    here on a view they draw deterministically (scenes.reference_render_view), and against the committed
+    fixture: byte for byte."""
+    import torch
+    from pathlib import Path
+
+    from gpe import scenes
+    from oracle import refrun
+
+    pos, counts = scenes.reference_render_view()
+    w, h = 470, 300
+    ref = refrun.RefRender().render(pos, counts, w, h)
+    g = dict(np.load(Path(__file__).resolve().parent / "golden" / "render_reference_frame.npz"))
+    assert np.array_equal(ref, g["image"]), "the reference's kernels drew another image than the fixture's"
+    cx, cy, cap = 12, 6, pos.shape[1]
+    d_pos = torch.from_numpy(np.ascontiguousarray(pos.reshape(-1, 2))).cuda()
+    d_vel = torch.zeros_like(d_pos)
+    d_cnt = torch.from_numpy(counts).cuda()
+    view = gpe_mod.View(d_pos.data_ptr(), d_vel.data_ptr(), d_cnt.data_ptr(), cx, cy, 32.0, cap)
+    pitch = 4 * w + 64
+    img = torch.zeros((h, pitch), dtype=torch.uint8, device="cuda")
+    cov = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    gpe_mod.render_frame(gpe_mod.Raster(img.data_ptr(), pitch, w, h, 5.0, 32.0, cov.data_ptr()), view)
+    torch.cuda.synchronize()
+    got = img[:, : 4 * w].cpu().numpy().reshape(h, w, 4)
+    diff = np.argwhere(got != ref)
+    assert len(diff) == 0, (len(diff), diff[:5])
+
