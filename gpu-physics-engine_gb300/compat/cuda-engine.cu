@@ -217,8 +217,21 @@ void TickStaging::outputTargetUpload(cudaStream_t stream)
                                       stream));
 }
 
+// Seams other than (0, 0) would rotate the chunk storage of a streaming world (PBF-internal.cuh:307-347);
+// the engine's scene is one walled domain stored by position, so a moved seam is refused instead of being
+// silently ignored.
+void require_no_seam(const int2& t)
+{
+    if (t.x != 0 || t.y != 0) {
+        std::fprintf(stderr, "torusUpload: seams (%d, %d) are not supported: the engine simulates one walled scene "
+                             "(seams must stay at (0, 0))\n", t.x, t.y);
+        std::abort();
+    }
+}
+
 void TickStaging::torusUpload(cudaStream_t stream)
 {
+    require_no_seam(staged->torus);
     CUDACHECK(cudaMemcpyToSymbolAsync(g_torus, &staged->torus, sizeof(int2), 0, cudaMemcpyHostToDevice, stream));
 }
 
@@ -255,6 +268,7 @@ void MPMTickStaging::outputTargetUpload(cudaStream_t stream)
 
 void MPMTickStaging::torusUpload(cudaStream_t stream)
 {
+    require_no_seam(staged->torus);
     CUDACHECK(cudaMemcpyToSymbolAsync(g_torus, &staged->torus, sizeof(int2), 0, cudaMemcpyHostToDevice, stream));
 }
 

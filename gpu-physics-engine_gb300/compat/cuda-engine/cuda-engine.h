@@ -18,8 +18,9 @@
 //     into the current output target — into g.graph, and instantiates g.exec, as the reference does.
 //   * hosePipe appends particles on the device (gpe_*_emit) instead of going through migration queues.
 //   * TickStaging uploads the output target into a device-resident view that the recorded publish reads at
-//     run time, like the reference's __constant__ c_output. The torus seams are stored but must stay (0, 0):
-//     streaming worlds are not supported.
+//     run time, like the reference's __constant__ c_output. The torus seams must stay (0, 0), as the
+//     reference's drivers keep them (main/PBF-master.cpp:48-50): torusUpload aborts with a message for any
+//     other value, since the engine's scene is one walled domain and has no chunk storage to rotate.
 #pragma once
 
 #include <atomic>
