@@ -204,23 +204,38 @@ __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __r
     return make_uint4(w[0] | (bad ? MASK_BAD : 0u), w[1], w[2], 0u);
 }
 
-// Visits the candidates of the masks m around base cell (bx, by), in scan order.
+// Visits the candidates of the masks m around base cell (bx, by), in scan order. The three rows run as one
+// loop (the next row with candidates takes over when a row's bits run out), so a warp iterates as often as
+// its lane with the most candidates, not the sum over rows of each row's maximum.
 template <class L, class A>
 __device__ __forceinline__ void scan_masked(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
                                             int32_t by, const uint4 m, L&& ld, A&& ap)
 {
-    const int32_t x0    = max(bx - 1, 0);
-    const uint32_t w[3] = {m.x & ~MASK_BAD, m.y, m.z};
-#pragma unroll
-    for (int32_t r = 0; r < 3; ++r) {
-        const int32_t y = by - 1 + r;
-        uint32_t bits   = w[r];
-        if (y < 0 || y >= d.ncy || bits == 0u) { continue; }
-        const uint32_t b = __ldg(&start[d.coff + (uint32_t)y * (uint32_t)d.ncx + x0]);
-        while (bits) {
-            const uint32_t t = (uint32_t)__ffs(bits) - 1u;
-            bits &= bits - 1u;
-            ap(b + t, ld(b + t));
+    // a row outside the scene has no bits, and its start is not read
+    const uint32_t row0 = d.coff + (uint32_t)max(bx - 1, 0);
+    const uint32_t ncx  = (uint32_t)d.ncx;
+    uint32_t w1 = m.y, w2 = m.z;
+    uint32_t bits = m.x & ~MASK_BAD;
+    uint32_t base = bits ? __ldg(&start[row0 + (uint32_t)(by - 1) * ncx]) : 0u;
+    uint32_t b1   = w1 ? __ldg(&start[row0 + (uint32_t)by * ncx]) : 0u;
+    const uint32_t b2 = w2 ? __ldg(&start[row0 + (uint32_t)(by + 1) * ncx]) : 0u;
+    if (bits == 0u) {
+        bits = w1 ? w1 : w2;
+        base = w1 ? b1 : b2;
+        w1   = w1 ? w2 : 0u;
+        b1   = b2;
+        w2   = 0u;
+    }
+    while (bits) {
+        const uint32_t t = (uint32_t)__ffs(bits) - 1u;
+        bits &= bits - 1u;
+        ap(base + t, ld(base + t));
+        if (bits == 0u) {
+            bits = w1 ? w1 : w2;
+            base = w1 ? b1 : b2;
+            w1   = w1 ? w2 : 0u;
+            b1   = b2;
+            w2   = 0u;
         }
     }
 }
