@@ -49,15 +49,16 @@ ALG_BYTES = {  # algorithmic bytes per particle per launch (FP32 SoA, each field
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the 1M-particle step's neighbour
-# kernels from ncu captures of this workload (cold caches: ncu flushes them before each replay). lambda: the
-# mean over a step's four launches, the mask-recording pass (13.7 MB) and three masked passes (30.7 MB each,
-# which also read the 16 MB candidate-mask array and the cell starts that stay in L2 in a live step)
-NCU_TRAFFIC = {"lambda": 26.48e6, "delta_p": 34.97e6, "xsph": 39.12e6}
-# warp instructions per launch (smsp__inst_executed.sum) of the same kernels from the same kind of capture;
-# lambda and delta p: the mean over a step's four launches (the mask-recording lambda executes 48.3 M, a
-# masked one 24.9 M). The neighbour kernels are bound by instruction issue, and the issue roofline is
-# these instructions over the live launch time against 4 schedulers x SMs x the sampled SM clock.
-NCU_WARP_INST = {"lambda": 30.75e6, "delta_p": 21.59e6, "xsph": 18.60e6}
+# kernels from ncu captures of this workload's first timed step (cold caches: ncu flushes them before each
+# replay). lambda: the mean over a step's four launches, the mask-recording pass (22.1 MB) and three masked
+# passes (39.1 MB each, which also read the 16 MB candidate-mask array and the cell starts that stay in L2
+# in a live step)
+NCU_TRAFFIC = {"lambda": 34.87e6, "delta_p": 43.5e6, "xsph": 39.27e6}
+# warp instructions per launch (smsp__inst_executed.sum) of the same kernels from the same captures; lambda:
+# the mean over a step's four launches (the mask-recording lambda executes 45.8 M, a masked one 20.8 M). The
+# neighbour kernels are bound by instruction issue, and the issue roofline is these instructions over the
+# live launch time against 4 schedulers x SMs x the sampled SM clock.
+NCU_WARP_INST = {"lambda": 27.05e6, "delta_p": 20.21e6, "xsph": 15.71e6}
 
 # engines whose steps alternate in the end-to-end measurement (measured: 1 engine 0.608 ms per step with
 # synchronous copies, 2 engines 0.411, 3 engines 0.386, against 0.295 ms of device time)
