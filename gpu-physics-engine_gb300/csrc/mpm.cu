@@ -2,16 +2,19 @@
 //
 // The reference runs, per substep, resetGrid -> P2GKernel -> gridKernel -> G2PKernel (MPM.cu:353-371) with
 // 27 scalar global atomics per particle (MPM.cu:124-126) and a separate streaming pass over the grid.
-// Here one step is two launches and the grid update needs no pass of its own:
+// Here one step is three launches:
 //   k_p2g            P2G: lanes that share a stencil base node (particles are kept sorted by base node) sum
 //                    their contributions per node with a segmented shuffle reduction, and the run's first
 //                    lane adds each of its 9 node sums to the grid with one vector global atomic
 //                    (red.global.add.v4.f32, resolved in L2).
-//   k_g2p            G2P on the raw momentum grid: the grid update (v = p/m + g dt, walls, MPM.cu:150-175) is
-//                    applied on the fly to each node the gather reads, and the grid read two steps earlier is
-//                    zeroed in the same launch (three grids rotate).
-// (A G2P fused with the next step's P2G in one kernel measured slower: 0.300 against 0.279 ms per step at 4M
-// particles, its 62 registers and shared tile halving the occupancy of either pass.)
+//   k_grid_vel       the grid update (v = p/m + g dt, walls, MPM.cu:150-175) once per node into an array of
+//                    node velocities (8 bytes a node), zeroing the grid read two steps earlier in the same
+//                    pass (three grids rotate).
+//   k_g2p            G2P: each particle gathers its 9 node velocities from that array (L1/L2 hits: sorted
+//                    neighbours share nodes).
+// (Measured alternatives, each slower: a G2P that staged its block's node box in shared memory and updated
+// each node there, 0.198 against 0.186 ms per step at 4M particles; a G2P fused with the next step's P2G,
+// its registers and shared tile halving the occupancy of either pass.)
 // Stage kernels (k_clear, k_p2g, k_grid, k_g2p on an updated grid) reproduce the reference's four kernels
 // one to one for stage-level parity tests.
 #include <cuda_runtime.h>
@@ -59,7 +62,6 @@ struct MpmK {
 namespace {
 
 constexpr int T_MPM     = 256;
-constexpr int TILE_CAP  = 2048; // nodes of G2P's shared-memory velocity tile (16 KB)
 
 // single-material modes are the material ids; MODE_MIXED reads an id per particle
 enum MatMode { MODE_FLUID = 0, MODE_COROT = 1, MODE_SNOW = 2, MODE_NEOHOOKEAN = 3, MODE_SAND = 4, MODE_MIXED = 8 };
@@ -247,15 +249,7 @@ struct PState {
     float J;
 };
 
-// G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301). RAW: the grid holds accumulated
-// momentum/mass and the node update is applied on the fly; otherwise it holds velocities.
-// node velocity of a RAW (accumulated momentum and mass) or updated grid node, at scene-local node (x, y)
-template <bool RAW>
-__device__ __forceinline__ float2 grid_velocity(const MpmK& k, const MpmScene& sc, float4 g, int32_t x, int32_t y)
-{
-    return RAW ? node_velocity(k, sc, g, x, y) : make_float2(g.x, g.y);
-}
-
+// G2P body (gridToParticle MPM.cu:227-265, handleOOB MPM.cu:267-301).
 // G2P of one particle whose stencil is s; nv(x, y) gives the velocity of scene-local node (x, y)
 template <class NodeVel>
 __device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, int m, bool track_f, const Stencil& s,
@@ -364,65 +358,6 @@ __device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, in
                                U.z * c0 * V.x + U.w * c1 * V.y, U.z * c0 * V.z + U.w * c1 * V.w);
         }
     }
-}
-
-// The node box that one block's particles touch: nodes [tx0, tx0 + tw) x [ty0, ty0 + th) of scene sc.
-// tiled: the box fits TILE_CAP nodes and holds one scene. empty: no thread of the block carries a particle.
-struct BlockBox {
-    int32_t tx0, ty0, tw, th;
-    bool tiled, empty;
-    MpmScene sc;
-};
-
-// All threads of the block must call it; `valid` marks threads that carry a particle (stencil s, scene sc).
-template <bool MS>
-__device__ __forceinline__ BlockBox block_box(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s)
-{
-    __shared__ int32_t s_box[4];
-    __shared__ uint32_t s_goff[2]; // the block's lowest and highest scene (first node): one scene to tile
-    __shared__ MpmScene s_sc;
-    if (threadIdx.x == 0) {
-        s_box[0]  = INT32_MAX;
-        s_box[1]  = INT32_MAX;
-        s_box[2]  = INT32_MIN;
-        s_box[3]  = INT32_MIN;
-        s_goff[0] = 0xffffffffu;
-        s_goff[1] = 0u;
-    }
-    __syncthreads();
-    // bounding box of the block's stencil bases
-    int32_t mnx = valid ? s.bx : INT32_MAX, mny = valid ? s.by : INT32_MAX;
-    int32_t mxx = valid ? s.bx : INT32_MIN, mxy = valid ? s.by : INT32_MIN;
-    mnx = __reduce_min_sync(0xffffffffu, mnx); // one warp reduction instruction each
-    mny = __reduce_min_sync(0xffffffffu, mny);
-    mxx = __reduce_max_sync(0xffffffffu, mxx);
-    mxy = __reduce_max_sync(0xffffffffu, mxy);
-    if ((threadIdx.x & 31) == 0 && mnx != INT32_MAX) {
-        atomicMin(&s_box[0], mnx);
-        atomicMin(&s_box[1], mny);
-        atomicMax(&s_box[2], mxx);
-        atomicMax(&s_box[3], mxy);
-    }
-    if (MS && k.n_scenes > 1) { // uniform: the scenes of the block's particles, a warp at a time
-        const uint32_t glo = __reduce_min_sync(0xffffffffu, valid ? sc.goff : 0xffffffffu);
-        const uint32_t ghi = __reduce_max_sync(0xffffffffu, valid ? sc.goff : 0u);
-        if ((threadIdx.x & 31) == 0 && glo != 0xffffffffu) {
-            atomicMin(&s_goff[0], glo);
-            atomicMax(&s_goff[1], ghi);
-        }
-        if (valid && glo == sc.goff) { s_sc = sc; } // read only when the block holds one scene
-    }
-    __syncthreads();
-    BlockBox b;
-    b.tx0          = s_box[0];
-    b.ty0          = s_box[1];
-    b.empty        = b.tx0 == INT32_MAX;
-    b.tw           = s_box[2] - b.tx0 + 3;
-    b.th           = s_box[3] - b.ty0 + 3;
-    const bool one = !MS || k.n_scenes <= 1;
-    b.tiled        = !b.empty && b.tw * b.th <= TILE_CAP && (one || s_goff[0] == s_goff[1]);
-    b.sc           = one ? k.s0 : (b.tiled ? s_sc : sc);
-    return b;
 }
 
 // Scatter of one warp's particles (particleToGrid, MPM.cu:116-126). All lanes of the warp must call it;
@@ -536,60 +471,47 @@ __global__ void k_grid(const MpmK k, float4* __restrict__ grid)
     }
 }
 
-// G2P on a grid of velocities (RAW=false) or of raw momentum (RAW=true); writes the whole particle state
-// 5 blocks per SM in 48 registers (the scene-lookup variants spill a little there, and still run faster
-// than at 4 blocks)
-template <int MODE, bool RAW, bool MS>
-__global__ void __launch_bounds__(T_MPM, 5)
-    k_g2p(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ x, float2* __restrict__ v,
-          float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
-          const int32_t* __restrict__ sid, float4* __restrict__ zero_grid, int64_t zero_nodes, uint32_t* status)
+// The grid update once per node (gridKernel, MPM.cu:131-177) into node velocities, and the zeroing of the
+// grid read two steps earlier (zero may be null).
+template <bool MS>
+__global__ void k_grid_vel(const MpmK k, const float4* __restrict__ grid, float2* __restrict__ vel,
+                           float4* __restrict__ zero, int64_t nn)
 {
-    __shared__ float2 s_v[TILE_CAP];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn; idx += stride) {
+        const float4 g      = grid[idx];
+        const MpmScene sc   = MS ? scene_of_node(k, idx) : k.s0;
+        const int64_t local = idx - (int64_t)sc.goff;
+        vel[idx]            = node_velocity(k, sc, g, (int32_t)(local % sc.nx), (int32_t)(local / sc.nx));
+        if (zero) { zero[idx] = make_float4(0.f, 0.f, 0.f, 0.f); }
+    }
+}
+
+// G2P from node velocities: node q's velocity is vel[q * VS] (VS = 1: the node-velocity array; VS = 2: the
+// .xy of a float4 grid that k_grid updated in place). Writes the whole particle state.
+// 6 blocks per SM (40 registers; the scene-lookup variants spill a little there)
+template <int MODE, int VS, bool MS>
+__global__ void __launch_bounds__(T_MPM, 6)
+    k_g2p(const MpmK k, const float2* __restrict__ vel, float2* __restrict__ x, float2* __restrict__ v,
+          float4* __restrict__ C, float4* __restrict__ F, float* __restrict__ J, const int32_t* __restrict__ mat,
+          const int32_t* __restrict__ sid, uint32_t* status)
+{
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (zero_grid) {
-        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-        for (int64_t z = i; z < zero_nodes; z += stride) { zero_grid[z] = make_float4(0.f, 0.f, 0.f, 0.f); }
-    }
-    if ((int64_t)blockIdx.x * blockDim.x >= count_of(k)) { return; } // uniform: the block holds no particle
-    const bool valid   = i < count_of(k);
-    const int m        = valid ? mat_of(k, MODE, mat, i) : 0;
+    if (i >= count_of(k)) { return; }
+    const int m        = mat_of(k, MODE, mat, i);
     const bool track_f = (k.flags & GPE_MPM_FLAG_FLUID_F) != 0;
-    const MpmScene sc  = valid ? scene_of<MS>(k, sid, i) : k.s0;
+    const MpmScene sc  = scene_of<MS>(k, sid, i);
     PState ps;
-    Stencil s{};
-    if (valid) {
-        ps.x = x[i];
-        ps.F = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
-        ps.J = keeps_j(m) ? J[i] : 1.f;
-        s    = stencil(k, sc, ps.x, status);
-    }
-    // The block's nodes go through shared memory once, each node's velocity computed once (the particles of
-    // a cell share their 9 nodes, and sorted neighbours overlap); a box wider than the tile or spread over
-    // several scenes gathers from global memory.
-    const BlockBox bb = block_box<MS>(k, sc, valid, s);
-    if (bb.tiled) {
-        const MpmScene& bs = bb.sc;
-        for (int t = threadIdx.x; t < bb.tw * bb.th; t += blockDim.x) {
-            const int32_t gx = bb.tx0 + t % bb.tw, gy = bb.ty0 + t / bb.tw;
-            const float4 g   = __ldg(&grid[(size_t)bs.goff + (size_t)gy * (size_t)bs.nx + (size_t)gx]);
-            s_v[t]           = grid_velocity<RAW>(k, bs, g, gx, gy);
-        }
-        __syncthreads();
-    }
-    if (!valid) { return; }
-    if (bb.tiled) {
-        g2p_finish(k, sc, m, track_f, s,
-                   [&](int32_t nxi, int32_t nyj) { return s_v[(nyj - bb.ty0) * bb.tw + (nxi - bb.tx0)]; }, ps,
-                   status);
-    } else {
-        g2p_finish(k, sc, m, track_f, s,
-                   [&](int32_t nxi, int32_t nyj) {
-                       const float4 g = __ldg(&grid[(size_t)sc.goff + (size_t)nyj * (size_t)sc.nx + (size_t)nxi]);
-                       return grid_velocity<RAW>(k, sc, g, nxi, nyj);
-                   },
-                   ps, status);
-    }
+    ps.x             = x[i];
+    ps.F             = keeps_f(m, track_f) ? F[i] : make_float4(1.f, 0.f, 0.f, 1.f);
+    ps.J             = keeps_j(m) ? J[i] : 1.f;
+    const Stencil s  = stencil(k, sc, ps.x, status);
+    const float2* nv = vel + (size_t)VS * (size_t)sc.goff;
+    g2p_finish(k, sc, m, track_f, s,
+               [&](int32_t nxi, int32_t nyj) {
+                   return __ldg(&nv[(size_t)VS * ((size_t)nyj * (size_t)sc.nx + (size_t)nxi)]);
+               },
+               ps, status);
     x[i] = ps.x;
     v[i] = ps.v;
     C[i] = ps.C;
@@ -777,6 +699,7 @@ struct gpe_mpm {
     std::vector<MpmScene> scenes;  // several scenes: their grids, in the order of the node array
     MpmScene* d_scenes = nullptr;
     float4* grid[3] = {};
+    float2* vel_n   = nullptr; // node velocities of the current step (k_grid_vel)
     uint2* keyrank  = nullptr;
     uint32_t* bucket = nullptr;
     uint32_t* count  = nullptr;
@@ -910,35 +833,48 @@ int32_t launch_p2g(gpe_mpm* s, float4* grid, cudaStream_t st)
     }
 }
 
-template <int MODE, bool RAW>
-int32_t launch_g2p_t(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
+// G2P from node velocities vel (stride VS float2 per node, see k_g2p)
+template <int MODE, int VS>
+int32_t launch_g2p_t(gpe_mpm* s, const float2* vel, cudaStream_t st)
 {
-    const int c      = s->cur;
-    const unsigned g = std::max(mblocks(lsz(s)), zero ? grid_blocks(s->nn) : 1u);
+    const int c = s->cur;
     if (s->scenes.size() > 1) {
-        k_g2p<MODE, RAW, true><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
-                                                    s->mat[c], s->sid[c], zero, zero ? s->nn : 0, s->status);
+        k_g2p<MODE, VS, true><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, vel, s->x[c], s->v[c], s->C[c], s->F[c],
+                                                                s->J[c], s->mat[c], s->sid[c], s->status);
     } else {
-        k_g2p<MODE, RAW, false><<<g, T_MPM, 0, st>>>(s->k, grid, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
-                                                     s->mat[c], nullptr, zero, zero ? s->nn : 0, s->status);
+        k_g2p<MODE, VS, false><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, vel, s->x[c], s->v[c], s->C[c], s->F[c],
+                                                                 s->J[c], s->mat[c], nullptr, s->status);
     }
     GPE_CHECK_LAUNCH("k_g2p");
     return GPE_OK;
 }
 
-template <bool RAW>
-int32_t launch_g2p(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
+template <int VS>
+int32_t launch_g2p(gpe_mpm* s, const float2* vel, cudaStream_t st)
 {
-    if (lsz(s) == 0 && !zero) { return GPE_OK; }
+    if (lsz(s) == 0) { return GPE_OK; }
     s->launches += 1;
     switch (mode_of(s)) {
-        case MODE_FLUID: return launch_g2p_t<MODE_FLUID, RAW>(s, grid, zero, st);
-        case MODE_COROT: return launch_g2p_t<MODE_COROT, RAW>(s, grid, zero, st);
-        case MODE_SNOW: return launch_g2p_t<MODE_SNOW, RAW>(s, grid, zero, st);
-        case MODE_NEOHOOKEAN: return launch_g2p_t<MODE_NEOHOOKEAN, RAW>(s, grid, zero, st);
-        case MODE_SAND: return launch_g2p_t<MODE_SAND, RAW>(s, grid, zero, st);
-        default: return launch_g2p_t<MODE_MIXED, RAW>(s, grid, zero, st);
+        case MODE_FLUID: return launch_g2p_t<MODE_FLUID, VS>(s, vel, st);
+        case MODE_COROT: return launch_g2p_t<MODE_COROT, VS>(s, vel, st);
+        case MODE_SNOW: return launch_g2p_t<MODE_SNOW, VS>(s, vel, st);
+        case MODE_NEOHOOKEAN: return launch_g2p_t<MODE_NEOHOOKEAN, VS>(s, vel, st);
+        case MODE_SAND: return launch_g2p_t<MODE_SAND, VS>(s, vel, st);
+        default: return launch_g2p_t<MODE_MIXED, VS>(s, vel, st);
     }
+}
+
+// node velocities of grid into s->vel_n, zeroing grid `zero` (or nothing) in the same pass
+int32_t launch_grid_vel(gpe_mpm* s, const float4* grid, float4* zero, cudaStream_t st)
+{
+    if (s->scenes.size() > 1) {
+        k_grid_vel<true><<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->k, grid, s->vel_n, zero, s->nn);
+    } else {
+        k_grid_vel<false><<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->k, grid, s->vel_n, zero, s->nn);
+    }
+    GPE_CHECK_LAUNCH("k_grid_vel");
+    s->launches += 1;
+    return GPE_OK;
 }
 
 int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
@@ -961,7 +897,8 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
     return GPE_OK;
 }
 
-// n_steps steps: [sort], P2G, (n-1) x (G2P, P2G), G2P. Grids ga+1 and ga+2 are zero on entry and exit.
+// n_steps steps: [sort], P2G, (n-1) x (node velocities, G2P, P2G), node velocities, G2P. Grids ga+1 and ga+2
+// are zero on entry and exit.
 int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
 {
     int32_t rc = GPE_OK;
@@ -972,8 +909,10 @@ int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
     for (int32_t t = 1; t < n_steps && rc == GPE_OK; ++t) {
         const int b = (a + 1) % 3, z = (a + 2) % 3;
         if (lsz(s) > 0) {
-            // G2P of this step (zeroing the grid read two steps ago), P2G of the next into the zero grid b
-            rc = launch_g2p<true>(s, s->grid[a], s->grid[z], st);
+            // node velocities of this step (zeroing the grid read two steps ago), its G2P, and the P2G of the
+            // next step into the zero grid b
+            rc = launch_grid_vel(s, s->grid[a], s->grid[z], st);
+            if (rc == GPE_OK) { rc = launch_g2p<1>(s, s->vel_n, st); }
             if (rc == GPE_OK) { rc = launch_p2g(s, s->grid[b], st); }
         } else {
             k_clear<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->grid[z], s->nn);
@@ -983,7 +922,8 @@ int32_t mpm_run(gpe_mpm* s, int32_t n_steps, bool do_sort, cudaStream_t st)
     }
     if (rc) { return rc; }
     // last G2P; zero the grid that was used before this one so two zero grids follow `a`
-    rc    = launch_g2p<true>(s, s->grid[a], s->grid[(a + 2) % 3], st);
+    rc = launch_grid_vel(s, s->grid[a], s->grid[(a + 2) % 3], st);
+    if (rc == GPE_OK) { rc = launch_g2p<1>(s, s->vel_n, st); }
     s->ga = a;
     return rc;
 }
@@ -1016,6 +956,7 @@ int32_t mpm_alloc(gpe_mpm* s)
         oid[b] = c.take<uint32_t>(N);
     }
     for (int b = 0; b < 3; ++b) { og[b] = c.take<float4>(M); }
+    const size_t ovn = c.take<float2>(M);
     const size_t okr = c.take<uint2>(N);
     const size_t obk = c.take<uint32_t>(N);
     const size_t ocn = c.take<uint32_t>(M);
@@ -1043,6 +984,7 @@ int32_t mpm_alloc(gpe_mpm* s)
         s->id[q]  = reinterpret_cast<uint32_t*>(b + oid[q]);
     }
     for (int q = 0; q < 3; ++q) { s->grid[q] = reinterpret_cast<float4*>(b + og[q]); }
+    s->vel_n   = reinterpret_cast<float2*>(b + ovn);
     s->keyrank = reinterpret_cast<uint2*>(b + okr);
     s->bucket  = reinterpret_cast<uint32_t*>(b + obk);
     s->count   = reinterpret_cast<uint32_t*>(b + ocn);
@@ -1363,7 +1305,7 @@ int32_t gpe_mpm_stage(gpe_mpm* s, int32_t stage, void* stream)
             k_grid<<<grid_blocks(s->nn), T_MPM, 0, st>>>(s->k, g);
             GPE_CHECK_LAUNCH("k_grid");
             return GPE_OK;
-        case GPE_MPM_STAGE_G2P: return launch_g2p<false>(s, g, nullptr, st);
+        case GPE_MPM_STAGE_G2P: return launch_g2p<2>(s, reinterpret_cast<const float2*>(g), st);
         case GPE_MPM_STAGE_SORT: return mpm_sort(s, st);
         default: return GPE_ERR_BAD_ARG;
     }
