@@ -176,15 +176,17 @@ constexpr uint32_t MASK_BAD = 0x80000000u; // in word 0: this particle's masks a
 
 // The full scan of particle i whose base cell is (bx, by) (cell h, R = 1), recording its masks. f(j)
 // returns whether candidate j lies within h + skin. The particle's own slot is not recorded: no pass takes
-// a term from the self pair inside its loop (the density's self term is added after it).
+// a term from the self pair inside its loop (the density's self term is added after it); its bit is cleared
+// after the scan, and self_in tells whether the scan met that slot.
 template <class F>
 __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __restrict__ start, int32_t bx,
-                                            int32_t by, int32_t i, F&& f)
+                                            int32_t by, int32_t i, bool& self_in, F&& f)
 {
     const int32_t x0 = max(bx - 1, 0);
     const int32_t x1 = min(bx + 1, d.ncx - 1);
     uint32_t w[3]    = {0u, 0u, 0u};
     bool bad         = false;
+    self_in          = false;
 #pragma unroll
     for (int32_t r = 0; r < 3; ++r) {
         const int32_t y = by - 1 + r;
@@ -193,15 +195,18 @@ __device__ __forceinline__ uint4 scan_build(const DomDev& d, const uint32_t* __r
         const uint32_t b   = __ldg(&start[row + x0]);
         const uint32_t e   = __ldg(&start[row + x1 + 1]);
         bad                = bad || (e - b > 31u);
-        uint32_t wr        = 0u;
-        for (uint32_t j = b; j < e; ++j) {
-            const bool near  = f(j) && j != (uint32_t)i;
-            const uint32_t t = j - b;
-            wr |= (near && t < 31u) ? (1u << t) : 0u;
+        // one bit per slot, shifted along with the slot (a row of more than 31 slots is marked bad above,
+        // and its bits are never read)
+        uint32_t wr = 0u, bit = 1u;
+        for (uint32_t j = b; j < e; ++j, bit <<= 1) { wr |= f(j) ? bit : 0u; }
+        const uint32_t t = (uint32_t)i - b;
+        if (t < e - b) { // the particle's own slot is in this row
+            self_in = true;
+            wr &= t < 31u ? ~(1u << t) : 0xffffffffu;
         }
         w[r] = wr;
     }
-    return make_uint4(w[0] | (bad ? MASK_BAD : 0u), w[1], w[2], 0u);
+    return make_uint4((w[0] & ~MASK_BAD) | (bad ? MASK_BAD : 0u), w[1], w[2], 0u);
 }
 
 // Visits the candidates of the masks m around base cell (bx, by), in scan order. The three rows run as one
@@ -256,7 +261,8 @@ __device__ __forceinline__ bool scan_ld2(const DomDev& d, const PbfK& k, const u
         const int32_t by   = cell_coord(py, d.oy, k.inv_cell, d.ncy);
         const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
         if constexpr (MASK == MASK_BUILD) {
-            uint4 m = scan_build(d, start, bx, by, i, f);
+            bool self_in;
+            uint4 m = scan_build(d, start, bx, by, i, self_in, f);
             if (key != __ldg(&k.keys[i])) { m.x |= MASK_BAD; } // built around another cell than the sort cell
             k.nmask[i] = m;
         } else {
@@ -503,9 +509,8 @@ __device__ __forceinline__ void lambda_one(const PbfK& k, const DomDev* __restri
         const int32_t by   = cell_coord(p.y, d.oy, k.inv_cell, d.ncy);
         const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
         bool seen          = false;
-        uint4 m            = scan_build(d, start, bx, by, i, [&](uint32_t j) -> bool {
+        uint4 m            = scan_build(d, start, bx, by, i, seen, [&](uint32_t j) -> bool {
             const float2 r = offset(px, pd, ld(j));
-            seen           = seen || (j == (uint32_t)i);
             return fmaf(r.x, r.x, r.y * r.y) < k.skin2;
         });
         const bool fits = !(m.x & MASK_BAD); // no row held more candidates than a mask word
