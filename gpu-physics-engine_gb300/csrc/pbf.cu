@@ -652,12 +652,13 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
     float s4 = 0.f, s6 = 0.f, swl = 0.f;
     int32_t nn     = 0;
     bool self_seen = false;
-    scan<MASK, false>(d, k, start, p.x, p.y, i, [&](uint32_t j) -> bool {
-        const float4 q  = __ldg(&xd[j]);
-        const float lp  = __ldg(&prev[j]);
+    // ME: the candidate may be the particle itself (full scans); masked scans never visit it
+    auto body = [&](uint32_t j, const Nbr ql, auto me) -> bool {
+        const float4 q  = ql.q;
+        const float lp  = ql.a;
         const float2 r  = offset(px, pd, q);
         const float r2  = fmaf(r.x, r.x, r.y * r.y);
-        const bool self = j == (uint32_t)i;
+        const bool self = decltype(me)::value && j == (uint32_t)i;
         self_seen       = self_seen || self;
         const bool in   = (r2 <= k.h2) && !self;
         const bool dir  = in && (r2 > 1e-12f);
@@ -683,7 +684,33 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
             s4 = fmaf(k.h2, k.h2, s4);
         }
         return r2 < k.skin2;
-    });
+    };
+    auto ld   = [&](uint32_t j) { return Nbr{__ldg(&xd[j]), __ldg(&prev[j])}; };
+    auto full = [&](uint32_t j, const Nbr q) -> bool { return body(j, q, std::true_type{}); };
+    auto near = [&](uint32_t j, const Nbr q) -> bool { return body(j, q, std::false_type{}); };
+    if constexpr (MASK == MASK_BUILD) {
+        // as in k_lambda: a distance-only scan records the masks, then the feature terms run over the
+        // recorded candidates alone (the full scan's other candidates add exact zeros)
+        const int32_t bx   = cell_coord(p.x, d.ox, k.inv_cell, d.ncx);
+        const int32_t by   = cell_coord(p.y, d.oy, k.inv_cell, d.ncy);
+        const uint32_t key = d.coff + (uint32_t)by * (uint32_t)d.ncx + (uint32_t)bx;
+        bool seen          = false;
+        uint4 m            = scan_build(d, start, bx, by, i, seen, [&](uint32_t j) -> bool {
+            const float2 r = offset(px, pd, __ldg(&xd[j]));
+            return fmaf(r.x, r.x, r.y * r.y) < k.skin2;
+        });
+        const bool fits = !(m.x & MASK_BAD);
+        if (key != __ldg(&k.keys[i])) { m.x |= MASK_BAD; } // built around another cell than the sort cell
+        k.nmask[i] = m;
+        if (fits) {
+            scan_masked(d, start, bx, by, m, ld, near);
+            self_seen = seen;
+        } else {
+            for_neighbours_at(d, k, start, bx, by, [&](uint32_t j) { full(j, ld(j)); });
+        }
+    } else {
+        scan_ld<MASK, false>(d, k, start, p.x, p.y, i, ld, full);
+    }
     const float lpi = prev[i];
     if (self_seen) {
         s6  = fmaf(k.h2 * k.h2, k.h2, s6);
@@ -728,7 +755,8 @@ __device__ __forceinline__ float warm_features(const PbfK& k, const DomDev& d, c
 // particles is 4 KB at feat + t * 2048 in the tensor cores' K-major layout, so part 2 moves it to shared
 // memory with one bulk copy. (Computing the features inside the tensor-core kernel caps the neighbour loop
 // at the 7 CTAs of 4 warps that fit an SM beside their TMEM and operand tiles: 126 us against about 50 us
-// here at 1M particles.)
+// here at 1M particles.) With MASK_BUILD the pass records the step's candidate masks with a distance-only
+// scan and computes the features over the recorded candidates alone, as k_lambda does.
 template <bool MULTI, bool SELFG, int MASK>
 __global__ void __launch_bounds__(T_PART)
     k_lambda_feat(const PbfK k, const DomDev* __restrict__ doms, const int32_t* __restrict__ dom,
