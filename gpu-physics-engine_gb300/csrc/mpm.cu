@@ -3,10 +3,10 @@
 // The reference runs, per substep, resetGrid -> P2GKernel -> gridKernel -> G2PKernel (MPM.cu:353-371) with
 // 27 scalar global atomics per particle (MPM.cu:124-126) and a separate streaming pass over the grid.
 // Here one step is three launches:
-//   k_p2g            P2G: lanes that share a stencil base node (particles are kept sorted by base node) sum
-//                    their contributions per node with a segmented shuffle reduction, and the run's first
-//                    lane adds each of its 9 node sums to the grid with one vector global atomic
-//                    (red.global.add.v4.f32, resolved in L2).
+//   k_p2g            P2G, two consecutive particles per thread: lanes that share a stencil base node
+//                    (particles are kept sorted by base node) sum their contributions per node with a
+//                    segmented shuffle reduction, and the run's first lane adds each of its 9 node sums to
+//                    the grid with one vector global atomic (red.global.add.v4.f32, resolved in L2).
 //   k_grid_vel       the grid update (v = p/m + g dt, walls, MPM.cu:150-175) once per node into an array of
 //                    node velocities (8 bytes a node), zeroing the grid read two steps earlier in the same
 //                    pass (three grids rotate).
@@ -360,65 +360,35 @@ __device__ __forceinline__ void g2p_finish(const MpmK& k, const MpmScene& sc, in
     }
 }
 
-// Scatter of one warp's particles (particleToGrid, MPM.cu:116-126). All lanes of the warp must call it;
-// `valid` marks lanes that carry a particle. wide_warps counts the warps that need the 5-round reduction (a
-// run longer than 16 lanes).
-// Node sums go straight to the grid with vector atomics in L2: staging them in a shared-memory tile of the
-// block's nodes first (float atomics on shared memory, a block barrier, then one global atomic per touched
-// node) measured slower, 0.216 against 0.198 ms per 4M-particle step.
-__device__ __forceinline__ void p2g_scatter(const MpmK& k, const MpmScene& sc, bool valid, const Stencil& s,
-                                            float2 v, float4 Q, float4* __restrict__ grid, uint32_t* wide_warps)
+// The node term of one particle (stencil s, velocity v, affine matrix Q) for node (i, j) of its stencil,
+// added to (c, cm): w (m v + Q dp) and w m (particleToGrid, MPM.cu:116-126); momentum as packed FP32 pairs
+__device__ __forceinline__ void p2g_term(const MpmK& k, const Stencil& s, float2 v, float4 Q, int i, int j,
+                                         float2& c, float& cm)
 {
-    // Particles are kept spatially sorted, so consecutive lanes mostly share their stencil's base node and
-    // with it all 9 target nodes. For each node the lanes of such a run sum their contributions with a
-    // segmented shuffle reduction, and only the run's first lane updates the grid: the lanes of a run would
-    // otherwise all hit the same 9 nodes.
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t key  = valid ? sc.goff + (uint32_t)s.by * (uint32_t)sc.nx + (uint32_t)s.bx : 0xffffffffu;
-    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const bool head     = lane == 0u || prev != key;
-    const uint32_t heads = __ballot_sync(0xffffffffu, head);
-    const uint32_t later = lane == 31u ? 0u : (heads & (0xffffffffu << (lane + 1u)));
-    const uint32_t run_end = later ? (uint32_t)(__ffs(later) - 1) : 32u; // first lane of the next run
-    // momentum terms as packed FP32 pairs: (v.x, v.y) m + (Q.x, Q.z) dpx + (Q.y, Q.w) dpy
-    const float2 qa = make_float2(Q.x, Q.z), qb = make_float2(Q.y, Q.w);
-    const float2 mm = make_float2(k.mass, k.mass);
-    // the reduction needs log2 of the warp's longest run rounds: 4 while no run is longer than 16 lanes
-    const uint32_t longest = __reduce_max_sync(0xffffffffu, head ? run_end - lane : 0u);
-    float4* const base = grid + (size_t)sc.goff + (size_t)s.by * (size_t)sc.nx + (size_t)s.bx;
-    auto scatter = [&](auto rounds) {
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        const int i = q % 3, j = q / 3;
-        float2 c = make_float2(0.f, 0.f);
-        float cm = 0.f;
-        if (valid) {
-            const float w   = s.wx[i] * s.wy[j];
-            const float dpx = ((float)i - s.fx) * k.dx;
-            const float dpy = ((float)j - s.fy) * k.dx;
-            const float2 a  = fma2(qb, make_float2(dpy, dpy), mul2(qa, make_float2(dpx, dpx)));
-            c               = mul2(make_float2(w, w), fma2(v, mm, a));
-            cm              = w * k.mass;
-        }
-#pragma unroll
-        for (uint32_t d = 1u; d < (1u << decltype(rounds)::value); d <<= 1) {
-            const float ox = __shfl_down_sync(0xffffffffu, c.x, d);
-            const float oy = __shfl_down_sync(0xffffffffu, c.y, d);
-            const float om = __shfl_down_sync(0xffffffffu, cm, d);
-            if (lane + d < run_end) {
-                c = add2(c, make_float2(ox, oy));
-                cm += om;
-            }
-        }
-        if (head && valid) { atomicAdd(base + (size_t)j * (size_t)sc.nx + i, make_float4(c.x, c.y, cm, 0.f)); }
-    }
-    };
-    if (longest <= 16u) {
-        scatter(std::integral_constant<int, 4>{});
-    } else {
-        if (lane == 0u) { atomicAdd(wide_warps, 1u); } // warp-uniform branch: one count per warp
-        scatter(std::integral_constant<int, 5>{});
-    }
+    const float w   = s.wx[i] * s.wy[j];
+    const float dpx = ((float)i - s.fx) * k.dx;
+    const float dpy = ((float)j - s.fy) * k.dx;
+    const float2 a  = fma2(make_float2(Q.y, Q.w), make_float2(dpy, dpy),
+                           mul2(make_float2(Q.x, Q.z), make_float2(dpx, dpx)));
+    c               = add2(c, mul2(make_float2(w, w), fma2(v, make_float2(k.mass, k.mass), a)));
+    cm += w * k.mass;
+}
+
+// particle i's scene, stencil, velocity and affine matrix for P2G
+template <int MODE, bool MS>
+__device__ __forceinline__ void p2g_load(const MpmK& k, const float2* __restrict__ x, const float2* __restrict__ v,
+                                         const float4* __restrict__ C, const float4* __restrict__ F,
+                                         const float* __restrict__ J, const int32_t* __restrict__ mat,
+                                         const int32_t* __restrict__ sid, int32_t i, MpmScene& sc, Stencil& s,
+                                         float2& vv, float4& Q, uint32_t* status)
+{
+    sc              = scene_of<MS>(k, sid, i);
+    const int m     = mat_of(k, MODE, mat, i);
+    const float4 Fp = (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : F[i];
+    const float Jp  = keeps_j(m) ? J[i] : 1.f;
+    Q               = affine(k, m, C[i], Fp, Jp);
+    vv              = v[i];
+    s               = stencil(k, sc, x[i], status);
 }
 
 // ----- kernels -------------------------------------------------------------------------------------------
@@ -431,28 +401,89 @@ __global__ void k_clear(float4* __restrict__ grid, int64_t nn)
     }
 }
 
+// P2G, two consecutive particles per thread (particles 2t and 2t + 1). Particles are kept sorted by stencil
+// base node, so consecutive lanes mostly share their base node and with it all 9 target nodes. When a
+// thread's two particles share one, their terms are summed in registers; then, for each node, the lanes of a
+// run (consecutive lanes with the same base node, 64 particles a warp) sum their contributions with a
+// segmented shuffle reduction (2 to 5 rounds, as the warp's longest run needs), and the run's first lane adds
+// the node sum to the grid with one vector global atomic (red.global.add.v4.f32, resolved in L2). A first
+// particle whose base node differs from its partner's (a run boundary inside the thread) adds its 9 terms
+// with atomics of its own. One particle per thread measured slower: 0.185 against 0.153 ms per 4M-particle
+// step, its shuffle rounds covering half as many particles; staging node sums in a shared-memory tile of the
+// block's nodes (float atomics on shared memory, a block barrier, a flush) slower again.
+// status[2] counts the warps that need the 5-round reduction (a run of more than 16 lanes).
 template <int MODE, bool MS>
-// 8 blocks per SM (32 registers); 6 with the scene lookup
-__global__ void __launch_bounds__(T_MPM, MS ? 6 : 8)
+__global__ void __launch_bounds__(T_MPM)
     k_p2g(const MpmK k, const float2* __restrict__ x, const float2* __restrict__ v, const float4* __restrict__ C,
           const float4* __restrict__ F, const float* __restrict__ J, const int32_t* __restrict__ mat,
           const int32_t* __restrict__ sid, float4* __restrict__ grid, uint32_t* status)
 {
-    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < count_of(k);
-    const MpmScene sc = valid ? scene_of<MS>(k, sid, i) : k.s0;
-    Stencil s{};
-    float2 vv = make_float2(0.f, 0.f);
-    float4 Q  = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid) {
-        const int m     = mat_of(k, MODE, mat, i);
-        const float4 Fp = (m == MODE_FLUID) ? make_float4(1.f, 0.f, 0.f, 1.f) : F[i];
-        const float Jp  = keeps_j(m) ? J[i] : 1.f;
-        Q               = affine(k, m, C[i], Fp, Jp);
-        vv              = v[i];
-        s               = stencil(k, sc, x[i], status);
+    const int32_t t  = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t n  = count_of(k);
+    const int32_t i0 = 2 * t, i1 = 2 * t + 1;
+    const bool ok0 = i0 < n, ok1 = i1 < n;
+    MpmScene sc0 = k.s0, sc1 = k.s0;
+    Stencil s0{}, s1{};
+    float2 v0 = make_float2(0.f, 0.f), v1 = v0;
+    float4 Q0 = make_float4(0.f, 0.f, 0.f, 0.f), Q1 = Q0;
+    if (ok0) { p2g_load<MODE, MS>(k, x, v, C, F, J, mat, sid, i0, sc0, s0, v0, Q0, status); }
+    if (ok1) { p2g_load<MODE, MS>(k, x, v, C, F, J, mat, sid, i1, sc1, s1, v1, Q1, status); }
+    const uint32_t key0 = ok0 ? sc0.goff + (uint32_t)s0.by * (uint32_t)sc0.nx + (uint32_t)s0.bx : 0xffffffffu;
+    const uint32_t key1 = ok1 ? sc1.goff + (uint32_t)s1.by * (uint32_t)sc1.nx + (uint32_t)s1.bx : 0xffffffffu;
+    const bool join = ok1 && key0 == key1; // the first particle joins the thread's run
+    const bool solo = ok0 && !join;        // the first particle goes to the grid on its own
+    // runs of lanes with the same base node (that of the second particle)
+    const uint32_t lane    = threadIdx.x & 31u;
+    const uint32_t prev    = __shfl_up_sync(0xffffffffu, key1, 1);
+    const bool head        = lane == 0u || prev != key1;
+    const uint32_t heads   = __ballot_sync(0xffffffffu, head);
+    const uint32_t later   = lane == 31u ? 0u : (heads & (0xffffffffu << (lane + 1u)));
+    const uint32_t run_end = later ? (uint32_t)(__ffs(later) - 1) : 32u; // first lane of the next run
+    const uint32_t longest = __reduce_max_sync(0xffffffffu, head ? run_end - lane : 0u);
+    float4* const base1    = grid + (size_t)sc1.goff + (size_t)s1.by * (size_t)sc1.nx + (size_t)s1.bx;
+    auto scatter = [&](auto rounds) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int i = q % 3, j = q / 3;
+            float2 c = make_float2(0.f, 0.f);
+            float cm = 0.f;
+            if (join) { p2g_term(k, s0, v0, Q0, i, j, c, cm); }
+            if (ok1) { p2g_term(k, s1, v1, Q1, i, j, c, cm); }
+#pragma unroll
+            for (uint32_t d = 1u; d < (1u << decltype(rounds)::value); d <<= 1) {
+                const float ox = __shfl_down_sync(0xffffffffu, c.x, d);
+                const float oy = __shfl_down_sync(0xffffffffu, c.y, d);
+                const float om = __shfl_down_sync(0xffffffffu, cm, d);
+                if (lane + d < run_end) {
+                    c = add2(c, make_float2(ox, oy));
+                    cm += om;
+                }
+            }
+            if (head && ok1) { atomicAdd(base1 + (size_t)j * (size_t)sc1.nx + i, make_float4(c.x, c.y, cm, 0.f)); }
+        }
+    };
+    // warp-uniform branches on the longest run
+    if (longest <= 4u) {
+        scatter(std::integral_constant<int, 2>{});
+    } else if (longest <= 8u) {
+        scatter(std::integral_constant<int, 3>{});
+    } else if (longest <= 16u) {
+        scatter(std::integral_constant<int, 4>{});
+    } else {
+        if (lane == 0u) { atomicAdd(status + 2, 1u); }
+        scatter(std::integral_constant<int, 5>{});
     }
-    p2g_scatter(k, sc, valid, s, vv, Q, grid, status + 2);
+    if (solo) {
+        float4* const base0 = grid + (size_t)sc0.goff + (size_t)s0.by * (size_t)sc0.nx + (size_t)s0.bx;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const int i = q % 3, j = q / 3;
+            float2 c = make_float2(0.f, 0.f);
+            float cm = 0.f;
+            p2g_term(k, s0, v0, Q0, i, j, c, cm);
+            atomicAdd(base0 + (size_t)j * (size_t)sc0.nx + i, make_float4(c.x, c.y, cm, 0.f));
+        }
+    }
 }
 
 // gridKernel, MPM.cu:131-177 (in place)
@@ -809,10 +840,10 @@ int32_t launch_p2g_t(gpe_mpm* s, float4* grid, cudaStream_t st)
 {
     const int c = s->cur;
     if (s->scenes.size() > 1) {
-        k_p2g<MODE, true><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+        k_p2g<MODE, true><<<mblocks((lsz(s) + 1) / 2), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
                                                             s->mat[c], s->sid[c], grid, s->status);
     } else {
-        k_p2g<MODE, false><<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
+        k_p2g<MODE, false><<<mblocks((lsz(s) + 1) / 2), T_MPM, 0, st>>>(s->k, s->x[c], s->v[c], s->C[c], s->F[c], s->J[c],
                                                              s->mat[c], nullptr, grid, s->status);
     }
     GPE_CHECK_LAUNCH("k_p2g");

@@ -583,7 +583,8 @@ class Mpm:
         return v.value
 
     def p2g_wide_warps(self, stream=None) -> int:
-        """Warps whose P2G needed the 5-round run reduction since the last call (read and cleared)."""
+        """Warps whose P2G needed the 5-round run reduction since the last call (read and cleared); a warp
+        holds 64 particles, two per lane."""
         v = C.c_uint32()
         check(lib().gpe_mpm_p2g_wide_warps(self.h, C.byref(v), stream), "gpe_mpm_p2g_wide_warps")
         return v.value

@@ -498,8 +498,10 @@ int32_t gpe_mpm_get_grid(gpe_mpm* mpm, float* dst, int64_t n_nodes, int32_t mem,
 int32_t gpe_mpm_status(gpe_mpm* mpm, uint32_t* status, void* stream);
 /* Diagnostic without a counterpart in the reference (whose P2G, MPM.cu:116-126, issues one global atomic per
  * node and particle): reads and clears the number of warps whose P2G summed their particles' node
- * contributions with the 5-round segmented reduction, i.e. held a run of more than 16 consecutive particles
- * sharing one stencil base node (scenes at about 30 particles per cell), since the last call. */
+ * contributions with the 5-round segmented reduction since the last call. A P2G warp holds 64 consecutive
+ * particles, two per lane; it needs 5 rounds when more than 16 consecutive lanes share the stencil base node
+ * of their second particle (about 33 or more particles on one base node: scenes at about 30 particles per
+ * cell). */
 int32_t gpe_mpm_p2g_wide_warps(gpe_mpm* mpm, uint32_t* count, void* stream);
 int32_t gpe_mpm_launches_per_step(const gpe_mpm* mpm, int32_t* launches);
 /* Appends the hose's particles at the live count (MPMEmitterKernel, MPM.cu:380-438): C = 0, F = I, J = 1

@@ -9,8 +9,8 @@ parameters and tunings as bench.py — rather than on small scenes only:
     tuning (cell h, 128 threads): one step against the oracle, and three steps bit for bit against every
     scene run alone;
   * MLS-MPM, 65,536 fixed-corotated particles on 128^2 nodes (32 per cell, re-sorted by cell): P2G node
-    fields and one step against the oracle, with the P2G taking its 5-round run reduction (runs of more than
-    16 particles on one stencil base node);
+    fields and one step against the oracle, with the P2G taking its 5-round run reduction (two particles per
+    lane, runs of more than 16 lanes on one stencil base node);
   * MLS-MPM, 4,194,304 mixed-material particles (water, snow, jelly) on 1024^2 nodes: P2G node fields and
     one step against the oracle.
 
@@ -134,8 +134,9 @@ def test_mpm_65k_elastic_32_per_cell(gpe_mod, oracle, cuda_ok):
     e.stage(gpe_mod.MPM_STAGE_P2G)
     wide = e.p2g_wide_warps()
     _grid_close(e.grid(), o.p2g(pos, vel, C0, F0, J0))
-    # the warps with a run longer than 16 particles, counted on the host from the sorted base nodes: the
-    # device took the 5-round reduction in exactly those
+    # the warps with a run longer than 16 lanes, counted on the host from the sorted base nodes: the device
+    # took the 5-round reduction in exactly those. A warp holds 64 particles, two per lane; a lane's run key
+    # is the base node of its second particle
     # (the device's stencil: g = fma(x, 1/dx, offset) in FP32, base = floor(g - 0.5); the product of two
     # floats is exact in double, so one rounding to float32 reproduces the fma)
     inv_dx = np.float32(1.0) / np.float32(p.dx)
@@ -143,8 +144,8 @@ def test_mpm_65k_elastic_32_per_cell(gpe_mod, oracle, cuda_ok):
     base = np.floor(g - np.float32(0.5)).astype(np.int64)
     key = np.sort(base[:, 1] * p.nx + base[:, 0], kind="stable")
     want_wide = 0
-    for w in range(0, n, 32):
-        k = key[w:w + 32]
+    for w in range(0, n, 64):
+        k = key[w + 1:w + 64:2]
         runs = np.diff(np.flatnonzero(np.concatenate([[True], k[1:] != k[:-1], [True]])))
         want_wide += int(runs.max() > 16)
     assert want_wide > 100
