@@ -569,13 +569,15 @@ def batched_leg(args, stream, flush_l2):
 def mpm_leg(args, stream, flush_l2):
     """MLS-MPM, timed like the headline (graph-launched steps, L2 flushed before each):
     mixed: 4,194,304 particles (a third each of water, snow and jelly in seeded discs) on a 1024^2 grid,
-           dt = 5e-5, spatial re-sort every 16 steps; algorithmic bytes 136 per particle (x, v, C, F, J,
+           dt = 5e-5, spatial re-sort every 32 steps; algorithmic bytes 136 per particle (x, v, C, F, J,
            material and plastic state read and written once) plus 64 per grid node;
     library: the same grid and particle count with a fifth each of water, jelly, snow, Neo-Hookean and
            Drucker-Prager sand (two discs each);
     elastic: 65,536 fixed-corotated particles in two squares on a 128^2 grid (32 per cell), dt = 1e-4,
            re-sorted every 16 steps (launch-bound);
-    batched_32: 32 mixed scenes of 64k-512k particles in one engine (batched_mpm)."""
+    batched_32: 32 mixed scenes of 64k-512k particles in one engine (batched_mpm).
+    Each scene is timed over at least one re-sort interval of steps (so the re-sort's cost enters the mean at
+    its own frequency) and at least --steps steps."""
     import torch
 
     import gpe
@@ -591,7 +593,8 @@ def mpm_leg(args, stream, flush_l2):
         for _ in range(args.warmup):
             e.step(1, stream=sh)
         torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        steps = max(args.steps, p.sort_interval)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         for a, b in ev:
             flush_l2()
             a.record(stream)
@@ -602,10 +605,10 @@ def mpm_leg(args, stream, flush_l2):
         st = e.status()
         launches = e.launches_per_step()
         e.close()
-        gbs = alg_bytes * args.steps / s / 1e9
-        return {"particles": n, "value": n * args.steps / s, "unit": "particle-steps/s",
-                "ms_per_step": 1e3 * s / args.steps, "alg_bytes_per_step": alg_bytes, "effective_gbs": gbs,
-                "hbm_frac": gbs / peak, "launches_per_step": launches, "status": st}
+        gbs = alg_bytes * steps / s / 1e9
+        return {"particles": n, "value": n * steps / s, "unit": "particle-steps/s", "steps": steps,
+                "sort_interval": p.sort_interval, "ms_per_step": 1e3 * s / steps, "alg_bytes_per_step": alg_bytes,
+                "effective_gbs": gbs, "hbm_frac": gbs / peak, "launches_per_step": launches, "status": st}
 
     out = {}
     n = 4194304
@@ -652,7 +655,7 @@ def batched_mpm(timed, sh, stream):
             e.step(1, stream=sh)
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 10
+    reps = max(10, p.sort_interval)  # one re-sort interval, as the batched engine is timed
     a.record(stream)
     for _ in range(reps):
         for e in solo:
