@@ -83,6 +83,26 @@ def test_p2g_stage(gpe_mod, oracle, cuda_ok, kind):
     assert e.status() == 0
 
 
+@pytest.mark.parametrize("sort", [False, True])
+def test_p2g_odd_count_sorted_and_unsorted(gpe_mod, oracle, cuda_ok, sort):
+    """P2G takes two consecutive particles per thread: an odd count leaves the last thread one particle;
+    unsorted input puts almost every pair across a run boundary (the first particle scattered on its own),
+    sorted input joins most pairs and makes long runs."""
+    p, x, v, Cm, F, J, mat = _scene("corotated")
+    n = 4093
+    x, v, Cm, F, J = x[:n], v[:n], Cm[:n], F[:n], J[:n]
+    e = _engine(gpe_mod, p, x, v, Cm, F, J, mat)
+    e.stage(gpe_mod.MPM_STAGE_CLEAR)
+    if sort:
+        e.stage(gpe_mod.MPM_STAGE_SORT)
+    e.stage(gpe_mod.MPM_STAGE_P2G)
+    g = e.grid()
+    want = oracle.MpmOracle(p).p2g(x, v, Cm, F, J, mat)
+    _close(g[:, 2], want[:, 2], np.abs(want[:, 2]).max(), "grid mass")
+    _close(g[:, :2], want[:, :2], np.abs(want[:, :2]).max(), "grid momentum", rel=2e-5)
+    assert e.status() == 0
+
+
 @pytest.mark.parametrize("kind", KINDS)
 def test_grid_and_g2p_stages(gpe_mod, oracle, cuda_ok, kind):
     p, x, v, Cm, F, J, mat = _scene(kind)
