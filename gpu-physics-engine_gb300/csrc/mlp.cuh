@@ -88,17 +88,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}\n"
-                 : "=r"(ok)
-                 : "r"(saddr(bar)), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-
 __device__ __forceinline__ uint64_t globaltimer()
 {
     uint64_t t;
@@ -107,13 +96,25 @@ __device__ __forceinline__ uint64_t globaltimer()
 }
 
 // Waits for the completion of the barrier phase of the given parity; false after MLP_WAIT_NS without it.
+// try_wait suspends the thread until the phase completes or a hardware time limit passes; the loop around it
+// checks the global timer between tries.
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(ok)
+                 : "r"(saddr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {
-    if (mbar_test(bar, parity)) { return true; }
+    if (mbar_try(bar, parity)) { return true; }
     const uint64_t t0 = globaltimer();
-    while (!mbar_test(bar, parity)) {
+    while (!mbar_try(bar, parity)) {
         if (globaltimer() - t0 > MLP_WAIT_NS) { return false; }
-        __nanosleep(64);
     }
     return true;
 }
