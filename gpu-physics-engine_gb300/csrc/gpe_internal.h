@@ -65,7 +65,7 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
 int32_t scan_launches(uint32_t n_keys);
 // bucket[start[key] + rank] = i for every (key, rank) pair. n sizes the launch; with n_dev the kernel takes
 // the live count from the device (which must not exceed n).
-int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket,
+int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, uint32_t ncells,
                        cudaStream_t st, const int32_t* n_dev = nullptr);
 
 

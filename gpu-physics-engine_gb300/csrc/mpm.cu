@@ -916,7 +916,7 @@ int32_t mpm_sort(gpe_mpm* s, cudaStream_t st)
     GPE_CHECK_LAUNCH("k_mpm_key");
     int32_t rc = launch_exclusive_scan(s->count, (uint32_t)s->nn, s->bsum, s->start, st);
     if (rc) { return rc; }
-    rc = launch_scatter(s->keyrank, lsz(s), s->start, s->bucket, st, s->d_count);
+    rc = launch_scatter(s->keyrank, lsz(s), s->start, s->bucket, (uint32_t)s->nn, st, s->d_count);
     if (rc) { return rc; }
     k_mpm_gather<<<mblocks(lsz(s)), T_MPM, 0, st>>>(s->d_count, s->keyrank, s->start, s->bucket, s->x[c], s->v[c],
                                                    s->C[c], s->F[c], s->J[c], s->mat[c], s->id[c], s->x[o],

@@ -61,6 +61,11 @@ struct PbfK {
     uint8_t* mflag;
     float skin2;              // (h + skin)^2
     float move2;              // (skin / (2 iters))^2, shrunk by 1%
+    // set for the XSPH pass of a step that also computes the next step's predicted cell keys and their
+    // histogram (from the positions and velocities it writes); null otherwise
+    uint2* hist_kr;
+    uint32_t* hist_cnt;
+    uint32_t ncells;          // sort cells of all scenes (the placement's bounds checks)
 };
 
 
@@ -345,31 +350,41 @@ __device__ __forceinline__ float2 predict(const PbfK& k, float2 p, float2 w)
 
 // Lanes of a warp that share a cell take consecutive ranks in lane order from one atomicAdd. All lanes of
 // the warp call it; `valid` marks those that carry particle i.
-template <bool MULTI>
-__device__ __forceinline__ void predict_hist_one(const PbfK& k, const DomDev* __restrict__ doms,
-                                                 const int32_t* __restrict__ dom, const float2* __restrict__ x,
-                                                 const float2* __restrict__ v, uint2* __restrict__ keyrank,
-                                                 uint32_t* __restrict__ count, int32_t i, bool valid)
+// The rank of particle i among the particles of its cell key: lanes with the same key add their number to
+// the cell's count with one atomic (the leader's), and each takes its place after the lanes before it. All
+// lanes of the warp call it; valid marks those that carry a particle.
+__device__ __forceinline__ void hist_rank(uint32_t key, bool valid, uint2* __restrict__ keyrank,
+                                          uint32_t* __restrict__ count, int32_t i)
 {
-    const int32_t lane = threadIdx.x & 31;
-    uint32_t key       = 0xffffffffu;
-    float2 ps          = make_float2(0.f, 0.f);
-    if (valid) {
-        const DomDev d = load_dom<MULTI>(k, doms, dom, i);
-        ps             = predict(k, x[i], v[i]);
-        const int32_t cx = cell_coord(ps.x, d.ox, k.inv_cell, d.ncx);
-        const int32_t cy = cell_coord(ps.y, d.oy, k.inv_cell, d.ncy);
-        key              = d.coff + (uint32_t)cy * (uint32_t)d.ncx + (uint32_t)cx;
-    }
-    const uint32_t peers  = __match_any_sync(0xffffffffu, key);
-    const int32_t leader  = __ffs(peers) - 1;
-    uint32_t base         = 0;
+    const int32_t lane   = threadIdx.x & 31;
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const int32_t leader = __ffs(peers) - 1;
+    uint32_t base        = 0;
     if (valid && lane == leader) { base = atomicAdd(&count[key], (uint32_t)__popc(peers)); }
     base = __shfl_sync(0xffffffffu, base, leader);
     if (valid) {
         const uint32_t rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
         keyrank[i]          = make_uint2(key, rank);
     }
+}
+
+// the sort cell key of predicted position ps in scene d
+__device__ __forceinline__ uint32_t cell_key(const PbfK& k, const DomDev& d, float2 ps)
+{
+    const int32_t cx = cell_coord(ps.x, d.ox, k.inv_cell, d.ncx);
+    const int32_t cy = cell_coord(ps.y, d.oy, k.inv_cell, d.ncy);
+    return d.coff + (uint32_t)cy * (uint32_t)d.ncx + (uint32_t)cx;
+}
+
+template <bool MULTI>
+__device__ __forceinline__ void predict_hist_one(const PbfK& k, const DomDev* __restrict__ doms,
+                                                 const int32_t* __restrict__ dom, const float2* __restrict__ x,
+                                                 const float2* __restrict__ v, uint2* __restrict__ keyrank,
+                                                 uint32_t* __restrict__ count, int32_t i, bool valid)
+{
+    uint32_t key = 0xffffffffu;
+    if (valid) { key = cell_key(k, load_dom<MULTI>(k, doms, dom, i), predict(k, x[i], v[i])); }
+    hist_rank(key, valid, keyrank, count, i);
 }
 
 template <bool MULTI>
@@ -400,12 +415,17 @@ __device__ __forceinline__ void place_one(const PbfK& k, const uint2* __restrict
                                           const float* __restrict__ acc_in, float* __restrict__ prev_out,
                                           float* __restrict__ lam_out, int32_t i)
 {
-    const uint2 kr   = keyrank[i];
+    const uint2 kr = keyrank[i];
+    // the keys, the starts and the buckets come from one histogram; the bounds checks only keep an
+    // inconsistent set (a caller's bug) from reading or writing outside the arrays
+    const uint32_t n = (uint32_t)count_of(k);
+    if (kr.x >= k.ncells) { return; }
     const uint32_t s = ldn<CG>(&start[kr.x]);
-    const uint32_t e = ldn<CG>(&start[kr.x + 1]);
+    const uint32_t e = min(ldn<CG>(&start[kr.x + 1]), n);
     uint32_t rank    = 0;
     for (uint32_t t = s; t < e; ++t) { rank += (ldn<CG>(&bucket[t]) < (uint32_t)i) ? 1u : 0u; }
     const uint32_t dst = s + rank;
+    if (dst >= n) { return; }
     const float2 p     = x_in[i];
     const float2 ps    = predict(k, p, v_in[i]);
     if (xd_out) {
@@ -889,7 +909,7 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
                                          const int32_t* __restrict__ dom, const uint32_t* __restrict__ start,
                                          const float4* __restrict__ xd, float2* __restrict__ x_out,
                                          float2* __restrict__ v_out, float* __restrict__ omega,
-                                         uint32_t* __restrict__ status, int32_t i)
+                                         uint32_t* __restrict__ status, int32_t i, uint32_t* next_key = nullptr)
 {
     const DomDev d  = load_dom<MULTI>(k, doms, dom, i);
     const float4 p4 = xd[i];
@@ -939,6 +959,8 @@ __device__ __forceinline__ void xsph_one(const PbfK& k, const DomDev* __restrict
     v_out[i] = make_float2(vx, vy);
     x_out[i] = p; // the step's end position, in this step's sorted order
     if (VORT) { omega[i] = w; }
+    // the next step's predicted cell, from the values just written (as k_predict_hist would read them)
+    if (next_key) { *next_key = cell_key(k, d, predict(k, p, make_float2(vx, vy))); }
 }
 
 template <bool MULTI, bool VORT, int MASK>
@@ -947,8 +969,19 @@ __global__ void __launch_bounds__(T_MAX)
            const uint32_t* __restrict__ start, const float4* __restrict__ xd, float2* __restrict__ x_out,
            float2* __restrict__ v_out, float* __restrict__ omega, uint32_t* __restrict__ status)
 {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count_of(k)) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, xd, x_out, v_out, omega, status, i); }
+    const int32_t i  = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < count_of(k);
+    if (!k.hist_cnt) { // uniform
+        if (valid) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, xd, x_out, v_out, omega, status, i); }
+        return;
+    }
+    // XSPH of a step followed by another step without anything in between: the next step's cell keys and
+    // histogram come from here, and its sort starts with the scan (bit for bit what k_predict_hist computes
+    // from the same positions and velocities; only the order of the atomic ranks within a cell differs, which
+    // the stable placement does not depend on)
+    uint32_t key = 0xffffffffu;
+    if (valid) { xsph_one<MULTI, VORT, false, MASK>(k, doms, dom, start, xd, x_out, v_out, omega, status, i, &key); }
+    hist_rank(key, valid, k.hist_kr, k.hist_cnt, i);
 }
 
 // ----- vorticity confinement (Macklin & Mueller 2013 eq. 16) --------------------------------------------
@@ -1581,6 +1614,7 @@ using namespace gpe;
 struct PbfGraph {
     cudaGraphExec_t exec = nullptr;
     int id_end;
+    bool hist_end; // the last step's XSPH left the next step's keys and histogram
 };
 
 struct gpe_pbf {
@@ -1635,6 +1669,8 @@ struct gpe_pbf {
     uint4* nmask      = nullptr;  // candidate masks of the current step
     uint8_t* mflag    = nullptr;  // per cell: a particle of its 3 x 3 cells moved too far for the masks
     bool masks_valid  = false;    // the masks were made in this step
+    bool hist_ready   = false;    // the last step's XSPH left the next step's cell keys and histogram
+    bool count_dirty  = false;    // ... and was dropped: the histogram array must be cleared before a sort
     int32_t dp_since_build = 0;   // delta p passes since they were made
     int32_t mask_passes = 1;      // delta p passes the move threshold k.move2 allows for
 
@@ -1719,6 +1755,7 @@ PbfK make_k(const gpe_pbf_params& p)
 void bind_k(gpe_pbf* s)
 {
     s->k.n_dev       = s->d_count;
+    s->k.ncells      = s->ncells;
     s->k.keys        = s->keys;
     s->k.nmask       = s->nmask;
     s->k.mflag       = s->mflag;
@@ -1805,6 +1842,26 @@ unsigned nblk(const gpe_pbf* s) { return (unsigned)((lsize(s) + s->block - 1) / 
 
 // ----- stage launchers ----------------------------------------------------------------------------------
 
+// A call other than a step may change what the next step sorts (positions, velocities, count, parameters,
+// cells): a histogram left by the last step's XSPH is dropped, and the next sort clears the histogram
+// array before building its own (clear_hist).
+void drop_hist(gpe_pbf* s)
+{
+    if (s->hist_ready) {
+        s->hist_ready  = false;
+        s->count_dirty = true;
+    }
+}
+
+int32_t clear_hist(gpe_pbf* s, cudaStream_t st)
+{
+    if (s->count_dirty) {
+        GPE_TRY_CUDA(cudaMemsetAsync(s->count, 0, sizeof(uint32_t) * (size_t)s->cells_cap, st));
+        s->count_dirty = false;
+    }
+    return GPE_OK;
+}
+
 int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
 {
     s->masks_valid  = false;
@@ -1812,7 +1869,12 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     s->XS           = 0;
     s->XO           = 1;
     s->k.n = (int32_t)s->n;
-    if (n > 0) {
+    // the previous step's XSPH may already have computed the keys and the histogram (hist_ready)
+    const bool fused = s->hist_ready;
+    s->hist_ready    = false;
+    const int32_t rch = clear_hist(s, st);
+    if (rch) { return rch; }
+    if (n > 0 && !fused) {
         if (multi(s)) {
             k_predict_hist<true><<<blocks_for(n), T_PART, 0, st>>>(s->k, s->d_doms, s->dom, s->pos, s->vel,
                                                                    s->keyrank, s->count);
@@ -1825,7 +1887,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
     // the scan also clears the candidate masks' cell marks for this step
     int32_t rc = launch_exclusive_scan(s->count, s->ncells, s->bsum, s->start, st, masks_on(s) ? s->mflag : nullptr);
     if (rc) { return rc; }
-    rc = launch_scatter(s->keyrank, n, s->start, s->bucket, st, s->d_count);
+    rc = launch_scatter(s->keyrank, n, s->start, s->bucket, (uint32_t)s->ncells, st, s->d_count);
     if (rc) { return rc; }
     if (n > 0) {
         const bool ids = (s->prm.flags & (GPE_PBF_TRACK_IDS | GPE_PBF_PAIR_IDS)) != 0;
@@ -1839,7 +1901,7 @@ int32_t stage_predict_sort(gpe_pbf* s, cudaStream_t st)
         if (ids) { s->id_cur ^= 1; }
     }
     s->have_sort = true;
-    s->launches += 3 + scan_launches(s->ncells); // predict + histogram, scan, scatter, place
+    s->launches += (fused ? 2 : 3) + scan_launches(s->ncells); // [predict + histogram,] scan, scatter, place
     return GPE_OK;
 }
 
@@ -2017,16 +2079,26 @@ int32_t stage_delta_p(gpe_pbf* s, cudaStream_t st, bool accinit)
     return GPE_OK;
 }
 
-int32_t stage_xsph(gpe_pbf* s, cudaStream_t st)
+// next_hist: the step is followed by another with nothing in between (and no vorticity pass after XSPH):
+// XSPH also computes the next step's cell keys and histogram, and the next sort skips k_predict_hist.
+int32_t stage_xsph(gpe_pbf* s, cudaStream_t st, bool next_hist = false)
 {
     if (lsize(s) == 0) { return GPE_OK; }
     const int vort = s->prm.vort_eps != 0.f ? 1 : 0;
-    GPE_TRY_CUDA(kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, s->k, s->d_doms, s->dom, s->start,
+    PbfK kk        = s->k;
+    next_hist      = next_hist && vort == 0;
+    if (next_hist) {
+        kk.hist_kr  = s->keyrank;
+        kk.hist_cnt = s->count; // zeroed by this step's scan
+    }
+    GPE_TRY_CUDA(kXs[multi(s) ? 1 : 0][vort](nblk(s), (unsigned)s->block, st, kk, s->d_doms, s->dom, s->start,
                                              s->xd[s->XS], s->pos, s->vel, s->omega, s->status,
                                              s->masks_valid ? MASK_USE : MASK_OFF));
     s->launches += 1;
+    s->hist_ready = next_hist;
     return GPE_OK;
 }
+
 
 int32_t stage_vorticity(gpe_pbf* s, cudaStream_t st)
 {
@@ -2149,6 +2221,9 @@ const void* step_kernel_k(bool m, bool sg, bool sc, bool v)
 
 int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
 {
+    drop_hist(s); // its sort phases build their own histogram
+    const int32_t rch = clear_hist(s, st);
+    if (rch) { return rch; }
     s->masks_valid = false;
     s->XS  = 0;
     s->XO  = 1;
@@ -2200,7 +2275,8 @@ int32_t stage_step_persistent(gpe_pbf* s, cudaStream_t st)
     return GPE_OK;
 }
 
-int32_t run_step(gpe_pbf* s, cudaStream_t st)
+// next_hist: another step follows directly (see stage_xsph)
+int32_t run_step(gpe_pbf* s, cudaStream_t st, bool next_hist = false)
 {
     const bool acc = accumulating(s);
     if (s->step_kernel && s->persistent && !acc) {
@@ -2231,7 +2307,7 @@ int32_t run_step(gpe_pbf* s, cudaStream_t st)
             if (rc == GPE_OK) { rc = stage_delta_p(s, st, false); }
         }
     }
-    if (rc == GPE_OK) { rc = stage_xsph(s, st); }
+    if (rc == GPE_OK) { rc = stage_xsph(s, st, next_hist && !s->collecting); }
     if (rc == GPE_OK) { rc = stage_vorticity(s, st); }
     if (rc == GPE_OK && s->collecting && s->col.stride != 0u && lsize(s) > 0) {
         k_collect_targets<<<blocks_for(lsize(s)), T_PART, 0, st>>>(s->col.cnt, s->col.X, s->col.T, s->col.idx,
@@ -2398,6 +2474,7 @@ int32_t gpe_pbf_set_params(gpe_pbf* s, const gpe_pbf_params* params)
         gpe::set_error(GPE_ERR_BAD_ARG, "gpe_pbf_set_params: the sort-cell size is fixed at creation");
         return GPE_ERR_BAD_ARG;
     }
+    drop_hist(s);
     s->prm     = *params;
     s->dynamic = (params->flags & GPE_PBF_DYNAMIC_COUNT) != 0;
     build_domains(s);
@@ -2440,6 +2517,7 @@ int32_t gpe_pbf_set_state(gpe_pbf* s, const float* pos, const float* vel, const 
         }
     }
     cudaStream_t st = as_stream(stream);
+    drop_hist(s);
     s->XS = s->XO   = -1;
     s->id_cur     = 0;
     if (n > 0) {
@@ -2546,13 +2624,15 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
         const int32_t iters = s->prm.iters;
         s->prm.iters        = gpe::mlp_pair_iters(s->mlp);
         s->launches         = 0;
-        const int32_t rc    = run_step(s, st);
+        const int32_t rc    = run_step(s, st, true);
         s->prm.iters        = iters;
         if (rc) { return rc; }
         if (--n_steps == 0) { return GPE_OK; }
     }
-    // the step sequence is captured once per (steps, starting buffer roles) and replayed as one graph
-    const auto key = std::make_tuple(n_steps, 0, s->id_cur);
+    // the step sequence is captured once per (steps, whether the first sort's histogram is already there,
+    // starting buffer roles) and replayed as one graph; every step but none in between leaves the next
+    // step's keys and histogram (stage_xsph)
+    const auto key = std::make_tuple(n_steps, (s->hist_ready ? 1 : 0) + (s->count_dirty ? 2 : 0), s->id_cur);
     auto it        = s->graphs.find(key);
     if (it == s->graphs.end()) {
         cudaStream_t cap_st = st;
@@ -2561,16 +2641,20 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
             GPE_TRY_CUDA(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
             own = true;
         }
-        const int id0 = s->id_cur;
+        const int id0    = s->id_cur;
+        const bool hist0 = s->hist_ready, dirty0 = s->count_dirty;
         GPE_TRY_CUDA(cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
         s->launches = 0;
         int32_t rc  = GPE_OK;
-        for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, cap_st); }
+        for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, cap_st, true); }
         cudaGraph_t graph = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(cap_st, &graph);
         PbfGraph pg;
-        pg.id_end = s->id_cur;
-        s->id_cur = id0;
+        pg.id_end     = s->id_cur;
+        pg.hist_end   = s->hist_ready;
+        s->id_cur     = id0;
+        s->hist_ready = hist0;
+        s->count_dirty = dirty0;
         if (rc == GPE_OK && ce != cudaSuccess) {
             gpe::set_cuda_error(ce, "cudaStreamEndCapture");
             rc = GPE_ERR_CUDA;
@@ -2589,8 +2673,10 @@ int32_t gpe_pbf_step(gpe_pbf* s, int32_t n_steps, void* stream)
         it = s->graphs.emplace(key, pg).first;
     }
     GPE_TRY_CUDA(cudaGraphLaunch(it->second.exec, st));
-    s->id_cur    = it->second.id_end;
-    s->have_sort = true;
+    s->id_cur      = it->second.id_end;
+    s->hist_ready  = it->second.hist_end;
+    s->count_dirty = false; // the graph's first sort cleared it
+    s->have_sort  = true;
     return GPE_OK;
 }
 
@@ -2601,6 +2687,7 @@ int32_t gpe_pbf_stage(gpe_pbf* s, int32_t stage, void* stream)
     if (!s->have_state) { return GPE_ERR_NOT_READY; }
     cudaStream_t st = as_stream(stream);
     const bool in_step = s->XS >= 0;
+    if (stage != GPE_PBF_STAGE_DENSITY) { drop_hist(s); } // the density pass reads positions and cell starts
     switch (stage) {
         case GPE_PBF_STAGE_PREDICT_SORT:
             if (in_step) { break; }
@@ -2766,6 +2853,7 @@ int32_t gpe_pbf_get_field(gpe_pbf* s, int32_t field, void* dst, int64_t n_elems,
     if (n > 0) {
         if (f.kind == 1) {
             // x* = x + d into the sort's (key, rank) scratch, which is free within a step, then out
+            drop_hist(s); // the next step's keys may be waiting there
             float2* tmp = reinterpret_cast<float2*>(s->keyrank);
             k_xd_pred<<<blocks_for((int64_t)n), T_PART, 0, st>>>(static_cast<const float4*>(f.p), tmp, (int32_t)n);
             GPE_CHECK_LAUNCH("k_xd_pred");
@@ -2790,6 +2878,7 @@ int32_t gpe_pbf_set_field(gpe_pbf* s, int32_t field, const void* src, int64_t n_
         return GPE_ERR_BAD_ARG;
     }
     s->masks_valid = false; // a written position (or anything else) may move a particle past its masks
+    drop_hist(s);
     FieldLoc f{};
     int32_t rc = field_ptr(s, field, &f);
     if (rc) { return rc; }
@@ -2836,9 +2925,11 @@ int32_t gpe_pbf_launches_per_step(const gpe_pbf* s, int32_t* launches)
         *launches = (s->step_kernel ? 0 : sorted) + 1 + (vort ? 2 : 0);
         return GPE_OK;
     }
-    // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network
+    // GPE_WARM_PREV: lambda_prev is placed by the sort; GPE_WARM_MLP: features, then the network. Without
+    // vorticity the previous step's XSPH computes the keys and histogram of consecutive steps (one launch
+    // fewer).
     const int32_t first = (warm && s->warm == GPE_WARM_PREV) ? -1 : ((warm && s->warm == GPE_WARM_MLP) ? 1 : 0);
-    *launches = sorted + 2 * s->prm.iters + 1 + (vort ? 1 : 0) + first;
+    *launches = sorted - (vort ? 0 : 1) + 2 * s->prm.iters + 1 + (vort ? 1 : 0) + first;
     return GPE_OK;
 }
 
@@ -2883,6 +2974,7 @@ extern "C" int32_t gpe_pbf_emit(gpe_pbf* s, const gpe_hose* hose, uint64_t seed,
         gpe::set_error(GPE_ERR_NOT_READY, "gpe_pbf_emit: a step is in progress (stage API)");
         return GPE_ERR_NOT_READY;
     }
+    drop_hist(s); // the new particles are not in the histogram the last step may have left
     HoseK h{};
     const int32_t cnt = make_hose(*hose, s->prm.dt, seed, &h);
     if (requested) { *requested = cnt; }
@@ -2948,6 +3040,7 @@ extern "C" int32_t gpe_pbf_publish_chunks(gpe_pbf* s, const gpe_chunk_state* sta
     }
     cudaStream_t st     = as_stream(stream);
     const size_t chunks = (size_t)c.chunks_x * (size_t)c.chunks_y;
+    drop_hist(s); // the chunk sort uses the (key, rank) array, where the next step's keys may be waiting
     GPE_TRY_CUDA(cudaMemsetAsync(c.offsets, 0, sizeof(uint32_t) * chunks * (size_t)(c.chunk_cells * c.chunk_cells), st));
     const int64_t n = lsize(s);
     if (n > 0) {
@@ -2974,9 +3067,12 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
         return GPE_ERR_NOT_READY;
     }
     cudaStream_t st   = as_stream(stream);
-    const int id0     = s->id_cur;
-    int32_t rc        = GPE_OK;
-    for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, st); }
+    // the recorded sequence may be replayed after anything: it starts from the full sort and leaves no
+    // histogram behind (its last step's XSPH computes none)
+    drop_hist(s);
+    int32_t rc    = GPE_OK;
+    const int id0 = s->id_cur;
+    for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, st, k + 1 < n_steps); }
     if (rc) { return rc; }
     // return the id buffer role to where it started, so the recorded sequence can be replayed (positions stay
     // in one buffer: every step writes its end positions where it read its start positions)
@@ -3004,6 +3100,7 @@ int32_t apply_tuning(gpe_pbf* s, const gpe_pbf_tuning& t)
                        "gpe_pbf_set_tuning: block must be 128, 256 or 512, persistent 0, 1 or 2, skin in [0, 1]");
         return GPE_ERR_BAD_ARG;
     }
+    drop_hist(s);
     const float c_old = s->prm.cell > 0.f ? s->prm.cell : s->prm.h;
     const float c_new = t.cell > 0.f ? t.cell : s->prm.h;
     if (c_new != c_old) {
@@ -3193,6 +3290,7 @@ extern "C" int32_t gpe_pbf_set_warm_start(gpe_pbf* s, int32_t mode, const gpe_ml
         return GPE_ERR_BAD_ARG;
     }
     if (s->XS >= 0) { return GPE_ERR_NOT_READY; }
+    drop_hist(s);
     if (mode == GPE_WARM_MLP) {
         // the network kernel's tiles live in shared memory: prefer the largest carveout so that 6 CTAs fit
         GPE_TRY_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k_mlp_apply),
@@ -3240,6 +3338,7 @@ extern "C" int32_t gpe_mlp_collect(gpe_mlp* m, gpe_pbf* s, int32_t n_steps, int3
     cudaStream_t st       = as_stream(stream);
     const gpe::MlpData md = gpe::mlp_data(m);
     GPE_TRY_CUDA(cudaMemsetAsync(s->acc, 0, sizeof(float) * (size_t)s->cap, st));
+    drop_hist(s);
     uint64_t rs   = seed;
     int32_t rc    = GPE_OK;
     s->collecting = true;
@@ -3390,6 +3489,7 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     d.coff = 0;
     k.d0   = d;
     k.n    = (int32_t)n;
+    k.ncells = (uint32_t)cells;
 
     cudaStream_t st = as_stream(stream);
     // the histogram must start at zero whatever an earlier (possibly failed) call left behind
@@ -3404,7 +3504,7 @@ extern "C" int32_t gpe_pbf_predict_sort_noalloc(const gpe_pbf_params* params, co
     rc = launch_exclusive_scan(count, (uint32_t)cells, bsum, cell_start, st);
     if (rc) { return rc; }
     if (n > 0) {
-        rc = launch_scatter(keyrank, n, cell_start, bucket, st);
+        rc = launch_scatter(keyrank, n, cell_start, bucket, (uint32_t)cells, st);
         if (rc) { return rc; }
         k_place<<<blocks_for(n), T_PART, 0, st>>>(k, keyrank, cell_start, bucket,
                                                   reinterpret_cast<const float2*>(pos),

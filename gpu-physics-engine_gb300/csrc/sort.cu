@@ -187,14 +187,18 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(uint32_t* __restrict__ cou
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) { start[M] = prefix + total; }
 }
 
+// The keys and ranks come from the same histogram as the starts; the bounds checks only keep an
+// inconsistent pair (a caller's bug) from writing outside the arrays.
 __global__ void k_scatter(const uint2* __restrict__ keyrank, int64_t n_host, const int32_t* __restrict__ n_dev,
-                          const uint32_t* __restrict__ start, uint32_t* __restrict__ bucket)
+                          const uint32_t* __restrict__ start, uint32_t* __restrict__ bucket, uint32_t ncells)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = n_dev ? (int64_t)__ldg(n_dev) : n_host;
     if (i >= n) { return; }
-    const uint2 kr                  = keyrank[i];
-    bucket[__ldg(&start[kr.x]) + kr.y] = (uint32_t)i;
+    const uint2 kr = keyrank[i];
+    if (kr.x >= ncells) { return; }
+    const uint32_t dst = __ldg(&start[kr.x]) + kr.y;
+    if ((int64_t)dst < n) { bucket[dst] = (uint32_t)i; }
 }
 
 } // namespace
@@ -224,12 +228,12 @@ int32_t launch_exclusive_scan(uint32_t* count, uint32_t n_keys, uint32_t* bsum, 
 
 int32_t scan_launches(uint32_t n_keys) { return scan_blocks(n_keys) <= FUSED_MAX_TILES ? 2 : 3; }
 
-int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, cudaStream_t st,
-                       const int32_t* n_dev)
+int32_t launch_scatter(const uint2* keyrank, int64_t n, const uint32_t* start, uint32_t* bucket, uint32_t ncells,
+                       cudaStream_t st, const int32_t* n_dev)
 {
     if (n <= 0) { return GPE_OK; }
     const int T = 256;
-    k_scatter<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(keyrank, n, n_dev, start, bucket);
+    k_scatter<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(keyrank, n, n_dev, start, bucket, ncells);
     GPE_CHECK_LAUNCH("k_scatter");
     return GPE_OK;
 }

@@ -202,6 +202,47 @@ def test_graph_replay_is_deterministic(gpe_mod, cuda_ok):
     assert np.array_equal(xa, xb) and np.array_equal(va, vb)
 
 
+@pytest.mark.parametrize("kind", ["dam", "batched"])
+def test_next_step_histogram_from_xsph(gpe_mod, cuda_ok, kind):
+    """Consecutive steps take their cell keys and histogram from the previous step's XSPH pass (one launch
+    fewer); every other call drops them and the next sort builds its own. Five steps give the same state bit
+    for bit whichever way they are split, with state round trips, field writes, density passes and the stage
+    API in between, and against the per-pass stages alone."""
+    p, pos, vel, dom, boxes = _scene(kind)
+
+    def run(plan):
+        e = _engine(gpe_mod, p, pos, vel, dom, boxes)
+        for op in plan:
+            if isinstance(op, int):
+                e.step(op)
+            elif op == "roundtrip":  # the engine's own state back in (its order is kept)
+                x, v, d = e.get_state()
+                e.set_state(x, v, d)
+            elif op == "field":      # a field write with the same values
+                e.set_field(gpe_mod.PBF_FIELD_VEL, e.get_state()[1])
+            elif op == "density":    # reads positions and cell starts only
+                e.density_error()
+            elif op == "stages":     # one step through the stage API
+                e.stage(gpe_mod.PBF_STAGE_PREDICT_SORT)
+                for _ in range(p.iters):
+                    e.stage(gpe_mod.PBF_STAGE_LAMBDA)
+                    e.stage(gpe_mod.PBF_STAGE_DELTA_P)
+                e.stage(gpe_mod.PBF_STAGE_XSPH)
+                e.stage(gpe_mod.PBF_STAGE_VORTICITY)
+                e.stage(gpe_mod.PBF_STAGE_FINISH)
+        x, v, d = e.get_state()
+        assert e.status() == 0
+        e.close()
+        return x, v
+
+    ref = run([5])
+    for plan in ([1, 1, 1, 1, 1], [2, "roundtrip", 3], [1, "field", 2, "density", 2], [2, "stages", 2],
+                 ["stages", 1, "stages", 1, 1]):
+        got = run(plan)
+        assert np.array_equal(ref[0].view(np.uint32), got[0].view(np.uint32)), f"positions differ for {plan}"
+        assert np.array_equal(ref[1].view(np.uint32), got[1].view(np.uint32)), f"velocities differ for {plan}"
+
+
 def test_batched_equals_solo_bit_exact(gpe_mod, cuda_ok):
     p, pos, vel, dom, boxes = _scene("batched")
     e = _engine(gpe_mod, p, pos, vel, dom, boxes)
