@@ -755,8 +755,10 @@ def run_gpe(args, rank, ws):
 
     # ---- stage-by-stage pass for the per-kernel roofline ----
     stage_ms = {k: [] for k in ALG_BYTES}
-    # the sort stage's launches: the step's, less one λ and one Δp per iteration and the XSPH pass
-    stage_launches = {"predict_sort": launches - 2 * p.iters - 1, "lambda": 1, "delta_p": 1, "xsph": 1}
+    # the sort stage's launches: the step's, less one λ and one Δp per iteration and the XSPH pass, plus the
+    # predict + histogram kernel that the stage API runs (inside a run of steps the previous XSPH does its work)
+    stage_launches = {"predict_sort": launches - 2 * p.iters - 1 + (1 if p.vort_eps == 0.0 else 0), "lambda": 1,
+                      "delta_p": 1, "xsph": 1}
     for _ in range(args.steps):
         flush_l2()
         seq = [("predict_sort", gpe.PBF_STAGE_PREDICT_SORT)]
