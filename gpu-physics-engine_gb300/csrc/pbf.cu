@@ -3067,9 +3067,11 @@ extern "C" int32_t gpe_pbf_enqueue(gpe_pbf* s, int32_t n_steps, void* stream)
         return GPE_ERR_NOT_READY;
     }
     cudaStream_t st   = as_stream(stream);
-    // the recorded sequence may be replayed after anything: it starts from the full sort and leaves no
-    // histogram behind (its last step's XSPH computes none)
+    // the recorded sequence may be replayed after anything (a step of this engine may have left a histogram
+    // in the array): it clears the histogram array, starts from the full sort and leaves no histogram behind
+    // (its last step's XSPH computes none)
     drop_hist(s);
+    s->count_dirty = true;
     int32_t rc    = GPE_OK;
     const int id0 = s->id_cur;
     for (int32_t k = 0; k < n_steps && rc == GPE_OK; ++k) { rc = run_step(s, st, k + 1 < n_steps); }
