@@ -207,7 +207,8 @@ def test_next_step_histogram_from_xsph(gpe_mod, cuda_ok, kind):
     """Consecutive steps take their cell keys and histogram from the previous step's XSPH pass (one launch
     fewer); every other call drops them and the next sort builds its own. Five steps give the same state bit
     for bit whichever way they are split, with state round trips, field writes, density passes and the stage
-    API in between, and against the per-pass stages alone."""
+    API and recorded-sequence calls (gpe_pbf_enqueue, here run eagerly) in between, and against the per-pass
+    stages alone."""
     p, pos, vel, dom, boxes = _scene(kind)
 
     def run(plan):
@@ -215,6 +216,8 @@ def test_next_step_histogram_from_xsph(gpe_mod, cuda_ok, kind):
         for op in plan:
             if isinstance(op, int):
                 e.step(op)
+            elif isinstance(op, tuple):  # ("enqueue", n)
+                e.enqueue(op[1])
             elif op == "roundtrip":  # the engine's own state back in (its order is kept)
                 x, v, d = e.get_state()
                 e.set_state(x, v, d)
@@ -237,7 +240,7 @@ def test_next_step_histogram_from_xsph(gpe_mod, cuda_ok, kind):
 
     ref = run([5])
     for plan in ([1, 1, 1, 1, 1], [2, "roundtrip", 3], [1, "field", 2, "density", 2], [2, "stages", 2],
-                 ["stages", 1, "stages", 1, 1]):
+                 ["stages", 1, "stages", 1, 1], [2, ("enqueue", 3)], [("enqueue", 2), 3], [1, ("enqueue", 1), 3]):
         got = run(plan)
         assert np.array_equal(ref[0].view(np.uint32), got[0].view(np.uint32)), f"positions differ for {plan}"
         assert np.array_equal(ref[1].view(np.uint32), got[1].view(np.uint32)), f"velocities differ for {plan}"
