@@ -609,14 +609,17 @@ def mpm_leg(args, stream, flush_l2):
             e.step(1, stream=sh)
             b.record(stream)
         torch.cuda.synchronize()
-        s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+        ms = [a.elapsed_time(b) for a, b in ev]
+        s = sum(ms) / 1e3
         st = e.status()
         launches = e.launches_per_step()
         e.close()
         gbs = alg_bytes * steps / s / 1e9
         return {"particles": n, "value": n * steps / s, "unit": "particle-steps/s", "steps": steps,
                 "sort_interval": p.sort_interval, "ms_per_step": 1e3 * s / steps, "alg_bytes_per_step": alg_bytes,
-                "effective_gbs": gbs, "hbm_frac": gbs / peak, "launches_per_step": launches, "status": st}
+                "effective_gbs": gbs, "hbm_frac": gbs / peak, "launches_per_step": launches, "status": st,
+                # the step that re-sorts is the slowest; the median is a step between re-sorts
+                "ms_step_median": float(np.median(ms)), "ms_step_max": max(ms)}
 
     out = {}
     n = 4194304
