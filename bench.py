@@ -734,8 +734,11 @@ def run_gpe(args, rank, ws):
 
     eng.set_state(pos, vel, stream=sh)
     # the engine's autotuner picks cell size, block size, persistent solve and mask skin for this scene (it
-    # restores the state afterwards); untimed. --no-autotune keeps the engine's default tuning (for profiler
-    # launch lists, which would otherwise fill with the tuner's trials)
+    # restores the state afterwards); untimed. Its trials run consecutive steps without an L2 flush, as a
+    # simulation loop does; the timed steps below flush L2 before each step, and under that protocol its
+    # choice can trail another candidate by about 1% (skin 0.1 h against 0.075 h at 1M particles).
+    # --no-autotune keeps the engine's default tuning (for profiler launch lists, which would otherwise fill
+    # with the tuner's trials)
     if args.no_autotune:
         best = eng.tuning()
     else:

@@ -376,8 +376,9 @@ int32_t gpe_pbf_get_tuning(const gpe_pbf* pbf, gpe_pbf_tuning* tuning);
 int32_t gpe_pbf_set_tuning(gpe_pbf* pbf, const gpe_pbf_tuning* tuning);
 /* Times trial_steps steps of every candidate (cell h with mask skin 0.1, 0.075 or 0.05 or without masks,
  * or h/2; block 128, 256 or 512; persistent 0, 1 or 2) on the current state, which is restored after every
- * trial and at the end, and applies the fastest;
- * *best and *ms_per_step receive it and its time (-1 when the choice came from the cache). Choices are
+ * trial and at the end; the three fastest run three more trials each, taking turns, and the one with the
+ * smallest median time is applied;
+ * *best and *ms_per_step receive it and that median (-1 when the choice came from the cache). Choices are
  * cached for the process per (scenes, particle count and mean scene aspect to the nearest power of two,
  * iterations, pair-direction flags). Needs GPE_WARM_NONE and a host particle count. */
 int32_t gpe_pbf_autotune(gpe_pbf* pbf, int32_t trial_steps, gpe_pbf_tuning* best, float* ms_per_step,
