@@ -526,7 +526,8 @@ def render_leg(args, stream, flush_l2, eng):
 def batched_leg(args, stream, flush_l2):
     """Batched PBF: 256 independent dam-break scenes, particle counts log-uniform in [2048, 65536] (seed 3),
     box aspect U(0.5, 2), C0 physics at dt = 1/480, 4 iterations, all scenes in one engine; timed with the
-    default tuning and with the autotuner's choice (cell size, block size, persistent solve)."""
+    default tuning, with the autotuner's choice (cell size, block size, persistent solve) and with the two
+    persistent forms at the chosen cell size, block size and mask skin."""
     import torch
 
     import gpe
@@ -558,9 +559,15 @@ def batched_leg(args, stream, flush_l2):
     best, trial_ms = e.autotune(trial_steps=4, stream=sh)
     tune_s = time.perf_counter() - t0
     tuned = timed()
+    # the persistent forms at the tuned cell, block and skin: all passes of a step in one cooperative launch
+    # (after the sort's launches), and the whole step in one
+    persistent = {}
+    for mode, name in ((1, "solve"), (2, "whole_step")):
+        e.set_tuning(cell=best.cell, block=best.block, persistent=mode, skin=best.skin)
+        persistent[name] = timed()
     e.close()
     return {"workload": "pbf_batched_256_scenes", "scenes": 256, "particles": n, "unit": "particle-steps/s",
-            "default": default, "tuned": tuned,
+            "default": default, "tuned": tuned, "persistent": persistent,
             "tuning": {"cell_over_h": best.cell / p.h, "block": best.block, "persistent": int(best.persistent),
                        "skin": round(best.skin, 3),
                        "trial_ms_per_step": trial_ms, "autotune_s": tune_s}}
