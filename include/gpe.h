@@ -361,7 +361,9 @@ typedef struct gpe_pbf_tuning {
                            otherwise launch-bound; vorticity keeps its own launches); 2: the predict +
                            cell sort runs inside that launch too (the sort strategy: its histogram,
                            scan, scatter and stable placement as phases between grid barriers instead of
-                           five launches), so a plain step is one launch; 0: one launch per pass       */
+                           five launches), so a plain step is one launch; 0: one launch per pass
+                           (on a GB300, 0 measured fastest for 16k and 1M particles and 256 scenes, by
+                           15-30%; the autotuner times all three)                                       */
     float skin;         /* candidate masks, in units of h, in [0, 1] (cell h only; default 0.075): the
                            first lambda pass of a step records per particle which candidates of its
                            3 x 3 cells lie within h + skin * h, and the later passes of the step visit
