@@ -51,6 +51,24 @@ def test_persistent_and_block_sizes_are_bit_exact(gpe_mod, cuda_ok, kind, block,
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_persistent_ticket_path_is_bit_exact(gpe_mod, cuda_ok, block):
+    """A scene with more blocks of particles than the persistent grid holds (262,144 particles: 2,048 blocks
+    of 128 against at most 12 resident a SM, and so on), so the persistent kernels hand blocks of particles
+    out from their ticket counter; the state after three steps equals the per-pass launches' bit for bit."""
+    from gpe import scenes
+
+    p = scenes.dam_params(iters=3)
+    p.dt = 1.0 / 480.0
+    pos, _, boxes = scenes.dam_break(n_side=512, box=10.24)
+    vel = np.random.default_rng(6).normal(0, 0.5, pos.shape).astype(np.float32)
+    ref = _run(gpe_mod, p, pos, vel, None, boxes, tuning=dict(block=256, persistent=0))
+    for persistent in (1, 2):
+        got = _run(gpe_mod, p, pos, vel, None, boxes, tuning=dict(block=block, persistent=persistent))
+        for a, b in zip(ref, got):
+            np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("kind", ["dam", "batched"])
 def test_whole_step_launch_keeps_sort_outputs(gpe_mod, cuda_ok, kind):
     """The whole-step kernel sorts inside the launch: after a step, the sort's keys, order and cell starts
