@@ -452,7 +452,9 @@ typedef struct gpe_mpm_params {
     float J_min, J_max;/* J clamp after the update (MPM.cu:265 uses 0.1, 10)                     */
     float E, nu;       /* Young's modulus and Poisson ratio (corotated / snow)                   */
     float theta_c, theta_s, hardening; /* snow plasticity (Stomakhin 2013)                       */
-    int32_t sort_interval; /* re-sort particles by cell every this many steps; 0 = never          */
+    int32_t sort_interval; /* re-sort particles by cell every this many steps; 0 = never. Within a
+                              cell the storage order is that of the sort's atomics (get_state
+                              returns the caller's order all the same)                       */
     uint32_t flags;    /* GPE_MPM_FLAG_*                                                         */
     float sand_h[4];   /* sand friction angle in degrees, phi = h0 + (h1 q - h3) exp(-h2 q) (Klar et al.
                           2016); all zero selects their (35, 9, 0.2, 10)                          */
