@@ -2,7 +2,8 @@
 candidates of its 3 x 3 cells lie within h + skin; the later passes of the step visit only those, and a
 particle whose neighbourhood has moved too far (or that left its sort cell) scans in full. Terms of pairs
 beyond h are exact zeros, so the state after any number of steps equals the full scans' bit for bit: in
-calm and violent scenes (the violent ones mark most neighbourhoods as moved), one scene or many, with and
+calm and violent scenes (the violent ones mark most neighbourhoods as moved), crowded ones (rows of more
+candidates than a mask word holds), one scene or many, with and
 without vorticity, the reference's pair-direction flags, the persistent solve, and the network warm start
 (whose memory-start step runs more iterations than the masks' move threshold allows for).
 """
@@ -21,6 +22,17 @@ def _scene(kind):
         pos, vel, boxes = scenes.dam_break(n_side=64)
         sd = 0.2 if kind == "calm" else 2.0
         vel = np.random.default_rng(3).normal(0, sd, pos.shape).astype(np.float32)
+        return p, pos, vel, None, boxes
+    if kind == "crowded":
+        # a block at 0.3 h spacing (about 11 particles a cell) beside one at the rest spacing 0.5 h: many of
+        # the dense block's 3-cell rows hold more than 31 candidates, more than a mask word, so those
+        # particles scan in full while the others use their masks
+        p = scenes.dam_params(iters=3)
+        p.dt = 1.0 / 480.0
+        dense, _, boxes = scenes.dam_break(n_side=48, spacing=0.006)
+        rest, _, _ = scenes.dam_break(n_side=48, seed=1)
+        pos = np.concatenate([dense, rest + np.float32(0.6)]).astype(np.float32)
+        vel = np.random.default_rng(5).normal(0, 0.2, pos.shape).astype(np.float32)
         return p, pos, vel, None, boxes
     if kind == "batched":
         p = scenes.dam_params(iters=2)
@@ -47,7 +59,7 @@ def _run(gpe_mod, p, pos, vel, dom, boxes, skin, steps=6, persistent=False, vort
     return x, v, d
 
 
-@pytest.mark.parametrize("kind", ["calm", "violent", "batched", "reference"])
+@pytest.mark.parametrize("kind", ["calm", "violent", "batched", "reference", "crowded"])
 @pytest.mark.parametrize("vort", [0.0, 5e-4])
 def test_masked_steps_equal_full_scans(gpe_mod, cuda_ok, kind, vort):
     p, pos, vel, dom, boxes = _scene(kind)
@@ -58,7 +70,7 @@ def test_masked_steps_equal_full_scans(gpe_mod, cuda_ok, kind, vort):
             np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("kind", ["calm", "violent", "batched"])
+@pytest.mark.parametrize("kind", ["calm", "violent", "batched", "crowded"])
 @pytest.mark.parametrize("iters", [1, 2, 5])
 def test_masked_persistent_solve_equals_full_scans(gpe_mod, cuda_ok, kind, iters):
     p, pos, vel, dom, boxes = _scene(kind)
