@@ -38,6 +38,14 @@ def _scene(kind):
         pos, vel, dom, boxes = scenes.batched_scenes(n_scenes=5, seed=9, lo=500, hi=3000)
         vel = np.random.default_rng(8).normal(0, 0.2, pos.shape).astype(np.float32)
         return p, pos, vel, dom, boxes
+    if kind == "coincident":
+        # the reference's block with every 40th atom doubled at the same position: distinct atoms at zero
+        # distance take the reference's pseudo-random pair direction (SELF_GRAD | PAIR_IDS)
+        p = scenes.reference_pbf_params(iters=2)
+        pos, vel, boxes = scenes.reference_pbf_block()
+        pos = np.concatenate([pos, pos[::40]]).astype(np.float32)
+        vel = np.concatenate([vel, vel[::40]]).astype(np.float32)
+        return p, pos, vel, None, boxes
     if kind == "vortex":
         p = scenes.dam_params(iters=2)
         p.vort_eps = 5e-4
@@ -51,7 +59,11 @@ def _scene(kind):
     raise ValueError(kind)
 
 
-KINDS = ["reference", "dam", "dam_half_cell", "batched", "vortex"]
+KINDS = ["reference", "dam", "dam_half_cell", "batched", "vortex", "coincident"]
+# A whole step of the coincident scene departs from the FP64 oracle by more than 1e-5 of scale near the
+# twins, as the reference's own FP32 kernels do (the gradient along the sliver by which the twins part is
+# ill-conditioned); test_reference_parity.py bounds that step by the reference kernels' error instead.
+STEP_KINDS = [k for k in KINDS if k != "coincident"]
 
 
 def _well_conditioned(kind, x, p):
@@ -162,7 +174,7 @@ def test_xsph_stage(gpe_mod, oracle, cuda_ok, kind):
         _close(got_v2[m], want_v2[m], np.abs(want_v2).max(), "vorticity velocity", rel=1e-5 + ulp_v / vscale)
 
 
-@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("kind", STEP_KINDS)
 def test_one_step(gpe_mod, oracle, cuda_ok, kind):
     p, pos, vel, dom, boxes = _scene(kind)
     e = _engine(gpe_mod, p, pos, vel, dom, boxes)

@@ -40,10 +40,12 @@ def _check_pbf(x_in, out_x, out_v, out_lam, ref_x, ref_v, ref_lam, who):
     _assert_close(out_lam, ref_lam, 1e-4 * np.abs(ref_lam).max(), f"{who} lambda")
 
 
-def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok):
+def _pbf_three_ways(gpe_mod, oracle, p, pos, vel, boxes):
+    """One substep stopped after XSPH by the reference's kernels, by the engine stage by stage through the C
+    ABI and by the oracle, all seeded with the reference's chunk slots as pair ids. Returns the start x*
+    (x + v + g) and (x*, v, lambda) of each in input order."""
     from oracle import refrun
 
-    p, pos, vel, boxes = _pbf_case()
     ref = refrun.RefPBF((12, 6), 320)
     _, slot = ref.seed(pos, vel, float(p.gravity[1]))
     ref.substep(iters=p.iters, full=False)
@@ -51,7 +53,6 @@ def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok)
     xs0 = pos + vel
     xs0[:, 1] += p.gravity[1]
 
-    # engine, stage by stage through the C ABI
     q = p.copy()
     q.flags |= gpe_mod.PBF_PAIR_IDS
     e = gpe_mod.Pbf(q, boxes, capacity=len(pos))
@@ -67,15 +68,45 @@ def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok)
     ex[perm] = e.field(gpe_mod.PBF_FIELD_PRED)
     ev[perm] = e.field(gpe_mod.PBF_FIELD_VEL)
     el[perm] = e.field(gpe_mod.PBF_FIELD_LAMBDA)
-    _check_pbf(xs0, ex, ev, el, rx, rv, rl, "engine")
+    e.close()
 
-    # oracle
     o = oracle.PbfOracle(p, boxes)
     r = o.step(pos, vel, None, 1, pair_id=slot.astype(np.uint32))
     operm = o.predict_sort(pos, vel)["perm"]
     ox, ov, ol = np.empty_like(pos), np.empty_like(pos), np.empty(len(pos), np.float32)
     ox[operm], ov[operm], ol[operm] = r["x"], r["v"], r["lam"]
-    _check_pbf(xs0, ox, ov, ol, rx, rv, rl, "oracle")
+    return xs0, (ex, ev, el), (ox, ov, ol), (rx, rv, rl)
+
+
+def test_pbf_substep_engine_and_oracle_match_reference(gpe_mod, oracle, cuda_ok):
+    p, pos, vel, boxes = _pbf_case()
+    xs0, eng, orc, ref = _pbf_three_ways(gpe_mod, oracle, p, pos, vel, boxes)
+    _check_pbf(xs0, *eng, *ref, "engine")
+    _check_pbf(xs0, *orc, *ref, "oracle")
+
+
+def test_pbf_coincident_atoms_within_the_reference_kernels_own_error(gpe_mod, oracle, cuda_ok):
+    """Every 40th atom of the block doubled at the same position. The reference gives a coincident pair a
+    pseudo-random gradient direction in lambdaKernel (pairDirection) and skips it in posCorrectionKernel, so
+    the twins take different multipliers, part by a sliver in the first correction, and the second
+    iteration's gradient along that sliver is ill-conditioned in FP32: near the twins an FP32 substep
+    departs from the FP64 oracle by more than 1e-5 of the field's scale. The engine's error against the
+    oracle (x*, v and lambda) must be within 1e-5 of scale or within the reference kernels' own error on the
+    same substep."""
+    p, pos, vel, boxes = _pbf_case()
+    pos = np.concatenate([pos, pos[::40]]).astype(np.float32)
+    vel = np.concatenate([vel, vel[::40]]).astype(np.float32)
+    xs0, eng, orc, ref = _pbf_three_ways(gpe_mod, oracle, p, pos, vel, boxes)
+    corr = np.abs(orc[0].astype(np.float64) - xs0).max()
+    for k, what, scale in ((0, "x*", corr), (1, "v", np.abs(orc[1]).max()), (2, "lambda", np.abs(orc[2]).max())):
+        o = orc[k].astype(np.float64)
+        e_err = np.abs(eng[k] - o)
+        r_err = np.abs(ref[k] - o)
+        if k == 0:  # positions: plus a few ulp of the coordinate, the reference's change of frame included
+            e_err = np.maximum(e_err - 8 * EPS32 * np.abs(o), 0.0)
+            r_err = np.maximum(r_err - 8 * EPS32 * np.abs(o), 0.0)
+        bound = max(1e-5 * scale, r_err.max())
+        assert e_err.max() <= bound, f"{what}: engine {e_err.max():.3e}, reference {r_err.max():.3e}, scale {scale:.3e}"
 
 
 def _engine_substep_then_sort(gpe_mod, p, pos, vel, slot, boxes):
